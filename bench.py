@@ -1,0 +1,351 @@
+"""Benchmark of the GB300 monodomain hot path (driver contract).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (one bench "step" = one whole solve on one GPU): fk_holes_1024 —
+Fenton-Karma 3V in FP32 on a 1024x1024 grid, 20,000 explicit Euler steps,
+300 circular holes (r ~ U[2,6] cells), 12 S2 patches of 40x40 at seeded
+positions and times ~ U[200,400] ms, seeded u ~ U(-0.01, 0.01), v = w = 1,
+S1 on columns 0-9 (synthetic: there is no dataset).
+
+Metric: Gcell-steps/s (1024^2 cells x 20,000 steps per solve). The state is
+re-initialised from a device copy at the start of every solve and a 256 MB
+buffer (> the 129 MB L2) is written between solves; within one solve the
+12.6 MB state stays resident in L2, which is the physical behaviour of this
+workload, so the HBM roofline fraction computed on algorithmic bytes can
+exceed 1 (see `roofline` and the ncu traffic).
+
+N > 1 (torchrun): every rank runs its own replica (the path does not shard);
+value = all ranks' cell-steps / the max time over ranks.
+
+--impl reference: the reference has no CPU implementation of this path; its
+step semantics are timed as the FP32 C/OpenMP transcription in oracle/ (the
+CPU restatement of the reference kernels), on all host cores, on a bounded
+sample of the same workload, same metric and unit.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gcell-steps/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(key):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/traffic.json), or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    v = d.get(key)
+    return None if v is None else float(v)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(wl, seconds=10.0):
+    """The FP32 C/OpenMP transcription of the step (oracle/, the CPU
+    restatement of the reference kernels) on all host cores: a bounded
+    sample of the workload's first steps, about `seconds` long."""
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    st = wl.state0()
+    steps, elapsed = 0, 0.0
+    n = 4
+    while elapsed < seconds:
+        t0 = time.perf_counter()
+        st = O.run(wl.p, wl.model, wl.fk, st, n, wl.stims, wl.solid,
+                   step0=steps, dtype=np.float32)
+        elapsed += time.perf_counter() - t0
+        steps += n
+        n = min(n * 2, 256)
+    value = wl.cells * steps / elapsed / 1e9
+    return {"value": round(value, 4), "unit": METRIC, "cores": cores,
+            "kind": "port",
+            "sample": "%s: first %d of %d steps (%dx%d with holes), FP32, "
+                      "OpenMP %d threads, %.1f s" % (
+                          wl.name, steps, wl.nsteps, wl.p.nx, wl.p.ny, cores,
+                          elapsed)}
+
+
+def config_of(wl, args, tb):
+    return {"workload": wl.name, "grid": [wl.p.nx, wl.p.ny],
+            "steps_per_solve": wl.nsteps, "model": "FK3V",
+            "holes": 300, "s2_patches": len(wl.stims),
+            "cells": wl.cells, "dt_ms": wl.p.dt, "dx_cm": wl.p.hx,
+            "time_block": tb,
+            "l2": "256 MB write between solves; 12.6 MB state L2-resident within a solve",
+            "parallelism": "replicas x%d" % args.gpus}
+
+
+def run_reference(args, wl):
+    rank = env_int("RANK", 0)
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    sample_steps = 64
+    st0 = wl.state0()
+    times = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        O.run(wl.p, wl.model, wl.fk, st0, sample_steps, wl.stims, wl.solid,
+              dtype=np.float32)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    value = wl.cells * sample_steps * len(times) / total / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4),
+        "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * total / len(times), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": config_of(wl, args, 1),
+        "cpu_baseline": {
+            "value": round(value, 4), "unit": METRIC, "cores": cores,
+            "kind": "port",
+            "sample": "each step: first %d steps of %s on the host cores, FP32 "
+                      "C/OpenMP transcription of the reference step "
+                      "(the reference has no CPU path)" % (sample_steps, wl.name)},
+        "e2e": {"value": round(value, 4), "unit": METRIC,
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--time-block", type=int, default=0,
+                    help="steps per kernel launch (0: library default)")
+    ap.add_argument("--nsteps", type=int, default=20000,
+                    help="explicit steps per solve (the workload's 20,000)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    from yolohtli_gb300 import workloads as W
+    wl = W.fk_holes_1024(seed=0, nsteps=args.nsteps)
+
+    if args.impl == "reference":
+        run_reference(args, wl)
+        return
+
+    import torch
+    rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
+    local = env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from yolohtli_gb300 import _abi as A
+    from yolohtli_gb300.solver import Monodomain
+
+    stream = torch.cuda.Stream()
+    m = Monodomain(wl.p, wl.model, wl.fk, solid=wl.solid, stream=stream.cuda_stream)
+    tb = args.time_block if args.time_block > 0 else 1
+    m.set_time_block(tb)
+    ic = [torch.tensor(x, device="cuda") for x in wl.state0()]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    lib = m.lib
+
+    # One handle serves every solve (a fresh handle would re-upload the mask):
+    # its step counter keeps running, so the stimulus schedule is shifted by
+    # the steps already taken; each solve re-initialises the state from the
+    # device copy of the initial condition.
+    base = [0]
+
+    def solve_shifted():
+        stims = []
+        for s in wl.stims:
+            q = A.Stim()
+            q.step, q.i0, q.j0, q.i1, q.j1, q.value = (
+                s.step + base[0], s.i0, s.j0, s.i1, s.j1, s.value)
+            stims.append(q)
+        lib.yh_set_state(m.h, *[C.c_void_p(t.data_ptr()) for t in ic])
+        m.run(wl.nsteps, stims)
+        base[0] += wl.nsteps
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            solve_shifted()
+            flush.fill_(1.0)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
+        launches0 = m.launch_count()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for k in range(args.steps):
+            solve_shifted()
+            if k + 1 < args.steps:
+                flush.fill_(1.0)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        launches = m.launch_count() - launches0
+        ms = ev0.elapsed_time(ev1)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+
+    t = torch.tensor([ms], device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    cell_steps = wl.cells * wl.nsteps * args.steps * world
+    value = cell_steps / (ms_max * 1e-3) / 1e9
+
+    # dominant kernel: the RD step; per launch `tb` steps of all cells
+    rd_launches = args.steps * (-(-wl.nsteps // tb) if tb > 1 else wl.nsteps)
+    avg_launch_s = ms * 1e-3 / rd_launches  # upper bound: includes stim kernels and gaps
+    bytes_alg = 25.0 * wl.cells * tb      # u,v,w read+write FP32 + 1-byte mask
+    achieved = bytes_alg / avg_launch_s / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = profiled_traffic("rd_fk3v_holes_1024_tb%d" % tb)
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": traffic, "peak_kind": peak_kind,
+                "alg_bytes_per_cell_step": 25,
+                "note": "achieved = 25 B x cells x steps-per-launch / mean launch "
+                        "time over the timed region; state L2-resident"}
+
+    # end to end through the public C ABI with pinned host buffers
+    e2e = None
+    if rank == 0 or world > 1:
+        hst = [torch.tensor(x).pin_memory() for x in wl.state0()]
+        out_u = torch.empty(wl.cells, dtype=torch.float32).pin_memory()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            stims = []
+            for s in wl.stims:
+                q = A.Stim()
+                q.step, q.i0, q.j0, q.i1, q.j1, q.value = (
+                    s.step + base[0], s.i0, s.j0, s.i1, s.j1, s.value)
+                stims.append(q)
+            lib.yh_set_state(m.h, *[C.c_void_p(x.data_ptr()) for x in hst])
+            m.run(wl.nsteps, stims)
+            base[0] += wl.nsteps
+            lib.yh_get_state(m.h, C.c_void_p(out_u.data_ptr()), None, None)
+        e2e_s = time.perf_counter() - t0
+        et = torch.tensor([e2e_s], device="cuda")
+        if dist:
+            dist.all_reduce(et, op=dist.ReduceOp.MAX)
+        e2e = {"value": round(cell_steps / float(et.item()) / 1e9, 3),
+               "unit": METRIC, "h2d_bytes_per_step": 3 * 4 * wl.cells,
+               "d2h_bytes_per_step": 4 * wl.cells}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(wl)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": METRIC,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms_max / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": config_of(wl, args, tb),
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    m.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

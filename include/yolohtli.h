@@ -1,0 +1,366 @@
+/*
+ * yolohtli_gb300 — C ABI of the GB300 (sm_103a) monodomain hot path.
+ *
+ * One shared library, libyolohtli_gb300.so, exports everything declared here.
+ * Every entry point is `extern "C"`, takes plain pointers, sizes and POD structs,
+ * returns an int status (YH_OK = 0, negative = YH_E*), never calls exit(), and
+ * launches asynchronously on the cudaStream_t passed as `void *stream`
+ * (NULL = the legacy default stream, as the reference uses).
+ *
+ * Two layers:
+ *   1. Stateless operators on caller-owned device buffers. Each one replaces
+ *      one host wrapper of the reference (hostPrototypes.h:22-42); the
+ *      comment above each declaration names it.
+ *   2. A solver handle that owns the buffers and runs whole protocols
+ *      (plain steps, stimulus events, symmetry-reduced steps) inside CUDA
+ *      graphs without host round trips.
+ *
+ * Fields are FP32 structure-of-arrays, row-major, idx = i + nx*j, exactly the
+ * reference's I2D layout (typeDefinition.cuh:129). The reference stores
+ * FP64 (typeDefinition.cuh:4); the FP64 drop-in for its own symbols is in
+ * yolohtli_compat.h.
+ *
+ * Threading: a handle is not thread-safe; use one handle per host thread /
+ * stream. Stateless operators are reentrant.
+ */
+#ifndef YOLOHTLI_GB300_H
+#define YOLOHTLI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Status codes                                                         */
+/* ------------------------------------------------------------------ */
+enum {
+  YH_OK = 0,
+  YH_EINVAL = -1,        /* bad argument (null pointer, size, flag)          */
+  YH_ECUDA = -2,         /* a CUDA runtime call failed                       */
+  YH_ENOMEM = -3,        /* device or host allocation failed                 */
+  YH_ESINGULAR = -4,     /* 3x3 drift/rotation system singular (|pivot|<tol) */
+  YH_ENONFINITE = -5,    /* NaN or Inf in the state                          */
+  YH_EOVERFLOW = -6,     /* tip buffer full; extra tips were dropped         */
+  YH_EUNSUPPORTED = -7,  /* option off this path: RK2/RK4, lap4, anisotropy,
+                            Dirichlet boundaries                             */
+  YH_ENOTREADY = -8      /* call order (e.g. yh_sr_step before yh_sr_begin)  */
+};
+
+enum { YH_MODEL_REF2V = 0,   /* the reference's 2-variable cubic model
+                                (reactionDiffusion.cu:131-141)               */
+       YH_MODEL_FK3V = 1 };  /* Fenton-Karma 3-variable model (1998)        */
+
+enum { YH_TEMPLATE_CURRENT = 0,  /* template re-taken from the state every step,
+                                    as the reference does (symmetryReduction.cu:184-205) */
+       YH_TEMPLATE_FROZEN = 1 }; /* template derivatives taken once from a given state */
+
+/* ------------------------------------------------------------------ */
+/* ABI structs                                                          */
+/* ------------------------------------------------------------------ */
+
+/* CUDA's int2/float2 are 8-byte aligned; these mirror them in plain C. */
+typedef struct yh_int2 { int x, y; } __attribute__((aligned(8))) yh_int2;
+typedef struct yh_float2 { float x, y; } __attribute__((aligned(8))) yh_float2;
+
+/* Field-for-field the reference's paramVar (typeDefinition.cuh:35-125):
+ * same order, same types (REAL = double), so a reference driver can hand its
+ * `param` to this library unchanged. The fields this path reads are:
+ * nx, ny, hx, hy, dt, rx, ry, rscale, tc, invdx, invdy, alpha..theta, Uth,
+ * tipOffsetX/Y, tipx/tipy, solidSwitch, neumannBC, gateDiff, anisotropy,
+ * lap4, timeIntOrder, tipAlgorithm. */
+typedef struct yh_param_var {
+  bool animate;
+  bool saveEveryIt;
+  bool plotTip;
+  bool recordTip;
+  bool plotContour;
+  bool recordContour;
+  bool stimulate;
+  bool apdContour;
+  bool plotTimeSeries;
+  bool recordTimeSeries;
+  bool reduceSym;
+  bool reduceSymStart;
+  bool clock, counterclock;
+  bool firstIterTip, firstIterContour;
+  bool firstFPS;
+
+  bool solidSwitch;
+  bool neumannBC;
+  bool gateDiff;
+  bool anisotropy;
+  bool tipGrad;
+  int lap4;
+  int contourMode;
+  int timeIntOrder;
+  int tipAlgorithm;
+
+  bool load;
+  bool save;
+
+  int nx;
+  int ny;
+  int memSize;
+  double Lx, Ly, hx, hy;
+  double dt;
+  double diff_par, diff_per;
+  double Dxx, Dyy, Dxy;
+  double rx, ry, rxy, rbx, rby;
+  double rscale;
+  double invdx, invdy;
+  double sample;
+  int count;
+  double physicalTime, physicalTimeLim;
+  int startRecTime;
+  double stimPeriod;
+  double stimDuration;
+  double stimMag;
+  bool fibThreshold;
+  bool fibTerminated;
+  int leapShocks;
+  int eSize;
+  yh_int2 point;
+  int nc;
+  double rdomTrapz, rdomStim, rdomAPD;
+  double stcx, stcy;
+  yh_float2 pointStim;
+  int savePackage;
+  float tiempo;
+  double degrad;
+  double boundaryVal;
+  double qx4, qy4, fx4, fy4;
+
+  int itPerFrame;
+  int tipOffsetX;
+  int tipOffsetY;
+  float minVarColor;
+  float maxVarColor;
+
+  int wnx;
+  int wny;
+  float uMax;
+  float uMin;
+  float vMax;
+  float vMin;
+
+  float tipx;
+  float tipy;
+
+  double contourThresh1, contourThresh2, contourThresh3;
+  double Uth;
+  double tc;
+  double alpha;
+  double beta;
+  double gamma;
+  double delta;
+  double eps;
+  double mu;
+  double theta;
+} yh_param_var;
+
+/* Fenton-Karma (1998) parameters, times in ms, potentials dimensionless.
+ * Not in the reference (it has only the 2-variable model). */
+typedef struct yh_fk_params {
+  double tau_d, tau_r, tau_si, tau_0;
+  double tau_v_plus, tau_v1_minus, tau_v2_minus;
+  double tau_w_plus, tau_w_minus;
+  double u_c, u_v, u_csi, k;
+} yh_fk_params;
+
+/* A tip point: the reference's vec5dyn (typeDefinition.cuh:19-20). */
+typedef struct yh_tip { float x, y, vx, vy, t; } yh_tip;
+
+/* Device pointers of one FP32 state: the reference's stateVar
+ * (typeDefinition.cuh:7-9) plus the third FK variable w (NULL for REF2V). */
+typedef struct yh_fields { float *u, *v, *w; } yh_fields;
+
+/* Symmetry-reduction state, kept in DEVICE memory by the operators below.
+ * c and phi are the reference's REAL3 c, phi (main.cu:60); integrals is its
+ * `REAL *integrals` (main.cu:220), in the same order I0..I11
+ * (integralTrapz.cu:97-179). */
+typedef struct yh_sym_state {
+  double c[3];          /* cx, cy, ctheta of the last solve                 */
+  double phi[3];        /* phi_x, phi_y, phi_theta (integrated frame)       */
+  double c_adv[3];      /* c used for the advection field of the last BFECC */
+  double phi_adv[3];    /* phi used for the same                            */
+  double integrals[12];
+  float centre[2];      /* disc centre of the phase integrals (cells)       */
+  int step;             /* steps taken (the reference's param.count)        */
+  int status;           /* YH_OK or YH_ESINGULAR from the last solve        */
+  int ntips;            /* tips found by the last tip pass                  */
+  int pad_;
+} yh_sym_state;
+
+/* A stimulus event of a protocol: u = value on tissue cells of the box
+ * [i0,i1) x [j0,j1), applied before step `step` is taken. */
+typedef struct yh_stim { int step; int i0, j0, i1, j1; float value; } yh_stim;
+
+/* ------------------------------------------------------------------ */
+/* Parameter helpers                                                    */
+/* ------------------------------------------------------------------ */
+
+/* The reference's defaults (saveFiles.cu:105-231) for an nx x ny grid, with
+ * derived coefficients as main.cu:148-158 computes them (dt not halved). */
+int yh_param_defaults(yh_param_var *p, int nx, int ny);
+/* Recompute rx, ry, invdx, invdy, ... from dt, hx, hy, Dxx, Dyy. */
+int yh_param_derive(yh_param_var *p);
+/* Fenton-Karma BR-fit parameter set. */
+int yh_fk_defaults(yh_fk_params *fk);
+const char *yh_status_string(int status);
+const char *yh_version(void);
+/* sizeof of an ABI struct by name ("yh_param_var", "yh_fk_params",
+ * "yh_tip", "yh_fields", "yh_sym_state", "yh_stim"); 0 if unknown. */
+size_t yh_sizeof(const char *type_name);
+
+/* ------------------------------------------------------------------ */
+/* Layer 1: stateless operators on caller-owned device buffers         */
+/* ------------------------------------------------------------------ */
+
+/* One explicit Euler reaction-diffusion step, out <- in, with the 5-point
+ * mirror (no-flux) Laplacian, hole coefficients when p->solidSwitch, and the
+ * state tangent vel_tan = (out - in)/dt when vel_tan.u != NULL.
+ * Replaces reactionDiffusion_wrapper (hostPrototypes.h:22-25,
+ * reactionDiffusion.cu:568-577). `solid` is nx*ny bytes, nonzero = tissue. */
+int yh_reaction_diffusion(const yh_param_var *p, int model,
+                          const yh_fk_params *fk, yh_fields out, yh_fields in,
+                          yh_fields vel_tan, const uint8_t *solid,
+                          void *stream);
+
+/* Spiral-tip detection by the closed-form bilinear isoline intersection
+ * (algorithm 1). Resets *tip_count to 0, then appends every tip found between
+ * the time levels g_past and g_present (u fields) at time `physical_time`.
+ * Replaces tip_wrapper (hostPrototypes.h:26-28, tipTracker.cu:569-611).
+ * tip_count and tip_vector are device pointers; at most `capacity` tips are
+ * stored, *tip_count keeps the full number found. */
+int yh_spiral_tip(const yh_param_var *p, const float *g_past,
+                  const float *g_present, double physical_time,
+                  int *tip_count, yh_tip *tip_vector, int capacity,
+                  const uint8_t *solid, void *stream);
+
+/* Chooses the disc centre of the phase integrals from the tips found: the
+ * tip nearest to the previous centre (sym->centre); unchanged if no tip.
+ * The reference takes the last tip pushed (symmetryReduction.cu:102-103),
+ * whose order is not deterministic. */
+int yh_pick_centre(const int *tip_count, const yh_tip *tip_vector,
+                   int capacity, yh_sym_state *sym, void *stream);
+
+/* Workspace bytes needed by yh_phase_integrals for this grid (any disc
+ * radius). The workspace holds a completion counter that must be zero before
+ * the first call; every call leaves it at zero again. */
+size_t yh_phase_integrals_workspace(int nx, int ny);
+
+/* Fused slice + phase-condition integrals + FP64 3x3 solve:
+ *  - current-state derivatives (2nd-order one-sided, upwinded by the sign of
+ *    the comoving field adv_x_rows[j], adv_y_cols[i], 0 off tissue),
+ *  - template derivatives (negated 4th-order central of `state` when
+ *    templ_x.u == NULL, else the stored template fields templ_x/y/t),
+ *  - the 12 integrals over the open disc of radius^2 tipOffsetX*tipOffsetY
+ *    around sym->centre, accumulated in FP64, deterministic two-level sum,
+ *  - the FP64 3x3 solve with partial pivoting, rotated by sym->phi[2]:
+ *    sym->c, sym->integrals, sym->status; then sym->c_adv = c,
+ *    sym->phi_adv = phi.
+ * Replaces slice_wrapper + trapz_wrapper + solve_matrix
+ * (hostPrototypes.h:30-33,39-42; symmetryReduction.cu:72-222,329-420;
+ * integralTrapz.cu:17-184). `workspace`: device memory of at least
+ * yh_phase_integrals_workspace(nx, ny) bytes. */
+int yh_phase_integrals(const yh_param_var *p, int model, yh_fields state,
+                       yh_fields vel_tan, yh_fields templ_x,
+                       yh_fields templ_y, yh_fields templ_t,
+                       const double *adv_x_rows, const double *adv_y_cols,
+                       const uint8_t *solid, yh_sym_state *sym,
+                       void *workspace, void *stream);
+
+/* Template derivative fields (negated 4th-order central, as the reference's
+ * convCentral2X/Y, symmetryReduction.cu:224-240) of a state over the whole
+ * grid; used to freeze a template. */
+int yh_template_slices(const yh_param_var *p, int model, yh_fields state,
+                       yh_fields templ_x, yh_fields templ_y,
+                       yh_fields templ_t, void *stream);
+
+/* The comoving field of (sym->c_adv, sym->phi_adv). It is separable:
+ * adv.x = hy*j*ct - cx*cos(pt) + cy*sin(pt) depends on the row j only and
+ * adv.y = -hx*i*ct - cx*sin(pt) - cy*cos(pt) on the column i only, so it is
+ * written as adv_x_rows[ny] and adv_y_cols[nx] in FP64 (and FP32 copies when
+ * the _f32 pointers are not NULL). With advance_phi != 0 it then applies
+ * phi += dt*c, step += 1 (main.cu:936-952).
+ * Replaces Cxy_field_wrapper (hostPrototypes.h:34-35,
+ * symmetryReduction.cu:20-70). */
+int yh_comoving_field(const yh_param_var *p, yh_sym_state *sym,
+                      double *adv_x_rows, double *adv_y_cols,
+                      float *adv_x_rows_f32, float *adv_y_cols_f32,
+                      int advance_phi, void *stream);
+
+/* BFECC advection out <- in by the comoving field (FP32 row/column vectors
+ * of yh_comoving_field), as three race-free passes through the caller's
+ * scratch fields uf and ue.
+ * Replaces advFDBFECC_wrapper (hostPrototypes.h:36-38, advFDBFECC.cu:18-362). */
+int yh_advect_bfecc(const yh_param_var *p, int model, yh_fields out,
+                    yh_fields in, const float *adv_x_rows_f32,
+                    const float *adv_y_cols_f32, const uint8_t *solid,
+                    yh_fields uf, yh_fields ue, void *stream);
+
+/* phi += dt * c and step += 1 on the device (main.cu:935-952). */
+int yh_sym_advance(const yh_param_var *p, yh_sym_state *sym, void *stream);
+
+/* u = value on tissue cells of [i0,i1) x [j0,j1). */
+int yh_stimulate_box(const yh_param_var *p, float *u, const uint8_t *solid,
+                     int i0, int j0, int i1, int j1, float value,
+                     void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Layer 2: solver handle                                               */
+/* ------------------------------------------------------------------ */
+typedef struct yh_solver yh_solver;
+
+/* Copies the parameters, uploads the hole mask (NULL = no holes) and
+ * allocates the device state. The state starts at zero. */
+int yh_create(const yh_param_var *p, int model, const yh_fk_params *fk,
+              const uint8_t *solid_host, void *stream, yh_solver **out);
+int yh_destroy(yh_solver *h);
+int yh_synchronize(yh_solver *h);
+
+/* Copies into / out of the current state; the pointers may be host (pinned
+ * or pageable) or device memory. NULL pointers are skipped. */
+int yh_set_state(yh_solver *h, const float *u, const float *v, const float *w);
+int yh_get_state(yh_solver *h, float *u, float *v, float *w);
+/* Device pointers of the current state (valid until the next step). */
+int yh_state_device(yh_solver *h, yh_fields *cur);
+
+/* Steps per kernel launch of the plain solver (temporal blocking depth);
+ * 1 = one launch per step. Values are clamped to what the kernel supports. */
+int yh_set_time_block(yh_solver *h, int steps_per_launch);
+
+/* nsteps plain explicit steps with the stimulus events of `stims` whose step
+ * lies in [h.step, h.step + nsteps), captured and replayed as a CUDA graph. */
+int yh_run(yh_solver *h, int nsteps, const yh_stim *stims, int nstims);
+
+/* Tip detection between the current state and the previous time level
+ * (plain mode: x = new u, y = old u, main.cu:963). */
+int yh_track_tips(yh_solver *h);
+int yh_get_tips(yh_solver *h, yh_tip *out, int capacity, int *n);
+
+/* Symmetry reduction (main.cu:894-954). template_mode YH_TEMPLATE_FROZEN
+ * takes the template from the host state (tu, tv, tw); CURRENT ignores it. */
+int yh_sr_begin(yh_solver *h, int template_mode, const float *tu,
+                const float *tv, const float *tw);
+int yh_sr_step(yh_solver *h, int nsteps);
+int yh_get_sym(yh_solver *h, yh_sym_state *out);
+
+/* Steps taken so far. */
+int yh_get_step(yh_solver *h, int *step);
+
+/* Kernel launches this handle has performed so far (graph replays count
+ * every kernel node they run). */
+int yh_get_launch_count(yh_solver *h, long long *n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* YOLOHTLI_GB300_H */

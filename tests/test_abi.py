@@ -1,0 +1,93 @@
+"""The C ABI: the library loads, exports every symbol the headers declare,
+and its structs match the reference's layout (CPU only, no compute calls)."""
+import ctypes as C
+import json
+import os
+import re
+
+import numpy as np
+
+from yolohtli_gb300 import _abi as A
+from yolohtli_gb300 import load
+
+from conftest import GOLDEN, ROOT
+
+
+def declared(header):
+    src = open(os.path.join(ROOT, "include", header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(yh_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_loads_and_exports_all_declared_symbols():
+    lib = load()
+    names = declared("yolohtli.h")
+    assert len(names) > 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert missing == []
+
+
+def test_struct_sizes_match_ctypes():
+    lib = load()
+    for name, ct in [("yh_param_var", A.ParamVar), ("yh_fk_params", A.FKParams),
+                     ("yh_tip", A.Tip), ("yh_fields", A.Fields),
+                     ("yh_sym_state", A.SymState), ("yh_stim", A.Stim)]:
+        assert lib.yh_sizeof(name.encode()) == C.sizeof(ct), name
+
+
+def test_param_layout_is_the_references_paramVar():
+    ref = json.load(open(os.path.join(GOLDEN, "paramvar_layout.json")))
+    assert ref["sizeof"] == C.sizeof(A.ParamVar)
+    for name, off in ref["offsets"].items():
+        assert getattr(A.ParamVar, name).offset == off, name
+    assert set(ref["offsets"]) == set(A.PARAM_FIELD_NAMES)
+
+
+def test_param_defaults_match_reference_parameterSetup(golden_host):
+    ref = A.ParamVar()
+    raw = golden_host["param_bytes"].tobytes()
+    C.memmove(C.byref(ref), raw, C.sizeof(ref))
+    lib = load()
+    p = A.ParamVar()
+    assert lib.yh_param_defaults(C.byref(p), ref.nx, ref.ny) == 0
+    # this path runs Euler / 5-point (the reference defaults to RK4 / lap4)
+    assert (ref.timeIntOrder, ref.lap4) == (4, 4)
+    assert (p.timeIntOrder, p.lap4) == (1, 0)
+    for name in A.PARAM_FIELD_NAMES:
+        # memSize is set later by main.cu:213, not by parameterSetup
+        if name in ("timeIntOrder", "lap4", "point", "pointStim", "memSize"):
+            continue
+        a, b = getattr(p, name), getattr(ref, name)
+        if isinstance(a, float):
+            assert a == b or abs(a - b) <= 1e-15 * abs(b), name
+        else:
+            assert a == b, name
+    assert (p.point.x, p.point.y) == (ref.point.x, ref.point.y)
+    q = A.param_defaults(ref.nx, ref.ny)
+    assert bytes(q) == bytes(p)
+
+
+def test_status_strings_and_fk_defaults():
+    lib = load()
+    assert lib.yh_status_string(A.YH_ESINGULAR) == b"singular drift/rotation system"
+    fk = A.FKParams()
+    assert lib.yh_fk_defaults(C.byref(fk)) == 0
+    assert bytes(fk) == bytes(A.fk_defaults())
+
+
+def test_invalid_arguments_are_rejected_without_a_gpu():
+    lib = load()
+    p = A.param_defaults(64, 64)
+    h = C.c_void_p()
+    fk = A.fk_defaults()
+    assert lib.yh_create(C.byref(p), 7, C.byref(fk), None, None, C.byref(h)) == A.YH_EINVAL
+    q = p.copy()
+    q.timeIntOrder = 4
+    assert lib.yh_create(C.byref(q), 0, None, None, None, C.byref(h)) == A.YH_EUNSUPPORTED
+    q = p.copy()
+    q.nx = 2
+    assert lib.yh_create(C.byref(q), 0, None, None, None, C.byref(h)) == A.YH_EINVAL
+    q = p.copy()
+    q.solidSwitch = True  # holes requested without a mask
+    assert lib.yh_create(C.byref(q), 0, None, None, None, C.byref(h)) == A.YH_EINVAL
+    assert lib.yh_create(C.byref(p), 1, None, None, None, C.byref(h)) == A.YH_EINVAL

@@ -1,0 +1,128 @@
+"""GPU parity of the explicit reaction-diffusion step (FP32 product kernels)
+against the FP64 oracle, through the C ABI."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from yolohtli_gb300 import _abi as A
+from yolohtli_gb300 import ops
+from yolohtli_gb300 import workloads as W
+from yolohtli_gb300.solver import Monodomain
+
+from gpu_util import dev, host, max_abs, rel_l2, smooth_state
+
+pytestmark = pytest.mark.gpu
+
+
+def params(model, nx, ny):
+    if model == A.YH_MODEL_FK3V:
+        return A.fk_tissue_params(nx, ny), A.fk_defaults()
+    return A.param_defaults(nx, ny), None
+
+
+# (64, 48): float4 path; (37, 29): scalar path (nx % 4 != 0)
+@pytest.mark.parametrize("nx,ny", [(64, 48), (37, 29)])
+@pytest.mark.parametrize("model", [A.YH_MODEL_REF2V, A.YH_MODEL_FK3V])
+@pytest.mark.parametrize("holes", [False, True])
+def test_one_step_matches_oracle(nx, ny, model, holes):
+    import torch
+    p, fk = params(model, nx, ny)
+    nf = A.NFIELDS[model]
+    st = smooth_state(nx, ny, 5, nf)
+    solid = None
+    if holes:
+        solid = W.hole_mask(nx, ny, 5, 1.5, 3.0, np.random.default_rng(3))
+        p.solidSwitch = True
+    want, wtan = O.rd_step(p, model, fk, st, solid=solid, tangent=True)
+    inp = [dev(x) for x in st]
+    out = [torch.zeros_like(inp[0]) for _ in range(nf)]
+    tan = [torch.zeros_like(inp[0]) for _ in range(nf)]
+    ops.reaction_diffusion(p, model, fk, out, inp, tan,
+                           None if solid is None else dev(solid, torch.uint8))
+    torch.cuda.synchronize()
+    for f in range(nf):
+        # FP32 rounding of O(1) values
+        assert max_abs(host(out[f]), want[f]) < 2e-6, f
+        scale = max(np.abs(wtan[f]).max(), 1e-3)
+        assert max_abs(host(tan[f]), wtan[f]) / scale < 2e-5, f
+
+
+def test_vec4_and_scalar_paths_agree():
+    import torch
+    p, fk = params(A.YH_MODEL_FK3V, 64, 48)
+    st = smooth_state(64, 48, 7, 3)
+    inp = [dev(x) for x in st]
+    a = [torch.zeros_like(inp[0]) for _ in range(3)]
+    b = [torch.zeros_like(inp[0]) for _ in range(3)]
+    ops.reaction_diffusion(p, A.YH_MODEL_FK3V, fk, a, inp)
+    # a misaligned view forces the scalar kernel
+    big = [torch.zeros(64 * 48 + 1, device="cuda") for _ in range(3)]
+    inp2 = [t[1:] for t in big]
+    for s, d in zip(inp, inp2):
+        d.copy_(s)
+    ops.reaction_diffusion(p, A.YH_MODEL_FK3V, fk, b, inp2)
+    torch.cuda.synchronize()
+    for f in range(3):
+        assert max_abs(host(a[f]), host(b[f])) <= 1e-7
+
+
+def test_handle_protocol_matches_oracle_and_is_deterministic():
+    """FK3V spiral protocol (S1 + S2, 256x256 scaled down to 128x128) through
+    the solver handle (graph replay) against the FP64 oracle."""
+    wl = W.fk_spiral_256(seed=0, n=128, nsteps=1500)
+    # S2 at step 1000 on the lower-left quadrant
+    wl.stims[0].step = 1000
+    res = []
+    for _ in range(2):
+        m = Monodomain(wl.p, wl.model, wl.fk)
+        m.set_state(*wl.state0())
+        m.run(wl.nsteps, wl.stims)
+        res.append(m.get_state())
+        assert m.step_count() == wl.nsteps
+        m.close()
+    for f in range(3):
+        assert np.array_equal(res[0][f], res[1][f])  # bitwise run-to-run
+    ref = O.run(wl.p, wl.model, wl.fk, wl.state0(), wl.nsteps, wl.stims)
+    err = rel_l2(res[0][0], ref[0])
+    print("FK3V 128^2 x 1500 steps: rel L2(u) FP32 vs FP64 oracle = %.3e" % err)
+    assert err < 1e-4
+
+
+@pytest.mark.parametrize("nsteps", [1, 63, 64, 200])
+def test_handle_step_counts_and_ping_pong(nsteps):
+    p, fk = params(A.YH_MODEL_REF2V, 48, 40)
+    st = smooth_state(48, 40, 1, 2)
+    m = Monodomain(p, A.YH_MODEL_REF2V, None)
+    m.set_state(*st)
+    m.run(nsteps)
+    got = m.get_state()
+    ref = O.run(p, A.YH_MODEL_REF2V, None, st, nsteps)
+    assert max_abs(got[0], ref[0]) < 1e-5
+    assert m.step_count() == nsteps
+
+
+def test_handle_with_holes_matches_oracle():
+    wl = W.fk_holes_1024(seed=1, n=128, nsteps=400, nholes=20, npatch=3)
+    for s in wl.stims:
+        s.step = s.step % 300
+    m = Monodomain(wl.p, wl.model, wl.fk, solid=wl.solid)
+    m.set_state(*wl.state0())
+    m.run(wl.nsteps, wl.stims)
+    got = m.get_state()
+    ref = O.run(wl.p, wl.model, wl.fk, wl.state0(), wl.nsteps, wl.stims,
+                solid=wl.solid)
+    assert rel_l2(got[0], ref[0]) < 1e-5
+    assert np.all(got[0][wl.solid == 0] == 0)
+
+
+def test_stimulate_box_clips_and_respects_holes():
+    import torch
+    p = A.param_defaults(32, 32)
+    p.solidSwitch = True
+    solid = np.ones(32 * 32, np.uint8)
+    solid[5 * 32 + 5] = 0
+    u = torch.zeros(32 * 32, device="cuda")
+    ops.stimulate_box(p, u, -3, -3, 8, 8, 1.0, dev(solid, torch.uint8))
+    torch.cuda.synchronize()
+    g = host(u).reshape(32, 32)
+    assert g[:8, :8].sum() == 63 and g[5, 5] == 0 and g[8:, :].sum() == 0

@@ -1,0 +1,195 @@
+"""The reference's own CUDA kernels, run headless on the GPU (oracle/refgpu),
+against the oracle (pinning it) and against the FP32 product kernels.
+
+The reference computes in FP64, the product in FP32: the FP32 error against
+the reference is reported as a function of the number of steps and bounded
+by the tolerance stated in each test."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from oracle import refgpu as R
+from yolohtli_gb300 import _abi as A
+from yolohtli_gb300 import ops
+from yolohtli_gb300 import workloads as W
+from yolohtli_gb300.solver import Monodomain
+
+from gpu_util import dev, host, max_abs, rel_l2, smooth_state, tips_match
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(not R.available(),
+                                 reason="reference cubin not built (oracle/ref_build.sh)")]
+
+
+def ref_run(p, st, steps, solid=None):
+    import torch
+    a = [dev(x, torch.float64) for x in st]
+    b = [torch.zeros_like(a[0]) for _ in range(2)]
+    J = [torch.zeros_like(a[0]) for _ in range(2)]
+    vt = [torch.zeros_like(a[0]) for _ in range(2)]
+    sol = None if solid is None else dev(solid, torch.uint8)
+    R.set_params(p)
+    for _ in range(steps):
+        R.rd(p, b, a, J, vt, sol)
+        a, b = b, a
+    R.sync()
+    return [host(t) for t in a], [host(t) for t in vt]
+
+
+def cross_params(n, L=3.0):
+    p = A.param_defaults(n, n)
+    p.Lx = p.Ly = L
+    p.hx = p.hy = L / (n - 1)
+    return A.param_derive(p)
+
+
+@pytest.mark.parametrize("holes", [False, True])
+def test_reference_rd_pins_oracle(holes):
+    n = 96
+    p = cross_params(n)
+    st = list(W.ref2v_cross(n, n))
+    solid = None
+    if holes:
+        p.solidSwitch = True
+        solid = W.hole_mask(n, n, 8, 2.0, 4.0, np.random.default_rng(7))
+    ref, rt = ref_run(p, st, 300, solid)
+    orc = st
+    for _ in range(300):
+        orc, ot = O.rd_step(p, A.YH_MODEL_REF2V, None, orc, solid=solid, tangent=True)
+    assert rel_l2(orc[0], ref[0]) < 1e-12
+    assert rel_l2(orc[1], ref[1]) < 1e-12
+    assert rel_l2(ot[0], rt[0]) < 1e-10
+
+
+def test_product_fp32_against_reference_fp64_error_vs_steps():
+    """REF2V from the reference's own initial condition: relative L2 error of
+    u (FP32 product vs FP64 reference) after N steps."""
+    n = 128
+    p = cross_params(n)
+    st = list(W.ref2v_cross(n, n))
+    errs = {}
+    for N in (1, 10, 100, 1000):
+        ref, _ = ref_run(p, st, N)
+        m = Monodomain(p, A.YH_MODEL_REF2V, None)
+        m.set_state(*st)
+        m.run(N)
+        got = m.get_state()
+        m.close()
+        errs[N] = rel_l2(got[0], ref[0])
+    print("REF2V 128^2 rel L2(u) FP32 vs reference FP64:",
+          {k: "%.2e" % v for k, v in errs.items()})
+    assert errs[1] < 1e-7
+    assert errs[100] < 1e-6
+    assert errs[1000] < 1e-5
+
+
+def test_reference_tips_match_product():
+    import torch
+    nx, ny = 96, 80
+    p = A.param_defaults(nx, ny)
+    jj, ii = np.mgrid[0:ny, 0:nx]
+    x, y = ii - nx / 2 + 0.3, jj - ny / 2 - 0.2
+    f = lambda t: (0.5 + 0.5 * np.cos(np.arctan2(y, x) - 0.35 * np.hypot(x, y) - t)).ravel()
+    past = f(0.0).astype(np.float32).astype(np.float64)
+    present = f(0.3).astype(np.float32).astype(np.float64)
+    R.set_params(p)
+    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    vec = torch.zeros(5 * 4096, dtype=torch.float32, device="cuda")
+    plot = torch.zeros(nx * ny, dtype=torch.uint8, device="cuda")
+    R.tip(p, dev(past, torch.float64), dev(present, torch.float64), plot, cnt, vec, 1.0)
+    R.sync()
+    nr = int(cnt.item())
+    ref = host(vec)[: 5 * nr].reshape(nr, 5)
+    cnt2 = torch.zeros(1, dtype=torch.int32, device="cuda")
+    vec2 = torch.zeros(5 * 4096, dtype=torch.float32, device="cuda")
+    ops.spiral_tip(p, dev(past), dev(present), cnt2, vec2, 4096, 1.0)
+    torch.cuda.synchronize()
+    ng = int(cnt2.item())
+    got = host(vec2)[: 5 * ng].reshape(ng, 5)
+    assert nr >= 1
+    assert tips_match(got, ref, 1e-4)
+
+
+def test_reference_slices_and_trapz_match_product_phase_integrals():
+    import torch
+    nx, ny = 96, 80
+    p = A.param_defaults(nx, ny)
+    p.tipOffsetX = p.tipOffsetY = 25
+    st = [x.astype(np.float32).astype(np.float64) for x in smooth_state(nx, ny, 3, 2)]
+    tan = [x.astype(np.float32).astype(np.float64) for x in smooth_state(nx, ny, 4, 2)]
+    c_adv, phi_adv = (0.011, -0.02, 0.004), (0.0, 0.0, 0.6)
+    tip = (41.3, 37.8)
+    # reference: Cxy -> slice -> 12 x trapz around tip_vector[count-1]
+    R.set_params(p)
+    ax = torch.zeros(nx * ny, dtype=torch.float64, device="cuda")
+    ay = torch.zeros_like(ax)
+    R.cxy(p, ax, ay, c_adv, phi_adv)
+    slc = [torch.zeros_like(ax) for _ in range(6)]
+    slc0 = [torch.zeros_like(ax) for _ in range(6)]
+    tipv = torch.tensor([tip[0], tip[1], 0, 0, 0], dtype=torch.float32, device="cuda")
+    cnt = torch.ones(1, dtype=torch.int32, device="cuda")
+    intgl = torch.zeros(nx * ny, dtype=torch.uint8, device="cuda")
+    g = [dev(x, torch.float64) for x in st]
+    R.slice_(p, g, slc, slc0, ax, ay, intgl, cnt, tipv, 5)
+    R.sync()
+    Iref = R.integrals(p, slc, slc0, [dev(x, torch.float64) for x in tan], cnt, tipv, 5)
+    # product: one fused launch
+    s = A.SymState()
+    for k in range(3):
+        s.c_adv[k], s.phi_adv[k] = c_adv[k], phi_adv[k]
+    s.centre[0], s.centre[1] = tip
+    s.step = 5
+    sym = ops.sym_to_tensor(s)
+    ar = torch.zeros(ny, dtype=torch.float64, device="cuda")
+    ac = torch.zeros(nx, dtype=torch.float64, device="cuda")
+    ops.comoving_field(p, sym, ar, ac)
+    ws = torch.zeros(ops.phase_workspace_bytes(nx, ny), dtype=torch.uint8, device="cuda")
+    ops.phase_integrals(p, A.YH_MODEL_REF2V, [dev(x) for x in st],
+                        [dev(x) for x in tan], ar, ac, sym, ws)
+    torch.cuda.synchronize()
+    got = np.array(ops.sym_from_bytes(sym).integrals[:])
+    assert np.abs(got - Iref).max() <= 2e-6 * np.abs(Iref).max()
+
+
+def test_reference_bfecc_fixed_point_matches_product():
+    import torch
+    nx, ny = 64, 52
+    p = A.param_defaults(nx, ny)
+    p.dt = 0.01
+    A.param_derive(p)
+    st = [x.astype(np.float32).astype(np.float64) for x in smooth_state(nx, ny, 5, 2)]
+    c, phi = (1.3, -0.7, 0.02), (0.0, 0.0, 0.4)
+    R.set_params(p)
+    ax = torch.zeros(nx * ny, dtype=torch.float64, device="cuda")
+    ay = torch.zeros_like(ax)
+    R.cxy(p, ax, ay, c, phi)
+    gin = [dev(x, torch.float64) for x in st]
+    gout = [torch.zeros_like(ax) for _ in range(2)]
+    uf = [torch.zeros_like(ax) for _ in range(2)]
+    ub = [torch.zeros_like(ax) for _ in range(2)]
+    ue = [torch.zeros_like(ax) for _ in range(2)]
+    outs = []
+    for _ in range(4):
+        R.bfecc(p, gout, gin, ax, ay, uf, ub, ue)
+        R.sync()
+        outs.append(host(gout[0]).copy())
+    race = max_abs(outs[0], outs[2])
+    print("reference BFECC: single-launch deviation from its fixed point %.2e" % race)
+    assert np.array_equal(outs[2], outs[3])  # fixed point reached
+    s = A.SymState()
+    for k in range(3):
+        s.c_adv[k], s.phi_adv[k] = c[k], phi[k]
+    sym = ops.sym_to_tensor(s)
+    ar = torch.zeros(ny, dtype=torch.float64, device="cuda")
+    ac = torch.zeros(nx, dtype=torch.float64, device="cuda")
+    arf = torch.zeros(ny, device="cuda")
+    acf = torch.zeros(nx, device="cuda")
+    ops.comoving_field(p, sym, ar, ac, arf, acf)
+    inp = [dev(x) for x in st]
+    out = [torch.zeros_like(inp[0]) for _ in range(2)]
+    sf = [torch.zeros_like(inp[0]) for _ in range(2)]
+    se = [torch.zeros_like(inp[0]) for _ in range(2)]
+    ops.advect_bfecc(p, A.YH_MODEL_REF2V, out, inp, arf, acf, sf, se)
+    torch.cuda.synchronize()
+    assert max_abs(host(out[0]), outs[3]) < 2e-6
+    assert max_abs(host(out[1]), host(gout[1])) < 2e-6

@@ -1,0 +1,60 @@
+"""ctypes signatures of every function exported by libyolohtli_gb300.so
+(include/yolohtli.h)."""
+import ctypes as C
+
+from . import _abi as A
+
+_P = C.POINTER
+_v = C.c_void_p
+_i = C.c_int
+_d = C.c_double
+_f = C.c_float
+
+SIGNATURES = {
+    # parameter helpers
+    "yh_param_defaults": (_i, [_P(A.ParamVar), _i, _i]),
+    "yh_param_derive": (_i, [_P(A.ParamVar)]),
+    "yh_fk_defaults": (_i, [_P(A.FKParams)]),
+    "yh_status_string": (C.c_char_p, [_i]),
+    "yh_version": (C.c_char_p, []),
+    "yh_sizeof": (C.c_size_t, [C.c_char_p]),
+    # stateless operators
+    "yh_reaction_diffusion": (_i, [_P(A.ParamVar), _i, _P(A.FKParams), A.Fields,
+                                   A.Fields, A.Fields, _v, _v]),
+    "yh_spiral_tip": (_i, [_P(A.ParamVar), _v, _v, _d, _v, _v, _i, _v, _v]),
+    "yh_pick_centre": (_i, [_v, _v, _i, _v, _v]),
+    "yh_phase_integrals_workspace": (C.c_size_t, [_i, _i]),
+    "yh_phase_integrals": (_i, [_P(A.ParamVar), _i, A.Fields, A.Fields,
+                                A.Fields, A.Fields, A.Fields, _v, _v, _v, _v,
+                                _v, _v]),
+    "yh_template_slices": (_i, [_P(A.ParamVar), _i, A.Fields, A.Fields,
+                                A.Fields, A.Fields, _v]),
+    "yh_comoving_field": (_i, [_P(A.ParamVar), _v, _v, _v, _v, _v, _i, _v]),
+    "yh_advect_bfecc": (_i, [_P(A.ParamVar), _i, A.Fields, A.Fields, _v, _v,
+                             _v, A.Fields, A.Fields, _v]),
+    "yh_sym_advance": (_i, [_P(A.ParamVar), _v, _v]),
+    "yh_stimulate_box": (_i, [_P(A.ParamVar), _v, _v, _i, _i, _i, _i, _f, _v]),
+    # solver handle
+    "yh_create": (_i, [_P(A.ParamVar), _i, _P(A.FKParams), _v, _v, _P(_v)]),
+    "yh_destroy": (_i, [_v]),
+    "yh_synchronize": (_i, [_v]),
+    "yh_set_state": (_i, [_v, _v, _v, _v]),
+    "yh_get_state": (_i, [_v, _v, _v, _v]),
+    "yh_state_device": (_i, [_v, _P(A.Fields)]),
+    "yh_set_time_block": (_i, [_v, _i]),
+    "yh_run": (_i, [_v, _i, _P(A.Stim), _i]),
+    "yh_track_tips": (_i, [_v]),
+    "yh_get_tips": (_i, [_v, _P(A.Tip), _i, _P(_i)]),
+    "yh_sr_begin": (_i, [_v, _i, _v, _v, _v]),
+    "yh_sr_step": (_i, [_v, _i]),
+    "yh_get_sym": (_i, [_v, _P(A.SymState)]),
+    "yh_get_step": (_i, [_v, _P(_i)]),
+    "yh_get_launch_count": (_i, [_v, _P(C.c_longlong)]),
+}
+
+
+def declare(lib):
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args

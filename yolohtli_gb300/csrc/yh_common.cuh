@@ -1,0 +1,120 @@
+// Shared device definitions of the yolohtli_gb300 kernels (sm_103a).
+//
+// Fields are structure-of-arrays, row-major, idx = i + nx*j (the reference's
+// I2D, typeDefinition.cuh:129). Every kernel is a template on the element
+// type `Real`: float is the product path; double instantiates the same code
+// for the FP64 drop-in of the reference's own symbols (yh_compat.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/yolohtli.h"
+
+namespace yh {
+
+// Maximum number of state variables of any model (FK3V: u, v, w).
+constexpr int kMaxFields = 3;
+
+template <typename Real>
+struct Fld {
+  Real *f[kMaxFields];
+};
+
+template <typename Real>
+__host__ __device__ inline Fld<Real> make_fld(Real *u, Real *v, Real *w) {
+  Fld<Real> r;
+  r.f[0] = u;
+  r.f[1] = v;
+  r.f[2] = w;
+  return r;
+}
+
+// Mirror index about the edge cell, coord_i/coord_j of the reference
+// (helper_functions.cu:69-79), valid for -2 <= i <= n+1 and n >= 3.
+__host__ __device__ __forceinline__ int mirror(int i, int n) {
+  return i < 0 ? -i : (i >= n ? 2 * (n - 1) - i : i);
+}
+
+// Coefficients of one explicit step, computed on the host from the
+// parameter struct and passed by value (the reference keeps them in
+// process-global __constant__ memory, main.cu:40-51, which rules out
+// several grids or parameter sets in one process).
+template <typename Real>
+struct StepCoeffs {
+  int nx, ny;
+  int model;       // YH_MODEL_*
+  int gate_diff;   // REF2V: v diffuses with rscale
+  Real rx, ry, rscale, dt, tc, inv_dt;
+  // REF2V (reactionDiffusion.cu:131-141)
+  Real mu, alpha, eps, delta, gamma, beta, theta;
+  // FK3V (Fenton & Karma 1998) with reciprocals precomputed
+  Real u_c, u_v, u_csi;
+  Real k_exp2;      // -2*k*log2(e): 1 + tanh(k x) = 2/(1 + 2^(k_exp2 x))
+  Real inv_td, inv_tr, inv_to, inv_tsi, inv_tvp, inv_tv1m, inv_tv2m;
+  Real inv_twp, inv_twm;
+};
+
+// Hole coefficients along one axis (reactionDiffusion.cu:162-169):
+// weights (lo, centre, hi) for the neighbours on each side. Equivalent to a
+// mirror ghost at a hole face and no flux through a cell with holes on both
+// sides.
+template <typename Real>
+__device__ __forceinline__ void hole_coeffs(bool lo, bool c, bool hi,
+                                            Real &wlo, Real &wc, Real &whi) {
+  wlo = (lo && hi) && (lo && c) ? Real(1) : ((lo && c) ? Real(2) : Real(0));
+  wc = c ? ((lo || hi) ? Real(2) : Real(0)) : Real(0);
+  whi = (lo && hi) && (c && hi) ? Real(1) : ((c && hi) ? Real(2) : Real(0));
+}
+
+// Reaction right-hand sides (multiplied by dt where the reference does):
+//   REF2V: ru = -dt*I_sum, rv = -dt*I_v (reactionDiffusion.cu:131-141,498-499)
+//   FK3V:  ru = -dt*J_ion, rv = dt*dv/dt, rw = dt*dw/dt
+template <typename Real>
+__device__ __forceinline__ void ref2v_currents(const StepCoeffs<Real> &a,
+                                               Real u, Real v, Real &I_sum,
+                                               Real &I_v) {
+  I_sum = -(a.mu * u * (Real(1) - u) * (u - a.alpha) - u * v);
+  I_v = -(a.eps * (a.delta * (u - a.gamma) * (a.beta - u) - v - a.theta));
+}
+
+__device__ __forceinline__ float fk_sigmoid(const StepCoeffs<float> &a,
+                                            float u) {
+  // (1 + tanh(k (u - u_csi))) / 2 = 1 / (1 + exp(-2k (u - u_csi)))
+  return __frcp_rn(1.0f + exp2f(a.k_exp2 * (u - a.u_csi)));
+}
+__device__ __forceinline__ double fk_sigmoid(const StepCoeffs<double> &a,
+                                             double u) {
+  return 1.0 / (1.0 + exp2(a.k_exp2 * (u - a.u_csi)));
+}
+
+// FK3V: ionic current J and gate rates (Fenton & Karma 1998, eqs. 2-6).
+template <typename Real>
+__device__ __forceinline__ void fk3v_rates(const StepCoeffs<Real> &a, Real u,
+                                           Real v, Real w, Real &J, Real &gv,
+                                           Real &gw) {
+  const bool p = u >= a.u_c;
+  const bool q = u >= a.u_v;
+  const Real jfi = p ? -v * (Real(1) - u) * (u - a.u_c) * a.inv_td : Real(0);
+  const Real jso = p ? a.inv_tr : u * a.inv_to;
+  const Real jsi = -w * fk_sigmoid(a, u) * a.inv_tsi;
+  J = jfi + jso + jsi;
+  const Real itvm = q ? a.inv_tv1m : a.inv_tv2m;
+  gv = p ? -v * a.inv_tvp : (Real(1) - v) * itvm;
+  gw = p ? -w * a.inv_twp : (Real(1) - w) * a.inv_twm;
+}
+
+// Parameters of the symmetry-reduction kernels.
+template <typename Real>
+struct SymCoeffs {
+  int nx, ny;
+  int nf;
+  int r2;          // tipOffsetX*tipOffsetY: disc radius squared (cells)
+  int box;         // side of the disc's bounding box (cells)
+  Real hx, hy, invdx, invdy, dt, tc;
+  Real Rx_scale, Ry_scale;  // dt/hx, dt/hy
+  double hxhy;
+  double Uth;
+};
+
+}  // namespace yh

@@ -1,0 +1,305 @@
+// Explicit Euler reaction-diffusion step (the reference's
+// reactionDiffusion_kernel, reactionDiffusion.cu:26-566, on its Euler /
+// Neumann / 5-point path) and the stimulus box.
+//
+// rd_step_scalar: one cell per thread, any nx; also the FP64 instance.
+// rd_step_vec4:   FP32, four cells per thread with float4 loads/stores of
+//                 the centre row and of the rows above and below (nx % 4 == 0).
+// Both read the inputs through the read-only path and write every output
+// exactly once (the reference rewrites g_in in place, reactionDiffusion.cu:117-118,508-509).
+#include "yh_kernels.cuh"
+
+namespace yh {
+
+template <int MODEL, typename Real>
+__device__ __forceinline__ void reaction(const StepCoeffs<Real> &a, Real u,
+                                         Real v, Real w, Real du, Real dv,
+                                         Real r[kMaxFields]) {
+  if (MODEL == YH_MODEL_REF2V) {
+    Real I_sum, I_v;
+    ref2v_currents(a, u, v, I_sum, I_v);
+    du -= a.dt * I_sum;
+    dv -= a.dt * I_v;
+    r[0] = du;
+    r[1] = dv;
+    r[2] = Real(0);
+  } else {
+    Real J, gv, gw;
+    fk3v_rates(a, u, v, w, J, gv, gw);
+    r[0] = du - a.dt * J;
+    r[1] = a.dt * gv;
+    r[2] = a.dt * gw;
+  }
+}
+
+// velTan = rhs/dt (reactionDiffusion.cu:529-530): a division in FP64 as the
+// reference does it, a multiplication by 1/dt in FP32.
+__device__ __forceinline__ double tangent(const StepCoeffs<double> &a,
+                                          double r) {
+  return r / a.dt;
+}
+__device__ __forceinline__ float tangent(const StepCoeffs<float> &a, float r) {
+  return r * a.inv_dt;
+}
+
+template <int MODEL, typename Real, bool HOLES, bool TAN>
+__global__ void __launch_bounds__(256)
+    rd_step_scalar(const StepCoeffs<Real> a, const Fld<Real> in,
+                   const Fld<Real> out, const Fld<Real> tan,
+                   const uint8_t *__restrict__ solid) {
+  constexpr int NF = MODEL == YH_MODEL_FK3V ? 3 : 2;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.nx, ny = a.ny;
+  if (i >= nx || j >= ny) return;
+  const int C = i + nx * j;
+  const int W = mirror(i - 1, nx) + nx * j;
+  const int E = mirror(i + 1, nx) + nx * j;
+  const int S = i + nx * mirror(j - 1, ny);
+  const int N = i + nx * mirror(j + 1, ny);
+  const Real *__restrict__ U = in.f[0];
+  const Real *__restrict__ V = in.f[1];
+  const Real u = __ldg(U + C), v = __ldg(V + C);
+  const Real w = NF > 2 ? __ldg(in.f[2] + C) : Real(0);
+  bool sc = true;
+  Real du, dv = Real(0);
+  if (HOLES) {
+    sc = solid[C] != 0;
+    Real cxw, cxc, cxe, cyn, cyc, cys;
+    hole_coeffs(solid[W] != 0, sc, solid[E] != 0, cxw, cxc, cxe);
+    hole_coeffs(solid[N] != 0, sc, solid[S] != 0, cyn, cyc, cys);
+    du = (cxw * __ldg(U + W) - cxc * u + cxe * __ldg(U + E)) * a.rx +
+         (cyn * __ldg(U + N) - cyc * u + cys * __ldg(U + S)) * a.ry;
+    if (MODEL == YH_MODEL_REF2V && a.gate_diff)
+      dv = (cxw * __ldg(V + W) - cxc * v + cxe * __ldg(V + E)) * a.rx *
+               a.rscale +
+           (cyn * __ldg(V + N) - cyc * v + cys * __ldg(V + S)) * a.ry *
+               a.rscale;
+  } else {
+    du = (__ldg(U + W) - Real(2) * u + __ldg(U + E)) * a.rx +
+         (__ldg(U + N) - Real(2) * u + __ldg(U + S)) * a.ry;
+    if (MODEL == YH_MODEL_REF2V && a.gate_diff)
+      dv = (__ldg(V + W) - Real(2) * v + __ldg(V + E)) * a.rx * a.rscale +
+           (__ldg(V + N) - Real(2) * v + __ldg(V + S)) * a.ry * a.rscale;
+  }
+  Real r[kMaxFields];
+  reaction<MODEL>(a, u, v, w, du, dv, r);
+  const Real x0[3] = {u, v, w};
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    out.f[f][C] = sc ? x0[f] + a.tc * r[f] : Real(0);
+    if (TAN) tan.f[f][C] = sc ? tangent(a, r[f]) : Real(0);
+  }
+}
+
+// FP32 fast path: thread (tx, j) owns cells 4*tx .. 4*tx+3 of row j.
+template <int MODEL, bool HOLES, bool TAN>
+__global__ void __launch_bounds__(256)
+    rd_step_vec4(const StepCoeffs<float> a, const Fld<float> in,
+                 const Fld<float> out, const Fld<float> tan,
+                 const uint8_t *__restrict__ solid) {
+  constexpr int NF = MODEL == YH_MODEL_FK3V ? 3 : 2;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;  // float4 column
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.nx, ny = a.ny, nq = nx >> 2;
+  if (q >= nq || j >= ny) return;
+  const int i0 = q << 2;
+  const int row = nx * j;
+  const int rowS = nx * mirror(j - 1, ny);
+  const int rowN = nx * mirror(j + 1, ny);
+  const int iw = mirror(i0 - 1, nx), ie = mirror(i0 + 4, nx);
+  const float *__restrict__ U = in.f[0];
+  const float4 uc = __ldg(reinterpret_cast<const float4 *>(U + row + i0));
+  const float4 un = __ldg(reinterpret_cast<const float4 *>(U + rowN + i0));
+  const float4 us = __ldg(reinterpret_cast<const float4 *>(U + rowS + i0));
+  const float uw = __ldg(U + row + iw), ue = __ldg(U + row + ie);
+  float4 fv[NF];
+#pragma unroll
+  for (int f = 1; f < NF; ++f)
+    fv[f] = __ldg(reinterpret_cast<const float4 *>(in.f[f] + row + i0));
+  fv[0] = uc;
+  float4 vn, vs;
+  float vw = 0.f, ve = 0.f;
+  const bool vdiff = MODEL == YH_MODEL_REF2V && a.gate_diff;
+  if (vdiff) {
+    const float *__restrict__ V = in.f[1];
+    vn = __ldg(reinterpret_cast<const float4 *>(V + rowN + i0));
+    vs = __ldg(reinterpret_cast<const float4 *>(V + rowS + i0));
+    vw = __ldg(V + row + iw);
+    ve = __ldg(V + row + ie);
+  }
+  uchar4 mc, mn, ms;
+  uint8_t mw = 1, me = 1;
+  if (HOLES) {
+    mc = *reinterpret_cast<const uchar4 *>(solid + row + i0);
+    mn = *reinterpret_cast<const uchar4 *>(solid + rowN + i0);
+    ms = *reinterpret_cast<const uchar4 *>(solid + rowS + i0);
+    mw = solid[row + iw];
+    me = solid[row + ie];
+  }
+  const float ucv[4] = {uc.x, uc.y, uc.z, uc.w};
+  const float unv[4] = {un.x, un.y, un.z, un.w};
+  const float usv[4] = {us.x, us.y, us.z, us.w};
+  float res[NF][4], tres[NF][4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float u = ucv[k];
+    const float uW = k == 0 ? uw : ucv[k - 1];
+    const float uE = k == 3 ? ue : ucv[k + 1];
+    float x[3];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      const float4 t = fv[f];
+      x[f] = k == 0 ? t.x : (k == 1 ? t.y : (k == 2 ? t.z : t.w));
+    }
+    if (NF < 3) x[2] = 0.f;
+    bool sc = true;
+    float du, dv = 0.f;
+    if (HOLES) {
+      const uint8_t c8[4] = {mc.x, mc.y, mc.z, mc.w};
+      const uint8_t n8[4] = {mn.x, mn.y, mn.z, mn.w};
+      const uint8_t s8[4] = {ms.x, ms.y, ms.z, ms.w};
+      sc = c8[k] != 0;
+      const bool sw = (k == 0 ? mw : c8[k - 1]) != 0;
+      const bool se = (k == 3 ? me : c8[k + 1]) != 0;
+      float cxw, cxc, cxe, cyn, cyc, cys;
+      hole_coeffs(sw, sc, se, cxw, cxc, cxe);
+      hole_coeffs(n8[k] != 0, sc, s8[k] != 0, cyn, cyc, cys);
+      du = (cxw * uW - cxc * u + cxe * uE) * a.rx +
+           (cyn * unv[k] - cyc * u + cys * usv[k]) * a.ry;
+      if (vdiff) {
+        const float4 vc = fv[1];
+        const float vcv[4] = {vc.x, vc.y, vc.z, vc.w};
+        const float vnv[4] = {vn.x, vn.y, vn.z, vn.w};
+        const float vsv[4] = {vs.x, vs.y, vs.z, vs.w};
+        const float vW = k == 0 ? vw : vcv[k - 1];
+        const float vE = k == 3 ? ve : vcv[k + 1];
+        dv = (cxw * vW - cxc * vcv[k] + cxe * vE) * a.rx * a.rscale +
+             (cyn * vnv[k] - cyc * vcv[k] + cys * vsv[k]) * a.ry * a.rscale;
+      }
+    } else {
+      du = (uW - 2.f * u + uE) * a.rx + (unv[k] - 2.f * u + usv[k]) * a.ry;
+      if (vdiff) {
+        const float4 vc = fv[1];
+        const float vcv[4] = {vc.x, vc.y, vc.z, vc.w};
+        const float vnv[4] = {vn.x, vn.y, vn.z, vn.w};
+        const float vsv[4] = {vs.x, vs.y, vs.z, vs.w};
+        const float vW = k == 0 ? vw : vcv[k - 1];
+        const float vE = k == 3 ? ve : vcv[k + 1];
+        dv = (vW - 2.f * vcv[k] + vE) * a.rx * a.rscale +
+             (vnv[k] - 2.f * vcv[k] + vsv[k]) * a.ry * a.rscale;
+      }
+    }
+    float r[kMaxFields];
+    reaction<MODEL>(a, x[0], x[1], x[2], du, dv, r);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      res[f][k] = sc ? x[f] + a.tc * r[f] : 0.f;
+      if (TAN) tres[f][k] = sc ? tangent(a, r[f]) : 0.f;
+    }
+  }
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    *reinterpret_cast<float4 *>(out.f[f] + row + i0) =
+        make_float4(res[f][0], res[f][1], res[f][2], res[f][3]);
+    if (TAN)
+      *reinterpret_cast<float4 *>(tan.f[f] + row + i0) =
+          make_float4(tres[f][0], tres[f][1], tres[f][2], tres[f][3]);
+  }
+}
+
+template <typename Real>
+__global__ void stimulate_box_kernel(Real *u, const uint8_t *solid, int nx,
+                                     int i0, int j0, int i1, int j1,
+                                     Real value) {
+  const int i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = j0 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= i1 || j >= j1) return;
+  const int C = i + nx * j;
+  if (!solid || solid[C]) u[C] = value;
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+
+template <int MODEL, typename Real, bool HOLES, bool TAN>
+static cudaError_t launch_rd_t(const StepCoeffs<Real> &a, const Fld<Real> &in,
+                               const Fld<Real> &out, const Fld<Real> &tan,
+                               const uint8_t *solid, cudaStream_t s) {
+  if constexpr (std::is_same<Real, float>::value) {
+    if ((a.nx % 4) == 0 && aligned16(in, MODEL) && aligned16(out, MODEL) &&
+        (!TAN || aligned16(tan, MODEL)) &&
+        (!HOLES || (reinterpret_cast<uintptr_t>(solid) & 3) == 0)) {
+      const dim3 block(64, 4);
+      const dim3 grid((a.nx / 4 + block.x - 1) / block.x,
+                      (a.ny + block.y - 1) / block.y);
+      rd_step_vec4<MODEL, HOLES, TAN>
+          <<<grid, block, 0, s>>>(a, in, out, tan, solid);
+      return cudaGetLastError();
+    }
+  }
+  {
+    const dim3 block(32, 8);
+    const dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8);
+    rd_step_scalar<MODEL, Real, HOLES, TAN>
+        <<<grid, block, 0, s>>>(a, in, out, tan, solid);
+  }
+  return cudaGetLastError();
+}
+
+template <typename Real>
+cudaError_t launch_rd_step(const StepCoeffs<Real> &a, const Fld<Real> &in,
+                           const Fld<Real> &out, const Fld<Real> &tan,
+                           const uint8_t *solid, cudaStream_t s) {
+  const bool holes = solid != nullptr;
+  const bool t = tan.f[0] != nullptr;
+#define YH_RD_CASE(M, H, T)                                             \
+  if (a.model == M && holes == H && t == T)                             \
+    return launch_rd_t<M, Real, H, T>(a, in, out, tan, solid, s);
+  YH_RD_CASE(YH_MODEL_REF2V, false, false)
+  YH_RD_CASE(YH_MODEL_REF2V, false, true)
+  YH_RD_CASE(YH_MODEL_REF2V, true, false)
+  YH_RD_CASE(YH_MODEL_REF2V, true, true)
+  YH_RD_CASE(YH_MODEL_FK3V, false, false)
+  YH_RD_CASE(YH_MODEL_FK3V, false, true)
+  YH_RD_CASE(YH_MODEL_FK3V, true, false)
+  YH_RD_CASE(YH_MODEL_FK3V, true, true)
+#undef YH_RD_CASE
+  return cudaErrorInvalidValue;
+}
+
+template <typename Real>
+cudaError_t launch_stimulate(Real *u, const uint8_t *solid, int nx, int ny,
+                             int i0, int j0, int i1, int j1, Real value,
+                             cudaStream_t s) {
+  i0 = i0 < 0 ? 0 : i0;
+  j0 = j0 < 0 ? 0 : j0;
+  i1 = i1 > nx ? nx : i1;
+  j1 = j1 > ny ? ny : j1;
+  if (i1 <= i0 || j1 <= j0) return cudaSuccess;
+  const dim3 block(32, 8);
+  const dim3 grid((i1 - i0 + 31) / 32, (j1 - j0 + 7) / 8);
+  stimulate_box_kernel<Real>
+      <<<grid, block, 0, s>>>(u, solid, nx, i0, j0, i1, j1, value);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_rd_step<float>(const StepCoeffs<float> &,
+                                           const Fld<float> &,
+                                           const Fld<float> &,
+                                           const Fld<float> &,
+                                           const uint8_t *, cudaStream_t);
+template cudaError_t launch_rd_step<double>(const StepCoeffs<double> &,
+                                            const Fld<double> &,
+                                            const Fld<double> &,
+                                            const Fld<double> &,
+                                            const uint8_t *, cudaStream_t);
+template cudaError_t launch_stimulate<float>(float *, const uint8_t *, int,
+                                             int, int, int, int, int, float,
+                                             cudaStream_t);
+template cudaError_t launch_stimulate<double>(double *, const uint8_t *, int,
+                                              int, int, int, int, int, double,
+                                              cudaStream_t);
+
+}  // namespace yh

@@ -1,0 +1,522 @@
+// Solver handle of include/yolohtli.h: owns the device buffers of one grid
+// and runs plain and symmetry-reduced step sequences as captured CUDA graphs
+// (the reference drives every kernel from the GLUT idle callback with a
+// blocking copy per step, main.cu:862-1040).
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "yh_kernels.cuh"
+
+namespace yh {
+int check_params(const yh_param_var *p, int model, const yh_fk_params *fk);
+cudaError_t launch_rd_tb(const StepCoeffs<float> &a, const Fld<float> &in,
+                         const Fld<float> &out, const uint8_t *solid,
+                         int nsteps, cudaStream_t s);
+int rd_tb_max_steps();
+}  // namespace yh
+
+using namespace yh;
+
+namespace {
+
+constexpr int kPlainGraphSteps = 64;  // even: the state ends where it began
+constexpr int kSrGraphSteps = 16;
+constexpr int kTipCapacity = 1 << 16;
+
+struct GraphCache {
+  const float *key = nullptr;
+  int len = 0;
+  int tb = 0;
+  long long kernels = 0;  // kernel launches one replay performs
+  cudaGraphExec_t exec = nullptr;
+};
+
+inline int st(cudaError_t e) {
+  if (e == cudaSuccess) return YH_OK;
+  if (e == cudaErrorMemoryAllocation) return YH_ENOMEM;
+  return YH_ECUDA;
+}
+
+}  // namespace
+
+struct yh_solver {
+  yh_param_var p;
+  yh_fk_params fk;
+  int model = 0, nf = 2;
+  cudaStream_t s = nullptr;
+  size_t n = 0, stride = 0;
+  float *pool = nullptr;     // state ping-pong
+  float *sr_pool = nullptr;  // tangent, BFECC scratch, template
+  Fld<float> cur{}, nxt{}, tan{}, uf{}, ue{}, tx{}, ty{}, tt{};
+  uint8_t *solid = nullptr;
+  int *tip_count = nullptr;
+  yh_tip *tips = nullptr;
+  unsigned int *tip_done = nullptr;
+  yh_sym_state *sym = nullptr;
+  void *ws = nullptr;
+  double *adv_d = nullptr;  // ny rows then nx columns
+  float *adv_f = nullptr;
+  int step = 0;
+  int sr_step = 0;
+  int time_block = 1;
+  bool sr_ready = false;
+  bool frozen = false;
+  long long launches = 0;  // kernels enqueued by this handle
+  GraphCache plain[2];
+  GraphCache sr[2];
+};
+
+static void free_graph(GraphCache &g) {
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  g = GraphCache();
+}
+
+static Fld<float> carve(float *base, size_t stride, int nf, int slot) {
+  Fld<float> f{};
+  for (int k = 0; k < nf; ++k) f.f[k] = base + (size_t)(slot * nf + k) * stride;
+  return f;
+}
+
+extern "C" int yh_create(const yh_param_var *p, int model,
+                         const yh_fk_params *fk, const uint8_t *solid_host,
+                         void *stream, yh_solver **out) {
+  if (!out) return YH_EINVAL;
+  *out = nullptr;
+  int rc = check_params(p, model, fk);
+  if (rc) return rc;
+  if (p->solidSwitch && !solid_host) return YH_EINVAL;
+  yh_solver *h = new (std::nothrow) yh_solver();
+  if (!h) return YH_ENOMEM;
+  h->p = *p;
+  if (fk) h->fk = *fk; else memset(&h->fk, 0, sizeof(h->fk));
+  h->model = model;
+  h->nf = model == YH_MODEL_FK3V ? 3 : 2;
+  h->s = (cudaStream_t)stream;
+  h->n = (size_t)p->nx * p->ny;
+  h->stride = (h->n + 63) & ~(size_t)63;  // 256-byte aligned fields
+  cudaError_t e =
+      cudaMalloc(&h->pool, 2 * h->nf * h->stride * sizeof(float));
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(h->pool, 0, 2 * h->nf * h->stride * sizeof(float),
+                        h->s);
+  if (e == cudaSuccess) {
+    h->cur = carve(h->pool, h->stride, h->nf, 0);
+    h->nxt = carve(h->pool, h->stride, h->nf, 1);
+  }
+  if (e == cudaSuccess && p->solidSwitch) {
+    e = cudaMalloc(&h->solid, (h->n + 255) & ~(size_t)255);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h->solid, solid_host, h->n, cudaMemcpyHostToDevice,
+                          h->s);
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&h->tip_count, 256);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->tip_count, 0, 256, h->s);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&h->tips, (size_t)kTipCapacity * sizeof(yh_tip));
+  if (e == cudaSuccess) h->tip_done = (unsigned int *)(h->tip_count + 32);
+  if (e == cudaSuccess) e = cudaMalloc(&h->sym, sizeof(yh_sym_state));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  if (e != cudaSuccess) {
+    yh_destroy(h);
+    return st(e);
+  }
+  *out = h;
+  return YH_OK;
+}
+
+extern "C" int yh_destroy(yh_solver *h) {
+  if (!h) return YH_EINVAL;
+  if (h->s) cudaStreamSynchronize(h->s); else cudaDeviceSynchronize();
+  for (auto &g : h->plain) free_graph(g);
+  for (auto &g : h->sr) free_graph(g);
+  cudaFree(h->pool);
+  cudaFree(h->sr_pool);
+  cudaFree(h->solid);
+  cudaFree(h->tip_count);
+  cudaFree(h->tips);
+  cudaFree(h->sym);
+  cudaFree(h->ws);
+  cudaFree(h->adv_d);
+  cudaFree(h->adv_f);
+  delete h;
+  return YH_OK;
+}
+
+extern "C" int yh_synchronize(yh_solver *h) {
+  if (!h) return YH_EINVAL;
+  return st(cudaStreamSynchronize(h->s));
+}
+
+extern "C" int yh_set_state(yh_solver *h, const float *u, const float *v,
+                            const float *w) {
+  if (!h) return YH_EINVAL;
+  const float *src[3] = {u, v, w};
+  for (int f = 0; f < h->nf; ++f) {
+    if (!src[f]) continue;
+    cudaError_t e = cudaMemcpyAsync(h->cur.f[f], src[f], h->n * sizeof(float),
+                                    cudaMemcpyDefault, h->s);
+    if (e != cudaSuccess) return st(e);
+  }
+  return YH_OK;
+}
+
+extern "C" int yh_get_state(yh_solver *h, float *u, float *v, float *w) {
+  if (!h) return YH_EINVAL;
+  float *dst[3] = {u, v, w};
+  for (int f = 0; f < h->nf; ++f) {
+    if (!dst[f]) continue;
+    cudaError_t e = cudaMemcpyAsync(dst[f], h->cur.f[f], h->n * sizeof(float),
+                                    cudaMemcpyDefault, h->s);
+    if (e != cudaSuccess) return st(e);
+  }
+  return st(cudaStreamSynchronize(h->s));
+}
+
+extern "C" int yh_state_device(yh_solver *h, yh_fields *cur) {
+  if (!h || !cur) return YH_EINVAL;
+  cur->u = h->cur.f[0];
+  cur->v = h->cur.f[1];
+  cur->w = h->nf > 2 ? h->cur.f[2] : nullptr;
+  return YH_OK;
+}
+
+extern "C" int yh_get_step(yh_solver *h, int *step) {
+  if (!h || !step) return YH_EINVAL;
+  *step = h->step;
+  return YH_OK;
+}
+
+extern "C" int yh_set_time_block(yh_solver *h, int k) {
+  if (!h) return YH_EINVAL;
+  if (k < 1) k = 1;
+  const int kmax = rd_tb_max_steps();
+  h->time_block = k > kmax ? kmax : k;
+  return YH_OK;
+}
+
+// `len` plain steps starting from h->cur, leaving the result in h->cur.
+// With time_block > 1 the temporally blocked kernel takes that many steps
+// per launch (its depth is fixed per launch, so the ping-pong flips once per
+// launch).
+static cudaError_t enqueue_plain(yh_solver *h, int len) {
+  const StepCoeffs<float> a = make_step_coeffs<float>(h->p, h->model, &h->fk);
+  const Fld<float> none{};
+  int left = len;
+  while (left > 0) {
+    cudaError_t e;
+    if (h->time_block > 1 && left >= 2) {
+      const int k = std::min(left, h->time_block);
+      e = launch_rd_tb(a, h->cur, h->nxt, h->solid, k, h->s);
+      left -= k;
+    } else {
+      e = launch_rd_step<float>(a, h->cur, h->nxt, none, h->solid, h->s);
+      left -= 1;
+    }
+    if (e != cudaSuccess) return e;
+    h->launches += 1;
+    std::swap(h->cur, h->nxt);
+  }
+  return cudaSuccess;
+}
+
+static int graph_for(yh_solver *h, GraphCache *cache, int len,
+                     cudaError_t (*body)(yh_solver *, int),
+                     cudaGraphExec_t *exec) {
+  for (int k = 0; k < 2; ++k)
+    if (cache[k].exec && cache[k].key == h->cur.f[0] && cache[k].len == len &&
+        cache[k].tb == h->time_block) {
+      *exec = cache[k].exec;
+      return YH_OK;
+    }
+  GraphCache &slot = cache[0].exec && !cache[1].exec ? cache[1] : cache[0];
+  free_graph(slot);
+  const float *key = h->cur.f[0];
+  const Fld<float> save_cur = h->cur, save_nxt = h->nxt;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return st(e);
+  const long long before = h->launches;
+  cudaError_t eb = body(h, len);
+  e = cudaStreamEndCapture(h->s, &g);
+  const long long kernels = h->launches - before;
+  h->launches = before;  // capturing launches nothing
+  h->cur = save_cur;
+  h->nxt = save_nxt;
+  if (eb != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return st(eb);
+  }
+  if (e != cudaSuccess) return st(e);
+  e = cudaGraphInstantiate(&slot.exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    slot = GraphCache();
+    return st(e);
+  }
+  slot.key = key;
+  slot.len = len;
+  slot.tb = h->time_block;
+  slot.kernels = kernels;
+  *exec = slot.exec;
+  return YH_OK;
+}
+
+// Replays a cached graph and counts its kernels.
+static int replay(yh_solver *h, GraphCache *cache, cudaGraphExec_t ex) {
+  cudaError_t e = cudaGraphLaunch(ex, h->s);
+  if (e != cudaSuccess) return st(e);
+  for (int k = 0; k < 2; ++k)
+    if (cache[k].exec == ex) h->launches += cache[k].kernels;
+  return YH_OK;
+}
+
+static cudaError_t plain_body(yh_solver *h, int len) {
+  return enqueue_plain(h, len);
+}
+
+// Runs `len` plain steps: whole graphs of kPlainGraphSteps, then the rest
+// launched directly. Returns with the state in h->cur.
+static int run_plain(yh_solver *h, int len) {
+  while (len >= kPlainGraphSteps) {
+    cudaGraphExec_t ex = nullptr;
+    int rc = graph_for(h, h->plain, kPlainGraphSteps, plain_body, &ex);
+    if (rc) return rc;
+    rc = replay(h, h->plain, ex);
+    if (rc) return rc;
+    // the graph is built so that an even number of flips returns the
+    // state to h->cur; with temporal blocking the flips are per launch
+    int flips = 0;
+    {
+      int left = kPlainGraphSteps;
+      while (left > 0) {
+        if (h->time_block > 1 && left >= 2) left -= std::min(left, h->time_block);
+        else left -= 1;
+        ++flips;
+      }
+    }
+    if (flips & 1) std::swap(h->cur, h->nxt);
+    len -= kPlainGraphSteps;
+    h->step += kPlainGraphSteps;
+  }
+  if (len > 0) {
+    cudaError_t e = enqueue_plain(h, len);
+    if (e != cudaSuccess) return st(e);
+    h->step += len;
+  }
+  return YH_OK;
+}
+
+extern "C" int yh_run(yh_solver *h, int nsteps, const yh_stim *stims,
+                      int nstims) {
+  if (!h || nsteps < 0 || (nstims > 0 && !stims)) return YH_EINVAL;
+  const int end = h->step + nsteps;
+  std::vector<yh_stim> ev;
+  for (int k = 0; k < nstims; ++k)
+    if (stims[k].step >= h->step && stims[k].step < end) ev.push_back(stims[k]);
+  std::stable_sort(ev.begin(), ev.end(),
+                   [](const yh_stim &a, const yh_stim &b) { return a.step < b.step; });
+  size_t k = 0;
+  while (h->step < end) {
+    while (k < ev.size() && ev[k].step == h->step) {
+      cudaError_t e = launch_stimulate<float>(
+          h->cur.f[0], h->solid, h->p.nx, h->p.ny, ev[k].i0, ev[k].j0,
+          ev[k].i1, ev[k].j1, ev[k].value, h->s);
+      if (e != cudaSuccess) return st(e);
+      h->launches += 1;
+      ++k;
+    }
+    const int next = k < ev.size() ? ev[k].step : end;
+    int rc = run_plain(h, next - h->step);
+    if (rc) return rc;
+  }
+  return st(cudaGetLastError());
+}
+
+extern "C" int yh_track_tips(yh_solver *h) {
+  if (!h) return YH_EINVAL;
+  cudaError_t e = cudaMemsetAsync(h->tip_count, 0, sizeof(int), h->s);
+  if (e != cudaSuccess) return st(e);
+  // plain mode: x = new u (present), y = old u (past) (main.cu:963)
+  e = launch_tips<float>(h->p, h->nxt.f[0], h->cur.f[0], h->solid,
+                         h->p.dt * (double)h->step, h->tip_count, h->tips,
+                         kTipCapacity, nullptr, nullptr, h->s);
+  if (e == cudaSuccess) h->launches += 1;
+  return st(e);
+}
+
+extern "C" int yh_get_launch_count(yh_solver *h, long long *n) {
+  if (!h || !n) return YH_EINVAL;
+  *n = h->launches;
+  return YH_OK;
+}
+
+extern "C" int yh_get_tips(yh_solver *h, yh_tip *out, int capacity, int *n) {
+  if (!h || !n || (capacity > 0 && !out)) return YH_EINVAL;
+  int cnt = 0;
+  cudaError_t e = cudaMemcpyAsync(&cnt, h->tip_count, sizeof(int),
+                                  cudaMemcpyDeviceToHost, h->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  if (e != cudaSuccess) return st(e);
+  const int have = std::min(cnt, kTipCapacity);
+  std::vector<yh_tip> buf((size_t)have);
+  if (have > 0) {
+    e = cudaMemcpyAsync(buf.data(), h->tips, (size_t)have * sizeof(yh_tip),
+                        cudaMemcpyDeviceToHost, h->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+    if (e != cudaSuccess) return st(e);
+  }
+  // the atomic push order is not deterministic: return them sorted by (y, x)
+  std::sort(buf.begin(), buf.end(), [](const yh_tip &a, const yh_tip &b) {
+    return a.y < b.y || (a.y == b.y && a.x < b.x);
+  });
+  const int m = std::min(have, capacity);
+  if (m > 0) memcpy(out, buf.data(), (size_t)m * sizeof(yh_tip));
+  *n = cnt;
+  return cnt > kTipCapacity || cnt > capacity ? YH_EOVERFLOW : YH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Symmetry reduction
+// ---------------------------------------------------------------------------
+
+extern "C" int yh_sr_begin(yh_solver *h, int template_mode, const float *tu,
+                           const float *tv, const float *tw) {
+  if (!h) return YH_EINVAL;
+  if (template_mode != YH_TEMPLATE_CURRENT && template_mode != YH_TEMPLATE_FROZEN)
+    return YH_EINVAL;
+  const bool frozen = template_mode == YH_TEMPLATE_FROZEN;
+  if (frozen && (!tu || !tv || (h->nf > 2 && !tw))) return YH_EINVAL;
+  cudaError_t e = cudaSuccess;
+  if (!h->sr_pool) {
+    // tan, uf, ue, tx, ty, tt
+    e = cudaMalloc(&h->sr_pool, 6 * h->nf * h->stride * sizeof(float));
+    if (e == cudaSuccess)
+      e = cudaMemsetAsync(h->sr_pool, 0, 6 * h->nf * h->stride * sizeof(float),
+                          h->s);
+    if (e != cudaSuccess) return st(e);
+    h->tan = carve(h->sr_pool, h->stride, h->nf, 0);
+    h->uf = carve(h->sr_pool, h->stride, h->nf, 1);
+    h->ue = carve(h->sr_pool, h->stride, h->nf, 2);
+    h->tx = carve(h->sr_pool, h->stride, h->nf, 3);
+    h->ty = carve(h->sr_pool, h->stride, h->nf, 4);
+    h->tt = carve(h->sr_pool, h->stride, h->nf, 5);
+    const size_t wsb = yh_phase_integrals_workspace(h->p.nx, h->p.ny);
+    e = cudaMalloc(&h->ws, wsb);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->ws, 0, wsb, h->s);
+    if (e == cudaSuccess)
+      e = cudaMalloc(&h->adv_d, (size_t)(h->p.nx + h->p.ny) * sizeof(double));
+    if (e == cudaSuccess)
+      e = cudaMalloc(&h->adv_f, (size_t)(h->p.nx + h->p.ny) * sizeof(float));
+    if (e != cudaSuccess) return st(e);
+  }
+  e = cudaMemsetAsync(h->adv_d, 0, (size_t)(h->p.nx + h->p.ny) * sizeof(double), h->s);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(h->adv_f, 0, (size_t)(h->p.nx + h->p.ny) * sizeof(float), h->s);
+  if (e != cudaSuccess) return st(e);
+  if (frozen) {
+    // the template state goes through the BFECC scratch uf
+    const float *src[3] = {tu, tv, tw};
+    for (int f = 0; f < h->nf; ++f) {
+      e = cudaMemcpyAsync(h->uf.f[f], src[f], h->n * sizeof(float),
+                          cudaMemcpyHostToDevice, h->s);
+      if (e != cudaSuccess) return st(e);
+    }
+    e = launch_template<float>(h->p, h->nf, h->uf, h->tx, h->ty, h->tt, h->s);
+    if (e != cudaSuccess) return st(e);
+  }
+  yh_sym_state s0;
+  memset(&s0, 0, sizeof(s0));
+  s0.centre[0] = h->p.tipx;  // tipx0_d (main.cu:373-376)
+  s0.centre[1] = h->p.tipy;
+  e = cudaMemcpyAsync(h->sym, &s0, sizeof(s0), cudaMemcpyHostToDevice, h->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  if (e != cudaSuccess) return st(e);
+  h->frozen = frozen;
+  h->sr_step = 0;
+  h->sr_ready = true;
+  for (auto &g : h->sr) free_graph(g);
+  return YH_OK;
+}
+
+// One symmetry-reduced step (main.cu:894-954) on the stream.
+static cudaError_t enqueue_sr_step(yh_solver *h, bool first) {
+  const StepCoeffs<float> a = make_step_coeffs<float>(h->p, h->model, &h->fk);
+  const Fld<float> none{};
+  const Fld<float> tx = h->frozen ? h->tx : none;
+  const Fld<float> ty = h->frozen ? h->ty : none;
+  const Fld<float> tt = h->frozen ? h->tt : none;
+  double *adv_rows = h->adv_d, *adv_cols = h->adv_d + h->p.ny;
+  float *advf_rows = h->adv_f, *advf_cols = h->adv_f + h->p.ny;
+  cudaError_t e = cudaMemsetAsync(h->tip_count, 0, sizeof(int), h->s);
+  if (e == cudaSuccess)  // 1. RD with tangent: cur -> nxt
+    e = launch_rd_step<float>(a, h->cur, h->nxt, h->tan, h->solid, h->s);
+  if (e == cudaSuccess)  // 2. tips x = pre-RD u, y = post-RD u; centre
+    e = launch_tips<float>(h->p, h->nxt.f[0], h->cur.f[0], h->solid, 0.0,
+                           h->tip_count, h->tips, kTipCapacity, h->sym,
+                           h->tip_done, h->s);
+  const int reps = first ? 2 : 1;  // main.cu:910-926
+  for (int r = 0; r < reps && e == cudaSuccess; ++r) {
+    e = launch_phase<float>(h->p, h->nf, h->cur, h->tan, tx, ty, tt, adv_rows,
+                            adv_cols, h->solid, h->sym, h->ws, h->s);
+    if (e == cudaSuccess)
+      e = launch_comoving(h->p, h->sym, adv_rows, adv_cols, advf_rows,
+                          advf_cols, r == reps - 1, h->s);
+  }
+  if (e == cudaSuccess)  // BFECC: nxt -> cur
+    e = launch_bfecc<float>(h->p, h->nf, h->nxt, h->cur, advf_rows, advf_cols,
+                            h->solid, h->uf, h->ue, h->s);
+  // RD, tips, (phase, comoving) x reps, 3 BFECC passes
+  if (e == cudaSuccess) h->launches += 2 + 2 * reps + 3;
+  return e;
+}
+
+static cudaError_t sr_body(yh_solver *h, int len) {
+  for (int k = 0; k < len; ++k) {
+    cudaError_t e = enqueue_sr_step(h, false);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+extern "C" int yh_sr_step(yh_solver *h, int nsteps) {
+  if (!h || nsteps < 0) return YH_EINVAL;
+  if (!h->sr_ready) return YH_ENOTREADY;
+  int left = nsteps;
+  if (left > 0 && h->sr_step == 0) {
+    cudaError_t e = enqueue_sr_step(h, true);
+    if (e != cudaSuccess) return st(e);
+    h->sr_step += 1;
+    h->step += 1;
+    left -= 1;
+  }
+  while (left >= kSrGraphSteps) {
+    cudaGraphExec_t ex = nullptr;
+    int rc = graph_for(h, h->sr, kSrGraphSteps, sr_body, &ex);
+    if (rc) return rc;
+    rc = replay(h, h->sr, ex);
+    if (rc) return rc;
+    left -= kSrGraphSteps;
+    h->sr_step += kSrGraphSteps;
+    h->step += kSrGraphSteps;
+  }
+  for (; left > 0; --left) {
+    cudaError_t e = enqueue_sr_step(h, false);
+    if (e != cudaSuccess) return st(e);
+    h->sr_step += 1;
+    h->step += 1;
+  }
+  return st(cudaGetLastError());
+}
+
+extern "C" int yh_get_sym(yh_solver *h, yh_sym_state *out) {
+  if (!h || !out) return YH_EINVAL;
+  if (!h->sr_ready) return YH_ENOTREADY;
+  cudaError_t e = cudaMemcpyAsync(out, h->sym, sizeof(*out),
+                                  cudaMemcpyDeviceToHost, h->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  return st(e);
+}

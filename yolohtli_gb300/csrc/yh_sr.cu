@@ -1,0 +1,779 @@
+// Symmetry-reduction kernels of the monodomain hot path:
+//   tip_kernel     spiral tips, closed-form bilinear isoline intersection
+//                  (spiralTip_kernel, tipTracker.cu:20-241) + the disc-centre
+//                  choice in the last block;
+//   phase_kernel   slices (symmetryReduction.cu:72-262) fused with the 12
+//                  phase integrals (integralTrapz.cu:17-184) in FP64 and the
+//                  FP64 3x3 solve (symmetryReduction.cu:329-420) in the last
+//                  block: one launch instead of 2 + 12 launches, 12 blocking
+//                  copies and a host solve;
+//   comoving_kernel the comoving field (Cxy_field_kernel,
+//                  symmetryReduction.cu:20-62), which is separable: adv.x
+//                  depends on the row, adv.y on the column, so it is two
+//                  vectors of ny and nx values, not two full grids;
+//   bfecc_pass1/2/3 BFECC advection (advFDBFECC.cu:18-353) as three passes,
+//                  so no thread reads a neighbour written in the same launch.
+//
+// Reductions are deterministic: per-thread FP64 accumulators, warp shuffles,
+// per-block partials, and a fixed-order sum by the last block to finish.
+#include "yh_kernels.cuh"
+
+namespace yh {
+
+// ---------------------------------------------------------------------------
+// Tips
+// ---------------------------------------------------------------------------
+
+struct TipArgs {
+  int nx, ny, r2;
+  double Uth;
+  double dt;     // with sym: time = dt * sym->step (graph-stable)
+  double ptime;  // without sym: the time stamp of the tips
+};
+
+__device__ __forceinline__ void tip_record(int i, int j, float s, float t,
+                                           float ptime, int *count,
+                                           yh_tip *vec, int cap) {
+  // tipRecordPlane (tipTracker.cu:215-236)
+  if ((s > 0.0f && s < 1.0f) && (t > 0.0f && t < 1.0f)) {
+    const int slot = atomicAdd(count, 1);
+    if (slot < cap) {
+      yh_tip d;
+      d.x = (float)i + s;
+      d.y = (float)j + t;
+      d.vx = 0.0f;
+      d.vy = 0.0f;
+      d.t = ptime;
+      vec[slot] = d;
+    }
+  }
+}
+
+// Candidate tips of one cell; x = present corners, y = past corners in the
+// order (i,j), (i+1,j), (i+1,j+1), (i,j+1) (tipTracker.cu:140-174), in FP64.
+__device__ __forceinline__ void tip_cell(double Uth, int i, int j, double x1,
+                                         double x2, double x3, double x4,
+                                         double y1, double y2, double y3,
+                                         double y4, bool need_disc,
+                                         float ptime, int *count, yh_tip *vec,
+                                         int cap) {
+  const double x3y1 = x3 * y1, x4y1 = x4 * y1, x3y2 = x3 * y2, x4y2 = x4 * y2;
+  const double x1y3 = x1 * y3, x2y3 = x2 * y3, x1y4 = x1 * y4, x2y4 = x2 * y4;
+  const double x2y1 = x2 * y1, x1y2 = x1 * y2, x4y3 = x4 * y3, x3y4 = x3 * y4;
+  const double den1 =
+      2.0 * (x3y1 - x4y1 - x3y2 + x4y2 - x1y3 + x2y3 + x1y4 - x2y4);
+  const double den2 =
+      2.0 * (x2y1 - x3y1 - x1y2 + x4y2 + x1y3 - x4y3 - x2y4 + x3y4);
+  const double ctn1 = x1 - x2 + x3 - x4 - y1 + y2 - y3 + y4;
+  const double ctn2 = x3y1 - 2.0 * x4y1 + x4y2 - x1y3 + 2.0 * x1y4 - x2y4;
+  const double disc =
+      sqrt(4.0 * (x3y1 - x3y2 - x4y1 + x4y2 - x1y3 + x1y4 + x2y3 - x2y4) *
+               (x4y1 - x1y4 + Uth * (x1 - x4 - y1 + y4)) +
+           (-ctn2 + Uth * ctn1) * (-ctn2 + Uth * ctn1));
+  const double px = ctn2 - Uth * ctn1;
+  const double py =
+      Uth * ctn1 - x3y1 + x4y2 + x1y3 - x2y4 + 2.0 * (x2y1 - x1y2);
+  if (need_disc && !(disc >= 0.0)) return;
+  tip_record(i, j, (float)((px + disc) / den1), (float)((py + disc) / den2),
+             ptime, count, vec, cap);
+  tip_record(i, j, (float)((px - disc) / den1), (float)((py - disc) / den2),
+             ptime, count, vec, cap);
+}
+
+// Block-wide argmin (256 threads, linear id t) of the tip nearest to the
+// current centre, ties broken by (y, x); writes the new centre unless no tip
+// was found or this is step 0 (slice_kernel uses tipx0/tipy0 at count == 0,
+// symmetryReduction.cu:98-101).
+__device__ void pick_centre_block(int t, const int *count, const yh_tip *vec,
+                                  int cap, yh_sym_state *sym) {
+  __shared__ double s_d[256];
+  __shared__ float s_x[256], s_y[256];
+  const int n0 = *(volatile const int *)count;
+  const int n = n0 < cap ? n0 : cap;
+  const float cx = sym->centre[0], cy = sym->centre[1];
+  double bd = 1e300;
+  float bx = 0.f, by = 0.f;
+  for (int k = t; k < n; k += 256) {
+    const float tx = ((volatile const float *)&vec[k].x)[0];
+    const float ty = ((volatile const float *)&vec[k].y)[0];
+    const double dx = (double)tx - cx, dy = (double)ty - cy;
+    const double d = dx * dx + dy * dy;
+    if (d < bd || (d == bd && (ty < by || (ty == by && tx < bx)))) {
+      bd = d;
+      bx = tx;
+      by = ty;
+    }
+  }
+  s_d[t] = bd;
+  s_x[t] = bx;
+  s_y[t] = by;
+  __syncthreads();
+  for (int off = 128; off > 0; off >>= 1) {
+    if (t < off) {
+      const int o = t + off;
+      const double d = s_d[o];
+      const float x = s_x[o], y = s_y[o];
+      const double db = s_d[t];
+      const float xb = s_x[t], yb = s_y[t];
+      if (d < db || (d == db && (y < yb || (y == yb && x < xb)))) {
+        s_d[t] = d;
+        s_x[t] = x;
+        s_y[t] = y;
+      }
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    sym->ntips = n0;
+    if (n > 0 && sym->step > 0) {
+      sym->centre[0] = s_x[0];
+      sym->centre[1] = s_y[0];
+    }
+  }
+}
+
+// HOLES: the disc around the grid centre, all cells, no disc>=0 test
+// (tipTracker.cu:47-122); otherwise i in [1,nx-3], j in [1,ny-3]
+// (tipTracker.cu:124-204). For FP32 fields a cell is skipped early when the
+// threshold lies outside the corner range of either level: a bilinear
+// interpolant on the unit cell stays within its corner values, so no root
+// of x = Uth, y = Uth can lie inside such a cell.
+template <typename Real, bool HOLES>
+__global__ void __launch_bounds__(256)
+    tip_kernel(const TipArgs a, const Real *__restrict__ past,
+               const Real *__restrict__ present, int *count, yh_tip *vec,
+               int cap, yh_sym_state *sym, unsigned int *done) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.nx, ny = a.ny;
+  const float ptime =
+      sym ? (float)(a.dt * (double)sym->step) : (float)a.ptime;
+  bool active;
+  if (HOLES) {
+    const int ic = i - nx / 2, jc = j - ny / 2;
+    active = i < nx && j < ny && (ic * ic + jc * jc) < a.r2;
+  } else {
+    active = (i >= 1) && (i < nx - 2) && (j >= 1) && (j < ny - 2);
+  }
+  if (active) {
+    const int s0 = i + nx * j;
+    const int sx = (i < nx - 1) ? s0 + 1 : s0;
+    const int sy = (j < ny - 1) ? s0 + nx : s0;
+    const int sxy = ((j < ny - 1) && (i < nx - 1)) ? s0 + nx + 1 : s0;
+    const Real x1 = present[s0], x2 = present[sx], x4 = present[sy],
+               x3 = present[sxy];
+    const Real y1 = past[s0], y2 = past[sx], y4 = past[sy], y3 = past[sxy];
+    bool cand = true;
+    if (sizeof(Real) == 4) {
+      const float th = (float)a.Uth, tol = 1e-5f;
+      const float xmn = fminf(fminf(x1, x2), fminf(x3, x4));
+      const float xmx = fmaxf(fmaxf(x1, x2), fmaxf(x3, x4));
+      const float ymn = fminf(fminf(y1, y2), fminf(y3, y4));
+      const float ymx = fmaxf(fmaxf(y1, y2), fmaxf(y3, y4));
+      cand = th >= xmn - tol && th <= xmx + tol && th >= ymn - tol &&
+             th <= ymx + tol;
+    }
+    if (cand)
+      tip_cell(a.Uth, i, j, x1, x2, x3, x4, y1, y2, y3, y4, !HOLES, ptime,
+               count, vec, cap);
+  }
+  if (sym == nullptr) return;
+  // Last block to finish chooses the disc centre.
+  __shared__ bool s_last;
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    __threadfence();
+    const unsigned nb = gridDim.x * gridDim.y;
+    s_last = atomicAdd(done, 1u) == nb - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const int t = threadIdx.x + blockDim.x * threadIdx.y;
+  if (t == 0) *done = 0u;
+  pick_centre_block(t, count, vec, cap, sym);
+}
+
+__global__ void pick_centre_kernel(const int *count, const yh_tip *vec,
+                                   int cap, yh_sym_state *sym) {
+  pick_centre_block(threadIdx.x, count, vec, cap, sym);
+}
+
+// With sym_pick != nullptr the tips are stamped dt*sym->step (so a captured
+// graph stays valid as steps advance) and the last block picks the centre;
+// otherwise they are stamped `ptime`. `done` is a zeroed counter.
+template <typename Real>
+cudaError_t launch_tips(const yh_param_var &p, const Real *past,
+                        const Real *present, const uint8_t *solid,
+                        double ptime, int *count, yh_tip *vec, int cap,
+                        yh_sym_state *sym_pick, unsigned int *done,
+                        cudaStream_t s) {
+  TipArgs a;
+  a.nx = p.nx;
+  a.ny = p.ny;
+  a.r2 = p.tipOffsetX * p.tipOffsetY;
+  a.Uth = p.Uth;
+  a.dt = p.dt;
+  a.ptime = ptime;
+  const dim3 block(32, 8);
+  const dim3 grid((p.nx + 31) / 32, (p.ny + 7) / 8);
+  const bool holes = p.solidSwitch && solid;
+  if (holes)
+    tip_kernel<Real, true><<<grid, block, 0, s>>>(a, past, present, count,
+                                                  vec, cap, sym_pick, done);
+  else
+    tip_kernel<Real, false><<<grid, block, 0, s>>>(a, past, present, count,
+                                                   vec, cap, sym_pick, done);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pick_centre(const int *count, const yh_tip *vec, int cap,
+                               yh_sym_state *sym, cudaStream_t s) {
+  pick_centre_kernel<<<1, 256, 0, s>>>(count, vec, cap, sym);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Phase integrals + solve
+// ---------------------------------------------------------------------------
+
+template <typename Real>
+struct PhaseArgs {
+  int nx, ny, r2, R;  // R: largest integer with R*R < r2
+  Real hx, hy, invdx, invdy;
+  double hxhy;
+};
+
+constexpr int kPhaseBX = 32, kPhaseBY = 8;
+
+// 2nd-order one-sided derivative, upwinded by the sign of adv
+// (convFB2ndOX/Y, symmetryReduction.cu:242-262).
+template <typename Real>
+__device__ __forceinline__ Real fb2(Real c, Real p1, Real p2, Real m1, Real m2,
+                                    double adv, Real inv) {
+  return adv > 0.0 ? (Real(-3) * c + Real(4) * p1 - p2) * inv
+                   : (Real(3) * c - Real(4) * m1 + m2) * inv;
+}
+// Negated 4th-order central derivative (convCentral2X/Y,
+// symmetryReduction.cu:224-240).
+template <typename Real>
+__device__ __forceinline__ Real c4(Real p1, Real p2, Real m1, Real m2,
+                                   Real inv) {
+  return (p2 - Real(8) * p1 + Real(8) * m1 - m2) * inv * Real(1.0 / 6.0);
+}
+
+// FP64 3x3 solve of the drift/rotation system with partial pivoting.
+// Row r: [I[3r] cos(pt) + I[3r+1] sin(pt), I[3r+1] cos(pt) - I[3r] sin(pt),
+// I[3r+2]] . c = I[9+r]  (symmetryReduction.cu:390-396). Returns YH_OK, or
+// YH_ESINGULAR when a pivot is below 1e-13 of the largest entry (the
+// reference divides by unpivoted entries, symmetryReduction.cu:398-412).
+__device__ int solve3(const double I[12], double pt, double c[3]) {
+  double cs, sn;
+  sincos(pt, &sn, &cs);
+  double A[3][4];
+  double amax = 0.0;
+  for (int r = 0; r < 3; ++r) {
+    A[r][0] = I[3 * r] * cs + I[3 * r + 1] * sn;
+    A[r][1] = I[3 * r + 1] * cs - I[3 * r] * sn;
+    A[r][2] = I[3 * r + 2];
+    A[r][3] = I[9 + r];
+    for (int k = 0; k < 3; ++k) amax = fmax(amax, fabs(A[r][k]));
+  }
+  if (!(amax > 0.0) || !isfinite(amax)) return YH_ESINGULAR;
+  const double tol = 1e-13 * amax;
+  for (int col = 0; col < 3; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < 3; ++r)
+      if (fabs(A[r][col]) > fabs(A[piv][col])) piv = r;
+    if (!(fabs(A[piv][col]) > tol)) return YH_ESINGULAR;
+    if (piv != col)
+      for (int k = 0; k < 4; ++k) {
+        const double t = A[col][k];
+        A[col][k] = A[piv][k];
+        A[piv][k] = t;
+      }
+    for (int r = col + 1; r < 3; ++r) {
+      const double m = A[r][col] / A[col][col];
+      for (int k = col; k < 4; ++k) A[r][k] -= m * A[col][k];
+    }
+  }
+  double x[3];
+  for (int r = 2; r >= 0; --r) {
+    double s = A[r][3];
+    for (int k = r + 1; k < 3; ++k) s -= A[r][k] * x[k];
+    x[r] = s / A[r][r];
+  }
+  for (int k = 0; k < 3; ++k) c[k] = x[k];
+  return YH_OK;
+}
+
+// One block covers a 32x8 tile of the disc's bounding box, placed by the
+// current disc centre read from `sym` (so a captured graph follows the tip).
+template <int NF, typename Real, bool FROZEN, bool HOLES>
+__global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
+    phase_kernel(const PhaseArgs<Real> a, const Fld<Real> st,
+                 const Fld<Real> tan, const Fld<Real> tx, const Fld<Real> ty,
+                 const Fld<Real> tt, const double *__restrict__ adv_rows,
+                 const double *__restrict__ adv_cols,
+                 const uint8_t *__restrict__ solid, yh_sym_state *sym,
+                 double *partials, unsigned int *done) {
+  const int nx = a.nx, ny = a.ny;
+  // integer centre as slice_kernel/trapz_kernel round it
+  // (symmetryReduction.cu:98-104): float arithmetic, round-half-even.
+  const int cx = __float2int_rn(sym->centre[0] - (float)(nx / 2));
+  const int cy = __float2int_rn(sym->centre[1] - (float)(ny / 2));
+  const int i = nx / 2 + cx - a.R + (int)(blockIdx.x * kPhaseBX + threadIdx.x);
+  const int j = ny / 2 + cy - a.R + (int)(blockIdx.y * kPhaseBY + threadIdx.y);
+  double acc[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) acc[k] = 0.0;
+  if (i >= 0 && i < nx && j >= 0 && j < ny) {
+    const int ic = i - nx / 2 - cx, jc = j - ny / 2 - cy;
+    if (ic * ic + jc * jc < a.r2) {
+      const int C = i + nx * j;
+      const bool tissue = !HOLES || solid[C] != 0;
+      const double ax = tissue ? adv_rows[j] : 0.0;
+      const double ay = tissue ? adv_cols[i] : 0.0;
+      const int row = nx * j;
+      const int iE = mirror(i + 1, nx), iW = mirror(i - 1, nx);
+      const int iEE = mirror(i + 2, nx), iWW = mirror(i - 2, nx);
+      const int jN = nx * mirror(j + 1, ny), jS = nx * mirror(j - 1, ny);
+      const int jNN = nx * mirror(j + 2, ny), jSS = nx * mirror(j - 2, ny);
+      const Real x = (Real)i, y = (Real)j;
+      Real s[12];
+#pragma unroll
+      for (int k = 0; k < 12; ++k) s[k] = Real(0);
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        const Real *__restrict__ g = st.f[f];
+        const Real c = g[C];
+        const Real e1 = g[row + iE], e2 = g[row + iEE];
+        const Real w1 = g[row + iW], w2 = g[row + iWW];
+        const Real n1 = g[i + jN], n2 = g[i + jNN];
+        const Real s1 = g[i + jS], s2 = g[i + jSS];
+        const Real dx = fb2(c, e1, e2, w1, w2, ax, a.invdx);
+        const Real dy = fb2(c, n1, n2, s1, s2, ay, a.invdy);
+        const Real dth = a.hx * x * dy - a.hy * y * dx;
+        Real Tx, Ty, Tt;
+        if (FROZEN) {
+          Tx = tx.f[f][C];
+          Ty = ty.f[f][C];
+          Tt = tt.f[f][C];
+        } else {
+          Tx = c4(e1, e2, w1, w2, a.invdx);
+          Ty = c4(n1, n2, s1, s2, a.invdy);
+          Tt = a.hx * x * Ty - a.hy * y * Tx;
+        }
+        const Real vt = tan.f[f][C];
+        const Real Tv[3] = {Tx, Ty, Tt};
+        const Real Cv[4] = {dx, dy, dth, vt};
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) s[q < 3 ? 3 * p + q : 9 + p] += Tv[p] * Cv[q];
+      }
+#pragma unroll
+      for (int k = 0; k < 12; ++k) acc[k] = (double)s[k];
+    }
+  }
+  // warp tree
+#pragma unroll
+  for (int k = 0; k < 12; ++k)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+      acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
+  __shared__ double s_w[kPhaseBY][12];
+  __shared__ bool s_last;
+  const int lane = threadIdx.x;  // blockDim.x == 32
+  const int warp = threadIdx.y;
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < 12; ++k) s_w[warp][k] = acc[k];
+  __syncthreads();
+  const int t = threadIdx.x + kPhaseBX * threadIdx.y;
+  const unsigned nb = gridDim.x * gridDim.y;
+  const unsigned bid = blockIdx.x + gridDim.x * blockIdx.y;
+  if (t < 12) {
+    double v = 0.0;
+    for (int w = 0; w < kPhaseBY; ++w) v += s_w[w][t];
+    partials[(size_t)bid * 12 + t] = v;
+  }
+  __syncthreads();
+  if (t == 0) {
+    __threadfence();
+    s_last = atomicAdd(done, 1u) == nb - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  // Last block: fixed-order sum of the block partials, then the solve.
+  __shared__ double s_r[12][kPhaseBX * kPhaseBY / 12 + 1];
+  // 12 groups of 21 threads each sum a strided subset of blocks, in order.
+  constexpr int G = kPhaseBX * kPhaseBY / 12;  // 21
+  const int k = t / G, r = t % G;
+  if (k < 12) {
+    double v = 0.0;
+    for (unsigned b = r; b < nb; b += G)
+      v += ((volatile double *)partials)[(size_t)b * 12 + k];
+    s_r[k][r] = v;
+  }
+  __syncthreads();
+  if (t == 0) {
+    double I[12];
+    for (int kk = 0; kk < 12; ++kk) {
+      double v = 0.0;
+      for (int rr = 0; rr < G; ++rr) v += s_r[kk][rr];
+      I[kk] = a.hxhy * v;
+      sym->integrals[kk] = I[kk];
+    }
+    double c[3];
+    const int st = solve3(I, sym->phi[2], c);
+    sym->status = st;
+    if (st == YH_OK)
+      for (int kk = 0; kk < 3; ++kk) sym->c[kk] = c[kk];
+    for (int kk = 0; kk < 3; ++kk) {
+      sym->c_adv[kk] = sym->c[kk];
+      sym->phi_adv[kk] = sym->phi[kk];
+    }
+    *done = 0u;
+  }
+}
+
+static void phase_geometry(const yh_param_var &p, int *R, dim3 *grid) {
+  const int r2 = p.tipOffsetX * p.tipOffsetY;
+  int r = 0;
+  while ((long long)(r + 1) * (r + 1) < r2) ++r;
+  // the box never needs to exceed twice the grid
+  const int bx = 2 * r + 1 < 2 * p.nx ? 2 * r + 1 : 2 * p.nx;
+  const int by = 2 * r + 1 < 2 * p.ny ? 2 * r + 1 : 2 * p.ny;
+  *R = r;
+  *grid = dim3((bx + kPhaseBX - 1) / kPhaseBX, (by + kPhaseBY - 1) / kPhaseBY);
+}
+
+size_t phase_workspace_bytes(const yh_param_var &p) {
+  int R;
+  dim3 g;
+  phase_geometry(p, &R, &g);
+  // counter (256 B slot) + 12 doubles per block
+  return 256 + (size_t)g.x * g.y * 12 * sizeof(double);
+}
+
+template <typename Real>
+cudaError_t launch_phase(const yh_param_var &p, int nf, const Fld<Real> &st,
+                         const Fld<Real> &tan, const Fld<Real> &tx,
+                         const Fld<Real> &ty, const Fld<Real> &tt,
+                         const double *adv_rows, const double *adv_cols,
+                         const uint8_t *solid, yh_sym_state *sym,
+                         void *workspace, cudaStream_t s) {
+  PhaseArgs<Real> a;
+  a.nx = p.nx;
+  a.ny = p.ny;
+  a.r2 = p.tipOffsetX * p.tipOffsetY;
+  dim3 grid;
+  phase_geometry(p, &a.R, &grid);
+  a.hx = (Real)p.hx;
+  a.hy = (Real)p.hy;
+  a.invdx = (Real)p.invdx;
+  a.invdy = (Real)p.invdy;
+  a.hxhy = p.hx * p.hy;
+  unsigned int *done = reinterpret_cast<unsigned int *>(workspace);
+  double *partials =
+      reinterpret_cast<double *>(reinterpret_cast<char *>(workspace) + 256);
+  const dim3 block(kPhaseBX, kPhaseBY);
+  const bool frozen = tx.f[0] != nullptr;
+  const bool holes = p.solidSwitch && solid;
+#define YH_PH(NF, FZ, HO)                                                      \
+  if (nf == NF && frozen == FZ && holes == HO) {                               \
+    phase_kernel<NF, Real, FZ, HO><<<grid, block, 0, s>>>(                     \
+        a, st, tan, tx, ty, tt, adv_rows, adv_cols, solid, sym, partials,      \
+        done);                                                                 \
+    return cudaGetLastError();                                                 \
+  }
+  YH_PH(2, false, false)
+  YH_PH(2, false, true)
+  YH_PH(2, true, false)
+  YH_PH(2, true, true)
+  YH_PH(3, false, false)
+  YH_PH(3, false, true)
+  YH_PH(3, true, false)
+  YH_PH(3, true, true)
+#undef YH_PH
+  return cudaErrorInvalidValue;
+}
+
+// Template derivative fields over the whole grid (frozen template).
+template <int NF, typename Real>
+__global__ void template_kernel(const PhaseArgs<Real> a, const Fld<Real> st,
+                                const Fld<Real> tx, const Fld<Real> ty,
+                                const Fld<Real> tt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.nx, ny = a.ny;
+  if (i >= nx || j >= ny) return;
+  const int C = i + nx * j, row = nx * j;
+  const Real x = (Real)i, y = (Real)j;
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    const Real *g = st.f[f];
+    const Real Tx = c4(g[row + mirror(i + 1, nx)], g[row + mirror(i + 2, nx)],
+                       g[row + mirror(i - 1, nx)], g[row + mirror(i - 2, nx)],
+                       a.invdx);
+    const Real Ty = c4(g[i + nx * mirror(j + 1, ny)],
+                       g[i + nx * mirror(j + 2, ny)],
+                       g[i + nx * mirror(j - 1, ny)],
+                       g[i + nx * mirror(j - 2, ny)], a.invdy);
+    tx.f[f][C] = Tx;
+    ty.f[f][C] = Ty;
+    tt.f[f][C] = a.hx * x * Ty - a.hy * y * Tx;
+  }
+}
+
+template <typename Real>
+cudaError_t launch_template(const yh_param_var &p, int nf,
+                            const Fld<Real> &st, const Fld<Real> &tx,
+                            const Fld<Real> &ty, const Fld<Real> &tt,
+                            cudaStream_t s) {
+  PhaseArgs<Real> a;
+  a.nx = p.nx;
+  a.ny = p.ny;
+  a.hx = (Real)p.hx;
+  a.hy = (Real)p.hy;
+  a.invdx = (Real)p.invdx;
+  a.invdy = (Real)p.invdy;
+  const dim3 block(32, 8);
+  const dim3 grid((p.nx + 31) / 32, (p.ny + 7) / 8);
+  if (nf == 2)
+    template_kernel<2, Real><<<grid, block, 0, s>>>(a, st, tx, ty, tt);
+  else
+    template_kernel<3, Real><<<grid, block, 0, s>>>(a, st, tx, ty, tt);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Comoving field and phi update
+// ---------------------------------------------------------------------------
+
+// adv_x[j] = hy*y*ct - cx*cos(pt) + cy*sin(pt);
+// adv_y[i] = -hx*x*ct - cx*sin(pt) - cy*cos(pt)   (symmetryReduction.cu:55-56)
+// from (c_adv, phi_adv); then, if `advance`, phi += dt*c and step += 1
+// (main.cu:936-952).
+__global__ void comoving_kernel(int nx, int ny, double hx, double hy,
+                                double dt, yh_sym_state *sym,
+                                double *adv_rows, double *adv_cols,
+                                float *adv_rows_f, float *adv_cols_f,
+                                int advance) {
+  __shared__ double s_c[3], s_cs, s_sn;
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 3; ++k) s_c[k] = sym->c_adv[k];
+    s_cs = cos(sym->phi_adv[2]);
+    s_sn = sin(sym->phi_adv[2]);
+  }
+  __syncthreads();
+  const double cx = s_c[0], cy = s_c[1], ct = s_c[2], cs = s_cs, sn = s_sn;
+  for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+    const double y = (double)j;
+    const double v = hy * y * ct - cx * cs + cy * sn;
+    adv_rows[j] = v;
+    if (adv_rows_f) adv_rows_f[j] = (float)v;
+  }
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+    const double x = (double)i;
+    const double v = -hx * x * ct - cx * sn - cy * cs;
+    adv_cols[i] = v;
+    if (adv_cols_f) adv_cols_f[i] = (float)v;
+  }
+  __syncthreads();
+  if (advance && threadIdx.x == 0) {
+    for (int k = 0; k < 3; ++k) sym->phi[k] = sym->phi[k] + sym->c[k] * dt;
+    sym->step += 1;
+  }
+}
+
+cudaError_t launch_comoving(const yh_param_var &p, yh_sym_state *sym,
+                            double *adv_rows, double *adv_cols,
+                            float *adv_rows_f, float *adv_cols_f,
+                            bool advance, cudaStream_t s) {
+  comoving_kernel<<<1, 256, 0, s>>>(p.nx, p.ny, p.hx, p.hy, p.dt, sym,
+                                    adv_rows, adv_cols, adv_rows_f,
+                                    adv_cols_f, advance ? 1 : 0);
+  return cudaGetLastError();
+}
+
+__global__ void sym_advance_kernel(double dt, yh_sym_state *sym) {
+  for (int k = 0; k < 3; ++k) sym->phi[k] = sym->phi[k] + sym->c[k] * dt;
+  sym->step += 1;
+}
+
+cudaError_t launch_sym_advance(const yh_param_var &p, yh_sym_state *sym,
+                               cudaStream_t s) {
+  sym_advance_kernel<<<1, 1, 0, s>>>(p.dt, sym);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// BFECC
+// ---------------------------------------------------------------------------
+
+template <typename Real>
+struct BfeccArgs {
+  int nx, ny;
+  Real dt, hx, hy, tc;
+};
+
+// Neighbour indices of the passes (advFDBFECC.cu:112-126), with "outside
+// the domain" extended to "not tissue" when there are holes.
+struct BIdx {
+  int W, E, S, N, cW, W2, cE, E2, cS, S2, cN, N2;
+};
+
+template <bool HOLES>
+__device__ __forceinline__ BIdx bfecc_idx(int i, int j, int nx, int ny,
+                                          const uint8_t *solid, bool &sc) {
+  const int C = i + nx * j;
+  bool hw = i > 0, he = i < nx - 1, hs = j > 0, hn = j < ny - 1;
+  sc = true;
+  if (HOLES) {
+    sc = solid[C] != 0;
+    if (!sc) {
+      BIdx r = {C, C, C, C, C, C, C, C, C, C, C, C};
+      return r;
+    }
+    hw = hw && solid[C - 1];
+    he = he && solid[C + 1];
+    hs = hs && solid[C - nx];
+    hn = hn && solid[C + nx];
+  }
+  BIdx r;
+  r.W = hw ? C - 1 : (he ? C + 1 : C);
+  r.E = he ? C + 1 : (hw ? C - 1 : C);
+  r.S = hs ? C - nx : (hn ? C + nx : C);
+  r.N = hn ? C + nx : (hs ? C - nx : C);
+  r.cW = hw ? C : (he ? C + 1 : C);
+  r.W2 = hw ? C - 1 : C;
+  r.cE = he ? C : (hw ? C - 1 : C);
+  r.E2 = he ? C + 1 : C;
+  r.cS = hs ? C : (hn ? C + nx : C);
+  r.S2 = hs ? C - nx : C;
+  r.cN = hn ? C : (hs ? C - nx : C);
+  r.N2 = hn ? C + nx : C;
+  return r;
+}
+
+// cx = -adv.x, Rx = sign(cx)*cx*dt/hx (advFDBFECC.cu:30-34).
+template <typename Real>
+__device__ __forceinline__ void bfecc_ratios(const BfeccArgs<Real> &a, Real ax,
+                                             Real ay, Real &cx, Real &cy,
+                                             Real &Rx, Real &Ry) {
+  cx = -ax;
+  cy = -ay;
+  const Real sx = cx > Real(0) ? Real(1) : (cx < Real(0) ? Real(-1) : Real(0));
+  const Real sy = cy > Real(0) ? Real(1) : (cy < Real(0) ? Real(-1) : Real(0));
+  Rx = sx * cx * a.dt / a.hx;
+  Ry = sy * cy * a.dt / a.hy;
+}
+
+template <int PASS, int NF, typename Real, bool HOLES>
+__global__ void __launch_bounds__(256)
+    bfecc_pass(const BfeccArgs<Real> a, const Fld<Real> in, const Fld<Real> uf,
+               const Fld<Real> ue, const Fld<Real> out,
+               const Real *__restrict__ adv_rows,
+               const Real *__restrict__ adv_cols,
+               const uint8_t *__restrict__ solid) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.nx, ny = a.ny;
+  if (i >= nx || j >= ny) return;
+  const int C = i + nx * j;
+  bool sc;
+  const BIdx n = bfecc_idx<HOLES>(i, j, nx, ny, solid, sc);
+  Real cx, cy, Rx, Ry;
+  bfecc_ratios(a, sc ? adv_rows[j] : Real(0), sc ? adv_cols[i] : Real(0), cx,
+               cy, Rx, Ry);
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    if (PASS == 1) {
+      const Real *__restrict__ g = in.f[f];
+      const Real FDx = cx > Real(0) ? g[C] - g[n.W] : g[C] - g[n.E];
+      const Real FDy = cy > Real(0) ? g[C] - g[n.S] : g[C] - g[n.N];
+      uf.f[f][C] = g[C] - a.tc * (Rx * FDx + Ry * FDy);
+    } else if (PASS == 2) {
+      const Real *__restrict__ q = uf.f[f];
+      const Real FDx = cx > Real(0) ? q[n.cE] - q[n.E2] : q[n.cW] - q[n.W2];
+      const Real FDy = cy > Real(0) ? q[n.cN] - q[n.N2] : q[n.cS] - q[n.S2];
+      const Real ub = q[C] - a.tc * (Rx * FDx + Ry * FDy);
+      const Real g = in.f[f][C];
+      ue.f[f][C] = g - Real(0.5) * (ub - g);
+    } else {
+      const Real *__restrict__ q = ue.f[f];
+      const Real FDx = cx > Real(0) ? q[C] - q[n.W] : q[C] - q[n.E];
+      const Real FDy = cy > Real(0) ? q[C] - q[n.S] : q[C] - q[n.N];
+      const Real r = q[C] - a.tc * (Rx * FDx + Ry * FDy);
+      out.f[f][C] = sc ? r : Real(0);
+    }
+  }
+}
+
+template <int NF, typename Real, bool HOLES>
+static cudaError_t bfecc_nf(const BfeccArgs<Real> &a, const Fld<Real> &in,
+                            const Fld<Real> &out, const Real *ar,
+                            const Real *ac, const uint8_t *solid,
+                            const Fld<Real> &uf, const Fld<Real> &ue,
+                            cudaStream_t s) {
+  const dim3 block(32, 8);
+  const dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8);
+  bfecc_pass<1, NF, Real, HOLES>
+      <<<grid, block, 0, s>>>(a, in, uf, ue, out, ar, ac, solid);
+  bfecc_pass<2, NF, Real, HOLES>
+      <<<grid, block, 0, s>>>(a, in, uf, ue, out, ar, ac, solid);
+  bfecc_pass<3, NF, Real, HOLES>
+      <<<grid, block, 0, s>>>(a, in, uf, ue, out, ar, ac, solid);
+  return cudaGetLastError();
+}
+
+template <typename Real>
+cudaError_t launch_bfecc(const yh_param_var &p, int nf, const Fld<Real> &in,
+                         const Fld<Real> &out, const Real *adv_rows,
+                         const Real *adv_cols, const uint8_t *solid,
+                         const Fld<Real> &uf, const Fld<Real> &ue,
+                         cudaStream_t s) {
+  BfeccArgs<Real> a;
+  a.nx = p.nx;
+  a.ny = p.ny;
+  a.dt = (Real)p.dt;
+  a.hx = (Real)p.hx;
+  a.hy = (Real)p.hy;
+  a.tc = (Real)p.tc;
+  const bool holes = p.solidSwitch && solid;
+  if (nf == 2)
+    return holes ? bfecc_nf<2, Real, true>(a, in, out, adv_rows, adv_cols,
+                                           solid, uf, ue, s)
+                 : bfecc_nf<2, Real, false>(a, in, out, adv_rows, adv_cols,
+                                            solid, uf, ue, s);
+  return holes ? bfecc_nf<3, Real, true>(a, in, out, adv_rows, adv_cols, solid,
+                                         uf, ue, s)
+               : bfecc_nf<3, Real, false>(a, in, out, adv_rows, adv_cols,
+                                          solid, uf, ue, s);
+}
+
+#define YH_INST(Real)                                                         \
+  template cudaError_t launch_tips<Real>(                                     \
+      const yh_param_var &, const Real *, const Real *, const uint8_t *,      \
+      double, int *, yh_tip *, int, yh_sym_state *, unsigned int *,           \
+      cudaStream_t);                                                          \
+  template cudaError_t launch_phase<Real>(                                    \
+      const yh_param_var &, int, const Fld<Real> &, const Fld<Real> &,        \
+      const Fld<Real> &, const Fld<Real> &, const Fld<Real> &,                \
+      const double *, const double *, const uint8_t *, yh_sym_state *,        \
+      void *, cudaStream_t);                                                  \
+  template cudaError_t launch_template<Real>(                                 \
+      const yh_param_var &, int, const Fld<Real> &, const Fld<Real> &,        \
+      const Fld<Real> &, const Fld<Real> &, cudaStream_t);                    \
+  template cudaError_t launch_bfecc<Real>(                                    \
+      const yh_param_var &, int, const Fld<Real> &, const Fld<Real> &,        \
+      const Real *, const Real *, const uint8_t *, const Fld<Real> &,         \
+      const Fld<Real> &, cudaStream_t);
+YH_INST(float)
+YH_INST(double)
+#undef YH_INST
+
+}  // namespace yh

@@ -1,0 +1,124 @@
+"""The solver handle (yh_create ... yh_destroy) as a Python class.
+
+Host arrays are numpy FP32 (flat nx*ny, row-major idx = i + nx*j). The handle
+owns its device buffers; `run` replays captured CUDA graphs.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+from ._loader import load
+from .ops import check
+
+
+def _f32(x):
+    return np.ascontiguousarray(x, dtype=np.float32)
+
+
+def _fptr(x):
+    return None if x is None else x.ctypes.data_as(C.c_void_p)
+
+
+class Monodomain:
+    """One grid of the 2D monodomain model on the GPU."""
+
+    def __init__(self, p, model=A.YH_MODEL_FK3V, fk=None, solid=None,
+                 stream=None):
+        self.lib = load()
+        self.p = p.copy()
+        self.model = model
+        self.nf = A.NFIELDS[model]
+        self.fk = fk if fk is not None else A.fk_defaults()
+        self._solid = None
+        if solid is not None:
+            self._solid = np.ascontiguousarray(solid, dtype=np.uint8)
+            self.p.solidSwitch = True
+        h = C.c_void_p()
+        check("yh_create", self.lib.yh_create(
+            C.byref(self.p), model, C.byref(self.fk),
+            None if self._solid is None else self._solid.ctypes.data_as(C.c_void_p),
+            C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.h = h
+
+    @property
+    def n(self):
+        return self.p.nx * self.p.ny
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.yh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, u, v, w=None):
+        arrs = [_f32(u), _f32(v), None if w is None else _f32(w)]
+        self._keep = arrs
+        check("yh_set_state", self.lib.yh_set_state(
+            self.h, *[_fptr(a) for a in arrs]))
+
+    def get_state(self):
+        out = [np.empty(self.n, np.float32) for _ in range(self.nf)]
+        ptrs = [_fptr(a) for a in out] + [None] * (3 - self.nf)
+        check("yh_get_state", self.lib.yh_get_state(self.h, *ptrs))
+        return out
+
+    def state_device(self):
+        f = A.Fields()
+        check("yh_state_device", self.lib.yh_state_device(self.h, C.byref(f)))
+        return f
+
+    def set_time_block(self, k):
+        check("yh_set_time_block", self.lib.yh_set_time_block(self.h, int(k)))
+
+    def run(self, nsteps, stims=()):
+        arr = (A.Stim * max(1, len(stims)))(*stims)
+        check("yh_run", self.lib.yh_run(self.h, int(nsteps), arr, len(stims)))
+
+    def synchronize(self):
+        check("yh_synchronize", self.lib.yh_synchronize(self.h))
+
+    def step_count(self):
+        s = C.c_int()
+        check("yh_get_step", self.lib.yh_get_step(self.h, C.byref(s)))
+        return s.value
+
+    def launch_count(self):
+        n = C.c_longlong()
+        check("yh_get_launch_count",
+              self.lib.yh_get_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def track_tips(self):
+        check("yh_track_tips", self.lib.yh_track_tips(self.h))
+
+    def get_tips(self, capacity=1 << 16):
+        buf = (A.Tip * capacity)()
+        n = C.c_int()
+        st = self.lib.yh_get_tips(self.h, buf, capacity, C.byref(n))
+        if st not in (A.YH_OK, A.YH_EOVERFLOW):
+            check("yh_get_tips", st)
+        m = min(n.value, capacity)
+        return np.array([[buf[k].x, buf[k].y, buf[k].vx, buf[k].vy, buf[k].t]
+                         for k in range(m)], np.float32).reshape(m, 5)
+
+    def sr_begin(self, template_mode=A.YH_TEMPLATE_CURRENT, template=None):
+        t = [None, None, None]
+        if template is not None:
+            t = [_f32(x) for x in template] + [None] * (3 - len(template))
+        self._tkeep = t
+        check("yh_sr_begin", self.lib.yh_sr_begin(
+            self.h, template_mode, *[_fptr(a) for a in t]))
+
+    def sr_step(self, nsteps=1):
+        check("yh_sr_step", self.lib.yh_sr_step(self.h, int(nsteps)))
+
+    def get_sym(self):
+        s = A.SymState()
+        check("yh_get_sym", self.lib.yh_get_sym(self.h, C.byref(s)))
+        return s

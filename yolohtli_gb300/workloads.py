@@ -1,0 +1,108 @@
+"""Seeded synthetic workloads of the FK3V tissue benchmarks (no datasets:
+every input is generated on the host from a seed with numpy's PCG64).
+
+fk_spiral_256      256x256, 10,000 steps, S1 columns 0-9 at t=0, S2 lower-left
+                   quadrant at t=320 ms: one spiral.
+fk_holes_1024      1024x1024, 20,000 steps, 300 circular holes (r ~ U[2,6]
+                   cells), 12 S2 patches of 40x40 at uniform positions and
+                   times ~ U[200,400] ms: fibrillation-like.
+All use dx = 0.025 cm, D = 0.001 cm^2/ms, dt = 0.05 ms (D dt/dx^2 = 0.08),
+the Fenton-Karma BR-fit parameters, u = U(-0.01, 0.01), v = w = 1.
+"""
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi as A
+
+
+@dataclass
+class Workload:
+    name: str
+    p: A.ParamVar
+    fk: A.FKParams
+    model: int
+    u0: np.ndarray
+    v0: np.ndarray
+    w0: np.ndarray
+    solid: object  # np.uint8 mask (1 = tissue) or None
+    stims: list = field(default_factory=list)
+    nsteps: int = 0
+
+    @property
+    def cells(self):
+        return self.p.nx * self.p.ny
+
+    def state0(self):
+        return [self.u0.copy(), self.v0.copy(), self.w0.copy()]
+
+
+def _ic(nx, ny, rng):
+    u = rng.uniform(-0.01, 0.01, size=nx * ny).astype(np.float32)
+    v = np.ones(nx * ny, np.float32)
+    w = np.ones(nx * ny, np.float32)
+    # S1: u = 1 on columns 0-9 at t = 0
+    u.reshape(ny, nx)[:, :10] = 1.0
+    return u, v, w
+
+
+def hole_mask(nx, ny, nholes, rmin, rmax, rng):
+    """1 = tissue, 0 = hole: `nholes` discs, radius ~ U[rmin, rmax] cells,
+    centres uniform over the grid (the reference's mask polarity, main.cu:679)."""
+    solid = np.ones((ny, nx), np.uint8)
+    jj, ii = np.mgrid[0:ny, 0:nx]
+    cx = rng.uniform(0, nx, nholes)
+    cy = rng.uniform(0, ny, nholes)
+    r = rng.uniform(rmin, rmax, nholes)
+    for k in range(nholes):
+        x0, x1 = int(max(0, cx[k] - r[k] - 1)), int(min(nx, cx[k] + r[k] + 2))
+        y0, y1 = int(max(0, cy[k] - r[k] - 1)), int(min(ny, cy[k] + r[k] + 2))
+        sub = (ii[y0:y1, x0:x1] - cx[k]) ** 2 + (jj[y0:y1, x0:x1] - cy[k]) ** 2
+        solid[y0:y1, x0:x1][sub <= r[k] ** 2] = 0
+    return solid.ravel()
+
+
+def stim(step, i0, j0, i1, j1, value=1.0):
+    s = A.Stim()
+    s.step, s.i0, s.j0, s.i1, s.j1, s.value = int(step), i0, j0, i1, j1, value
+    return s
+
+
+def fk_spiral_256(seed=0, n=256, nsteps=10000):
+    rng = np.random.default_rng(seed)
+    p = A.fk_tissue_params(n, n)
+    u, v, w = _ic(n, n, rng)
+    dt = p.dt
+    s2 = stim(int(round(320.0 / dt)), 0, 0, n // 2, n // 2)
+    return Workload("fk_spiral_%d" % n, p, A.fk_defaults(), A.YH_MODEL_FK3V,
+                    u, v, w, None, [s2], nsteps)
+
+
+def fk_holes_1024(seed=0, n=1024, nsteps=20000, nholes=300, npatch=12):
+    rng = np.random.default_rng(seed)
+    p = A.fk_tissue_params(n, n)
+    u, v, w = _ic(n, n, rng)
+    solid = hole_mask(n, n, nholes, 2.0, 6.0, rng)
+    p.solidSwitch = True
+    u[solid == 0] = 0.0
+    v[solid == 0] = 0.0
+    w[solid == 0] = 0.0
+    stims = []
+    for _ in range(npatch):
+        i0 = int(rng.integers(0, n - 40))
+        j0 = int(rng.integers(0, n - 40))
+        t = rng.uniform(200.0, 400.0)
+        stims.append(stim(int(round(t / p.dt)), i0, j0, i0 + 40, j0 + 40))
+    stims.sort(key=lambda s: s.step)
+    return Workload("fk_holes_%d" % n, p, A.fk_defaults(), A.YH_MODEL_FK3V,
+                    u, v, w, solid, stims, nsteps)
+
+
+def ref2v_cross(nx, ny):
+    """The reference's own initial condition: the cross-field stimulation of
+    initGates (main.cu:604-618): u = 1 for i < nx/8, v = 1 for j >= ny/2."""
+    u = np.zeros((ny, nx))
+    v = np.zeros((ny, nx))
+    u[:, : nx // 8] = 1.0
+    v[ny // 2:, :] = 1.0
+    return u.ravel(), v.ravel()
