@@ -148,13 +148,16 @@ def cpu_baseline(wl, seconds=10.0):
                           elapsed)}
 
 
-def config_of(wl, args, tb):
+def config_of(wl, args, tb, autotuned=False):
+    state_mb = 12.0 * wl.cells / 2 ** 20
     return {"workload": wl.name, "grid": [wl.p.nx, wl.p.ny],
             "steps_per_solve": wl.nsteps, "model": "FK3V",
-            "holes": 300, "s2_patches": len(wl.stims),
+            "holes": int(round(300 * wl.cells / 2 ** 20)),
+            "s2_patches": len(wl.stims),
             "cells": wl.cells, "dt_ms": wl.p.dt, "dx_cm": wl.p.hx,
-            "time_block": tb,
-            "l2": "256 MB write between solves; 12.6 MB state L2-resident within a solve",
+            "time_block": tb, "time_block_autotuned": autotuned,
+            "l2": "256 MB write between solves; %.1f MB state%s within a solve" % (
+                state_mb, " L2-resident" if 2 * state_mb < 100 else ""),
             "parallelism": "replicas x%d" % args.gpus}
 
 
@@ -202,14 +205,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--time-block", type=int, default=0,
-                    help="steps per kernel launch (0: library default)")
+                    help="steps per kernel launch (0: autotuned before timing)")
     ap.add_argument("--nsteps", type=int, default=20000,
                     help="explicit steps per solve (the workload's 20,000)")
+    ap.add_argument("--grid", type=int, default=1024,
+                    help="grid side (1024 = the benchmark; larger sides are "
+                         "for profiling beyond the L2, holes scaled by area)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
 
     from yolohtli_gb300 import workloads as W
-    wl = W.fk_holes_1024(seed=0, nsteps=args.nsteps)
+    scale = (args.grid / 1024.0) ** 2
+    wl = W.fk_holes_1024(seed=0, n=args.grid, nsteps=args.nsteps,
+                         nholes=int(round(300 * scale)))
 
     if args.impl == "reference":
         run_reference(args, wl)
@@ -229,9 +237,15 @@ def main():
 
     stream = torch.cuda.Stream()
     m = Monodomain(wl.p, wl.model, wl.fk, solid=wl.solid, stream=stream.cuda_stream)
-    tb = args.time_block if args.time_block > 0 else 1
-    m.set_time_block(tb)
     ic = [torch.tensor(x, device="cuda") for x in wl.state0()]
+    autotuned = args.time_block <= 0
+    if autotuned:
+        # the library's autotuner, on the workload's initial state (restored)
+        m.set_state(*wl.state0())
+        tb = m.autotune_time_block(512)
+    else:
+        m.set_time_block(args.time_block)
+        tb = m.time_block()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     lib = m.lib
 
@@ -286,19 +300,29 @@ def main():
     cell_steps = wl.cells * wl.nsteps * args.steps * world
     value = cell_steps / (ms_max * 1e-3) / 1e9
 
-    # dominant kernel: the RD step; per launch `tb` steps of all cells
-    rd_launches = args.steps * (-(-wl.nsteps // tb) if tb > 1 else wl.nsteps)
-    avg_launch_s = ms * 1e-3 / rd_launches  # upper bound: includes stim kernels and gaps
-    bytes_alg = 25.0 * wl.cells * tb      # u,v,w read+write FP32 + 1-byte mask
+    # Dominant kernel: the RD step (the 12 stimulus kernels per solve are
+    # the only other launches). Algorithmic bytes: 25 B per cell-step
+    # (u, v, w read + write in FP32 and the 1-byte hole mask); one launch
+    # advances all cells by steps_per_launch steps. The mean launch time is
+    # taken over the whole timed region, so it also carries the stimulus
+    # kernels, the L2 flushes and the gaps between launches.
+    rd_launches = max(1, launches - args.steps * len(wl.stims))
+    steps_per_launch = wl.nsteps * args.steps / rd_launches
+    avg_launch_s = ms * 1e-3 / rd_launches
+    bytes_alg = 25.0 * wl.cells * steps_per_launch
     achieved = bytes_alg / avg_launch_s / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = profiled_traffic("rd_fk3v_holes_1024_tb%d" % tb)
+    traffic = profiled_traffic("%s_tb%d" % (wl.name, tb))
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "traffic": traffic, "peak_kind": peak_kind,
                 "alg_bytes_per_cell_step": 25,
-                "note": "achieved = 25 B x cells x steps-per-launch / mean launch "
-                        "time over the timed region; state L2-resident"}
+                "steps_per_launch": round(steps_per_launch, 3),
+                "mean_launch_us": round(avg_launch_s * 1e6, 3),
+                "kernel": "rd_tb_kernel" if tb > 1 else "rd_step_vec4",
+                "note": "achieved = 25 B x cells x steps_per_launch / mean launch "
+                        "time; frac > 1 is possible: the state stays in L2 and "
+                        "temporal blocking re-reads it once per steps_per_launch"}
 
     # end to end through the public C ABI with pinned host buffers
     e2e = None
@@ -337,7 +361,7 @@ def main():
             "ms_per_step": round(ms_max / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": config_of(wl, args, tb),
+            "config": config_of(wl, args, tb, autotuned),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clk,
         }

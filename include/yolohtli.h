@@ -333,8 +333,15 @@ int yh_get_state(yh_solver *h, float *u, float *v, float *w);
 int yh_state_device(yh_solver *h, yh_fields *cur);
 
 /* Steps per kernel launch of the plain solver (temporal blocking depth);
- * 1 = one launch per step. Values are clamped to what the kernel supports. */
+ * 1 = one launch per step. Values are clamped to what the model allows
+ * (1..8; always 1 for REF2V with gateDiff, whose v diffuses too). */
 int yh_set_time_block(yh_solver *h, int steps_per_launch);
+int yh_get_time_block(yh_solver *h, int *steps_per_launch);
+
+/* Autotuner: times probe_steps plain steps from the current state for each
+ * allowed depth, restores the state and counters, keeps the fastest depth
+ * and returns it in *best. */
+int yh_autotune_time_block(yh_solver *h, int probe_steps, int *best);
 
 /* nsteps plain explicit steps with the stimulus events of `stims` whose step
  * lies in [h.step, h.step + nsteps), captured and replayed as a CUDA graph. */

@@ -1,0 +1,90 @@
+"""GPU tests of the temporally blocked step (K explicit steps per launch)
+and of the time-block autotuner, through the solver handle."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from yolohtli_gb300 import _abi as A
+from yolohtli_gb300 import workloads as W
+from yolohtli_gb300.solver import Monodomain
+
+from gpu_util import max_abs, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def fk_case(nx, ny, holes, seed=4):
+    rng = np.random.default_rng(seed)
+    p = A.fk_tissue_params(nx, ny)
+    u = rng.uniform(0, 1, nx * ny).astype(np.float32)
+    v = rng.uniform(0, 1, nx * ny).astype(np.float32)
+    w = rng.uniform(0, 1, nx * ny).astype(np.float32)
+    solid = None
+    if holes:
+        solid = W.hole_mask(nx, ny, 25, 2.0, 6.0, rng)
+        p.solidSwitch = True
+        for f in (u, v, w):
+            f[solid == 0] = 0
+    # a smooth excitation so that fronts move through tile boundaries
+    jj, ii = np.mgrid[0:ny, 0:nx]
+    u[((ii - nx // 3) ** 2 + (jj - ny // 2) ** 2 < 400).ravel()] = 1.0
+    return p, [u, v, w], solid
+
+
+def run(p, st, solid, nsteps, k, stims=()):
+    m = Monodomain(p, A.YH_MODEL_FK3V, A.fk_defaults(), solid=solid)
+    m.set_state(*st)
+    m.set_time_block(k)
+    assert m.time_block() == k
+    m.run(nsteps, stims)
+    out = m.get_state()
+    m.close()
+    return out
+
+
+@pytest.mark.parametrize("nx,ny", [(300, 170), (256, 128), (97, 61)])
+@pytest.mark.parametrize("holes", [False, True])
+def test_blocked_steps_equal_single_steps(nx, ny, holes):
+    p, st, solid = fk_case(nx, ny, holes)
+    ref = run(p, st, solid, 96, 1)
+    for k in range(2, 9):
+        got = run(p, st, solid, 96, k)
+        for f in range(3):
+            d = max_abs(got[f], ref[f])
+            assert d <= 2e-6, (k, f, d)
+
+
+def test_blocked_protocol_with_stimuli_matches_oracle():
+    p, st, solid = fk_case(256, 192, True)
+    stims = [W.stim(40, 10, 10, 60, 60), W.stim(133, 150, 100, 200, 150)]
+    got = run(p, st, solid, 300, 6, stims)
+    ref = O.run(p, A.YH_MODEL_FK3V, A.fk_defaults(), st, 300, stims, solid=solid)
+    assert rel_l2(got[0], ref[0]) < 1e-5
+    assert np.all(got[0][solid == 0] == 0)
+
+
+def test_autotune_picks_a_depth_and_restores_the_state():
+    p, st, solid = fk_case(512, 512, True)
+    m = Monodomain(p, A.YH_MODEL_FK3V, A.fk_defaults(), solid=solid)
+    m.set_state(*st)
+    before = m.get_state()
+    n0 = m.launch_count()
+    k = m.autotune_time_block(128)
+    after = m.get_state()
+    assert 1 <= k <= 8 and m.time_block() == k
+    assert m.step_count() == 0 and m.launch_count() == n0
+    for f in range(3):
+        assert np.array_equal(before[f], after[f])
+    m.close()
+
+
+def test_ref2v_with_diffusing_v_stays_at_one_step_per_launch():
+    p = A.param_defaults(64, 64)  # gateDiff = 1
+    m = Monodomain(p, A.YH_MODEL_REF2V, None)
+    m.set_time_block(6)
+    assert m.time_block() == 1
+    q = p.copy()
+    q.gateDiff = False
+    m2 = Monodomain(q, A.YH_MODEL_REF2V, None)
+    m2.set_time_block(6)
+    assert m2.time_block() == 6

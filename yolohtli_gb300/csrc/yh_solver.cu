@@ -66,6 +66,7 @@ struct yh_solver {
   bool sr_ready = false;
   bool frozen = false;
   long long launches = 0;  // kernels enqueued by this handle
+  bool own_stream = false;
   GraphCache plain[2];
   GraphCache sr[2];
 };
@@ -98,8 +99,15 @@ extern "C" int yh_create(const yh_param_var *p, int model,
   h->s = (cudaStream_t)stream;
   h->n = (size_t)p->nx * p->ny;
   h->stride = (h->n + 63) & ~(size_t)63;  // 256-byte aligned fields
-  cudaError_t e =
-      cudaMalloc(&h->pool, 2 * h->nf * h->stride * sizeof(float));
+  cudaError_t e = cudaSuccess;
+  if (!h->s) {
+    // The legacy default stream cannot be captured into a graph: use a
+    // blocking stream of our own, which still orders with it.
+    e = cudaStreamCreate(&h->s);
+    h->own_stream = e == cudaSuccess;
+  }
+  if (e == cudaSuccess)
+    e = cudaMalloc(&h->pool, 2 * h->nf * h->stride * sizeof(float));
   if (e == cudaSuccess)
     e = cudaMemsetAsync(h->pool, 0, 2 * h->nf * h->stride * sizeof(float),
                         h->s);
@@ -142,6 +150,7 @@ extern "C" int yh_destroy(yh_solver *h) {
   cudaFree(h->ws);
   cudaFree(h->adv_d);
   cudaFree(h->adv_f);
+  if (h->own_stream) cudaStreamDestroy(h->s);
   delete h;
   return YH_OK;
 }
@@ -190,11 +199,24 @@ extern "C" int yh_get_step(yh_solver *h, int *step) {
   return YH_OK;
 }
 
+// The blocked kernel exchanges only u between sub-steps: models where v
+// diffuses too (REF2V with gateDiff) take one launch per step.
+static int max_time_block(const yh_solver *h) {
+  if (h->model == YH_MODEL_REF2V && h->p.gateDiff) return 1;
+  return rd_tb_max_steps();
+}
+
 extern "C" int yh_set_time_block(yh_solver *h, int k) {
   if (!h) return YH_EINVAL;
   if (k < 1) k = 1;
-  const int kmax = rd_tb_max_steps();
+  const int kmax = max_time_block(h);
   h->time_block = k > kmax ? kmax : k;
+  return YH_OK;
+}
+
+extern "C" int yh_get_time_block(yh_solver *h, int *k) {
+  if (!h || !k) return YH_EINVAL;
+  *k = h->time_block;
   return YH_OK;
 }
 
@@ -308,6 +330,60 @@ static int run_plain(yh_solver *h, int len) {
     h->step += len;
   }
   return YH_OK;
+}
+
+// Times `probe_steps` plain steps from the current state for every time
+// block depth the model allows (one warm-up run each, CUDA events on the
+// handle's stream), restores the state, step and launch counters, and keeps
+// the fastest depth. Returns it in *best.
+extern "C" int yh_autotune_time_block(yh_solver *h, int probe_steps,
+                                      int *best) {
+  if (!h || probe_steps < 1) return YH_EINVAL;
+  const size_t bytes = h->n * sizeof(float);
+  float *save = nullptr;
+  cudaError_t e = cudaMalloc(&save, h->nf * bytes);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  for (int f = 0; f < h->nf && e == cudaSuccess; ++f)
+    e = cudaMemcpyAsync(save + f * h->n, h->cur.f[f], bytes,
+                        cudaMemcpyDeviceToDevice, h->s);
+  const int step0 = h->step;
+  const long long launches0 = h->launches;
+  const int kmax = max_time_block(h);
+  int best_k = 1;
+  float best_ms = 1e30f;
+  int rc = st(e);
+  for (int k = 1; k <= kmax && rc == YH_OK; ++k) {
+    h->time_block = k;
+    float ms = 0.f;
+    for (int rep = 0; rep < 2 && rc == YH_OK; ++rep) {
+      for (int f = 0; f < h->nf && rc == YH_OK; ++f)
+        rc = st(cudaMemcpyAsync(h->cur.f[f], save + f * h->n, bytes,
+                                cudaMemcpyDeviceToDevice, h->s));
+      if (rc == YH_OK) rc = st(cudaEventRecord(e0, h->s));
+      if (rc == YH_OK) rc = run_plain(h, probe_steps);
+      if (rc == YH_OK) rc = st(cudaEventRecord(e1, h->s));
+      if (rc == YH_OK) rc = st(cudaEventSynchronize(e1));
+      if (rc == YH_OK) rc = st(cudaEventElapsedTime(&ms, e0, e1));
+    }
+    if (rc == YH_OK && ms < best_ms) {
+      best_ms = ms;
+      best_k = k;
+    }
+  }
+  for (int f = 0; f < h->nf && rc == YH_OK; ++f)
+    rc = st(cudaMemcpyAsync(h->cur.f[f], save + f * h->n, bytes,
+                            cudaMemcpyDeviceToDevice, h->s));
+  if (rc == YH_OK) rc = st(cudaStreamSynchronize(h->s));
+  h->step = step0;
+  h->launches = launches0;
+  h->time_block = best_k;
+  if (best) *best = best_k;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(save);
+  return rc;
 }
 
 extern "C" int yh_run(yh_solver *h, int nsteps, const yh_stim *stims,

@@ -76,6 +76,17 @@ class Monodomain:
     def set_time_block(self, k):
         check("yh_set_time_block", self.lib.yh_set_time_block(self.h, int(k)))
 
+    def time_block(self):
+        k = C.c_int()
+        check("yh_get_time_block", self.lib.yh_get_time_block(self.h, C.byref(k)))
+        return k.value
+
+    def autotune_time_block(self, probe_steps=256):
+        k = C.c_int()
+        check("yh_autotune_time_block", self.lib.yh_autotune_time_block(
+            self.h, int(probe_steps), C.byref(k)))
+        return k.value
+
     def run(self, nsteps, stims=()):
         arr = (A.Stim * max(1, len(stims)))(*stims)
         check("yh_run", self.lib.yh_run(self.h, int(nsteps), arr, len(stims)))
