@@ -27,6 +27,28 @@ def test_library_loads_and_exports_all_declared_symbols():
     assert missing == []
 
 
+REFERENCE_HOST_SYMBOLS = [  # hostPrototypes.h:22-42, as the reference exports them
+    "_Z25reactionDiffusion_wrapperm4dim3S_8stateVarS0_S0_S0_bPbbPdb4int2",
+    "_Z11tip_wrapperm4dim3S_8stateVarS0_S0_dibPbPiP7vec5dyn",
+    "_Z13slice_wrapperm4dim3S_8stateVar8sliceVarS1_bb6advVariPbPiP7vec5dyni",
+    "_Z17Cxy_field_wrapperm4dim3S_6advVar5REAL3S1_Pb",
+    "_Z18advFDBFECC_wrapperm4dim3S_8stateVarS0_6advVarS0_S0_S0_Pb",
+    "_Z12solve_matrix5REAL3S_Pd",
+    "_Z13trapz_wrapper4dim3S_8sliceVarS0_8stateVarPdS2_PiP7vec5dyni",
+]
+
+
+def test_compat_exports_the_reference_host_symbols():
+    lib = load()
+    for name in REFERENCE_HOST_SYMBOLS + declared("yolohtli_compat.h"):
+        assert hasattr(lib, name), name
+    ref = os.path.join(ROOT, "oracle", "_ref", "libref_host.so")
+    if os.path.exists(ref):  # the reference's own host library, built here
+        r = C.CDLL(ref)
+        for name in REFERENCE_HOST_SYMBOLS:
+            assert hasattr(r, name), name
+
+
 def test_struct_sizes_match_ctypes():
     lib = load()
     for name, ct in [("yh_param_var", A.ParamVar), ("yh_fk_params", A.FKParams),

@@ -259,9 +259,10 @@ extern "C" int yh_spiral_tip(const yh_param_var *p, const float *g_past,
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(tip_count, 0, sizeof(int), s);
   if (e != cudaSuccess) return cuda_status(e);
+  (void)solid;  // the hole branch uses a disc, not the mask
   return cuda_status(launch_tips<float>(*p, g_past, g_present,
-                                        p->solidSwitch ? solid : nullptr,
-                                        physical_time, tip_count, tip_vector,
+                                        p->solidSwitch, physical_time,
+                                        tip_count, tip_vector,
                                         capacity, nullptr, nullptr, s));
 }
 

@@ -78,10 +78,23 @@ __device__ __forceinline__ void ref2v_currents(const StepCoeffs<Real> &a,
   I_v = -(a.eps * (a.delta * (u - a.gamma) * (a.beta - u) - v - a.theta));
 }
 
+// PTX approximate base-2 exponential and reciprocal (one MUFU operation
+// each; relative error below 2^-22), enough for the 1e-5 FP32 budget.
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ float fk_sigmoid(const StepCoeffs<float> &a,
                                             float u) {
   // (1 + tanh(k (u - u_csi))) / 2 = 1 / (1 + exp(-2k (u - u_csi)))
-  return __frcp_rn(1.0f + exp2f(a.k_exp2 * (u - a.u_csi)));
+  return rcp_approx(1.0f + ex2_approx(a.k_exp2 * (u - a.u_csi)));
 }
 __device__ __forceinline__ double fk_sigmoid(const StepCoeffs<double> &a,
                                              double u) {

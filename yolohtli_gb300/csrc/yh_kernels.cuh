@@ -26,10 +26,12 @@ cudaError_t launch_stimulate(Real *u, const uint8_t *solid, int nx, int ny,
                              cudaStream_t s);
 
 // yh_sr.cu
+// holes: the hole-domain branch of the reference (a disc around the grid
+// centre, tipTracker.cu:47-122); it does not read the mask itself.
 template <typename Real>
 cudaError_t launch_tips(const yh_param_var &p, const Real *past,
-                        const Real *present, const uint8_t *solid,
-                        double ptime, int *count, yh_tip *vec, int cap,
+                        const Real *present, bool holes, double ptime,
+                        int *count, yh_tip *vec, int cap,
                         yh_sym_state *sym_pick, unsigned int *done,
                         cudaStream_t s);
 cudaError_t launch_pick_centre(const int *count, const yh_tip *vec, int cap,
@@ -58,6 +60,59 @@ cudaError_t launch_bfecc(const yh_param_var &p, int nf, const Fld<Real> &in,
                          const Real *adv_cols, const uint8_t *solid,
                          const Fld<Real> &uf, const Fld<Real> &ue,
                          cudaStream_t s);
+// The same passes reading a full nx*ny comoving field (adv_x, adv_y), as
+// the reference's advFDBFECC_kernel receives it.
+template <typename Real>
+cudaError_t launch_bfecc_2d(const yh_param_var &p, int nf,
+                            const Fld<Real> &in, const Fld<Real> &out,
+                            const Real *adv_x, const Real *adv_y,
+                            const uint8_t *solid, const Fld<Real> &uf,
+                            const Fld<Real> &ue, cudaStream_t s);
+
+// FP64 3x3 solve of the drift/rotation system with partial pivoting.
+// Row r: [I[3r] cos(pt) + I[3r+1] sin(pt), I[3r+1] cos(pt) - I[3r] sin(pt),
+// I[3r+2]] . c = I[9+r]  (symmetryReduction.cu:390-396). Returns YH_OK, or
+// YH_ESINGULAR when a pivot is below 1e-13 of the largest entry (the
+// reference divides by unpivoted entries, symmetryReduction.cu:398-412).
+__host__ __device__ inline int solve3(const double I[12], double pt,
+                                      double c[3]) {
+  const double cs = cos(pt), sn = sin(pt);
+  double A[3][4];
+  double amax = 0.0;
+  for (int r = 0; r < 3; ++r) {
+    A[r][0] = I[3 * r] * cs + I[3 * r + 1] * sn;
+    A[r][1] = I[3 * r + 1] * cs - I[3 * r] * sn;
+    A[r][2] = I[3 * r + 2];
+    A[r][3] = I[9 + r];
+    for (int k = 0; k < 3; ++k) amax = fmax(amax, fabs(A[r][k]));
+  }
+  if (!(amax > 0.0) || !isfinite(amax)) return YH_ESINGULAR;
+  const double tol = 1e-13 * amax;
+  for (int col = 0; col < 3; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < 3; ++r)
+      if (fabs(A[r][col]) > fabs(A[piv][col])) piv = r;
+    if (!(fabs(A[piv][col]) > tol)) return YH_ESINGULAR;
+    if (piv != col)
+      for (int k = 0; k < 4; ++k) {
+        const double t = A[col][k];
+        A[col][k] = A[piv][k];
+        A[piv][k] = t;
+      }
+    for (int r = col + 1; r < 3; ++r) {
+      const double m = A[r][col] / A[col][col];
+      for (int k = col; k < 4; ++k) A[r][k] -= m * A[col][k];
+    }
+  }
+  double x[3];
+  for (int r = 2; r >= 0; --r) {
+    double s = A[r][3];
+    for (int k = r + 1; k < 3; ++k) s -= A[r][k] * x[k];
+    x[r] = s / A[r][r];
+  }
+  for (int k = 0; k < 3; ++k) c[k] = x[k];
+  return YH_OK;
+}
 cudaError_t launch_sym_advance(const yh_param_var &p, yh_sym_state *sym,
                                cudaStream_t s);
 

@@ -2,22 +2,33 @@
 // launch (FP32, models where only u diffuses: FK3V, or REF2V with
 // gateDiff = 0).
 //
-// A block of 512 threads owns a 128 x 64 region of cells: an interior of
-// (128 - 2K) x (64 - 2K) cells and a halo of K cells on each side. Each
-// thread owns 16 cells (4 columns lane + 32k x 4 rows) and keeps their v, w
-// in registers for all K sub-steps; u lives in a double-buffered
-// shared-memory copy of the region (64 KB), the only field exchanged. After sub-step
-// s the cells at distance >= s from the region edge are exact, so after K
-// sub-steps the interior is, and only the interior is stored. At the domain
-// edge the mirror ghost (helper_functions.cu:69-79) reads inward, so the
-// region does not shrink on that side. Global traffic per interior
-// cell-step is about (13 B x 128*64/interior + 12 B) / K instead of 25 B.
+// A block of 512 threads (16 warps) owns a 128 x 64 region of cells: an
+// interior of (128 - 2K) x (64 - 2K) cells and a halo of K cells on each
+// side. Thread (lane, warp) owns the 4 x 4 cells of columns 4*lane .. +3
+// and rows 4*warp .. +3 for all K sub-steps: their u in registers, their v
+// and w in the thread's own float4 slots of shared memory (no other thread
+// reads them: only u diffuses). Neighbours come from the thread's registers, from the
+// adjacent lanes by one warp shuffle per row (W of column 0, E of column 3),
+// and from the adjacent warps by one float4 row exchange in shared memory
+// per sub-step (S of the first row, N of the last): one __syncthreads per
+// sub-step.
+// After sub-step s the cells at distance >= s from the region edge are
+// exact, so after K sub-steps the interior is, and only the interior is
+// stored. At the domain edge the mirror ghost (helper_functions.cu:69-79)
+// reads inward, so the region does not shrink on that side. Global traffic
+// per interior cell-step is about (13 B x 128*64/interior + 12 B) / K
+// instead of 25 B.
 #include "yh_kernels.cuh"
 
 namespace yh {
 
 constexpr int kTbW = 128, kTbH = 64, kTbThreads = 512, kTbMaxK = 8;
-constexpr int kTbSmem = 2 * kTbW * kTbH * 4 + kTbW * kTbH;  // u x2 + mask
+constexpr int kTbWarps = kTbThreads / 32;
+constexpr int kR = kTbH / kTbWarps;  // rows per thread
+// edge rows [2 buffers][bottom/top][warps][128 floats], then the region's
+// v and w [2][64][128]
+constexpr int kTbEdge = 2 * 2 * kTbWarps * kTbW;
+constexpr int kTbSmem = (kTbEdge + 2 * kTbW * kTbH) * 4;
 
 int rd_tb_max_steps() { return kTbMaxK; }
 
@@ -34,95 +45,161 @@ __device__ __forceinline__ void pattern_weights(uint32_t pat, float &wlo,
   wc = pat == 3u ? 0.f : 2.f;
 }
 
+__device__ __forceinline__ float4 f4(const float x[4]) {
+  return make_float4(x[0], x[1], x[2], x[3]);
+}
+
 template <int MODEL, bool HOLES>
 __global__ void __launch_bounds__(kTbThreads, 1)
     rd_tb_kernel(const StepCoeffs<float> a, const Fld<float> in,
                  const Fld<float> out, const uint8_t *__restrict__ solid,
                  const int K) {
   extern __shared__ float4 smem4[];
-  float *us0 = reinterpret_cast<float *>(smem4);
-  float *us1 = us0 + kTbW * kTbH;
-  uint8_t *ms = reinterpret_cast<uint8_t *>(us1 + kTbW * kTbH);
+  float *edge = reinterpret_cast<float *>(smem4);  // [2][2][16][128]
+  float *vs = edge + kTbEdge;                      // [64][128]
+  float *ws = vs + kTbW * kTbH;                    // [64][128]
   const int nx = a.nx, ny = a.ny;
   const int TX = kTbW - 2 * K, TY = kTbH - 2 * K;
   const int x0 = (int)blockIdx.x * TX - K, y0 = (int)blockIdx.y * TY - K;
-  const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;  // wy in 0..15
-  const float *__restrict__ U = in.f[0];
-  const float *__restrict__ V = in.f[1];
-  const float *__restrict__ Wf = in.f[2];
+  const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
+  const int lx0 = 4 * lane, ly0 = kR * wy;
+  const int gx0 = x0 + lx0, gy0 = y0 + ly0;
   constexpr bool W3 = MODEL == YH_MODEL_FK3V;
 
-  float v[4][4], w[4][4];
-  // load the region: u to shared memory, v, w to registers
+  // domain-edge flags: bit k of xw/xe: column k is the first/last column;
+  // bit r of ys/yn: row r is the first/last row; inx/iny: inside the domain
+  uint32_t xw = 0, xe = 0, ys = 0, yn = 0, inx = 0, iny = 0;
 #pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int ly = wy * 4 + r, gy = y0 + ly;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int lx = lane + 32 * k, gx = x0 + lx;
-      const bool inside = (unsigned)gx < (unsigned)nx && (unsigned)gy < (unsigned)ny;
-      const size_t idx = (size_t)gy * nx + gx;
-      v[r][k] = inside ? __ldg(V + idx) : 0.f;
-      w[r][k] = (W3 && inside) ? __ldg(Wf + idx) : 0.f;
-      us0[ly * kTbW + lx] = inside ? __ldg(U + idx) : 0.f;
-      if (HOLES) ms[ly * kTbW + lx] = inside ? solid[idx] : 0;
-    }
+  for (int k = 0; k < 4; ++k) {
+    const int gx = gx0 + k;
+    xw |= (gx == 0 ? 1u : 0u) << k;
+    xe |= (gx == nx - 1 ? 1u : 0u) << k;
+    inx |= ((unsigned)gx < (unsigned)nx ? 1u : 0u) << k;
   }
-  __syncthreads();
-
-  // per-cell hole codes (bit 0 tissue, bits 1-2 x pattern, bits 3-4 y
-  // pattern), computed once from the mask and kept in shared memory in
-  // place of the mask: 1 byte per cell instead of 4 registers per thread
-  if (HOLES) {
-    uint32_t code[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int ly = wy * 4 + r, gy = y0 + ly;
-      const int lyS = min(max(gy == 0 ? ly + 1 : ly - 1, 0), kTbH - 1);
-      const int lyN = min(max(gy == ny - 1 ? ly - 1 : ly + 1, 0), kTbH - 1);
+  for (int r = 0; r < kR; ++r) {
+    const int gy = gy0 + r;
+    ys |= (gy == 0 ? 1u : 0u) << r;
+    yn |= (gy == ny - 1 ? 1u : 0u) << r;
+    iny |= ((unsigned)gy < (unsigned)ny ? 1u : 0u) << r;
+  }
+
+  float u[kR][4], v[4], w[4];
+  uint32_t m[kR];  // tissue bits of the 4 cells of a row
+  const bool vec = ((x0 & 3) == 0) && inx == 0xFu;
+#pragma unroll
+  for (int r = 0; r < kR; ++r) {
+    m[r] = 0u;
+    const bool rowin = (iny >> r) & 1u;
+    const size_t base = (size_t)(gy0 + r) * nx + gx0;
+    if (rowin && vec) {
+      const float4 q0 = __ldg(reinterpret_cast<const float4 *>(in.f[0] + base));
+      const float4 q1 = __ldg(reinterpret_cast<const float4 *>(in.f[1] + base));
+      u[r][0] = q0.x; u[r][1] = q0.y; u[r][2] = q0.z; u[r][3] = q0.w;
+      v[0] = q1.x; v[1] = q1.y; v[2] = q1.z; v[3] = q1.w;
+      if (W3) {
+        const float4 q2 = __ldg(reinterpret_cast<const float4 *>(in.f[2] + base));
+        w[0] = q2.x; w[1] = q2.y; w[2] = q2.z; w[3] = q2.w;
+      }
+    } else {
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        const int lx = lane + 32 * k, gx = x0 + lx;
-        const int lxW = min(max(gx == 0 ? lx + 1 : lx - 1, 0), kTbW - 1);
-        const int lxE = min(max(gx == nx - 1 ? lx - 1 : lx + 1, 0), kTbW - 1);
-        const bool sc = ms[ly * kTbW + lx] != 0;
-        const uint32_t px = hole_pattern(ms[ly * kTbW + lxW] != 0, sc,
-                                         ms[ly * kTbW + lxE] != 0);
-        const uint32_t py = hole_pattern(ms[lyN * kTbW + lx] != 0, sc,
-                                         ms[lyS * kTbW + lx] != 0);
+        const bool ok = rowin && ((inx >> k) & 1u);
+        u[r][k] = ok ? __ldg(in.f[0] + base + k) : 0.f;
+        v[k] = ok ? __ldg(in.f[1] + base + k) : 0.f;
+        w[k] = (W3 && ok) ? __ldg(in.f[2] + base + k) : 0.f;
+      }
+    }
+    *reinterpret_cast<float4 *>(vs + (ly0 + r) * kTbW + lx0) = f4(v);
+    if (W3) *reinterpret_cast<float4 *>(ws + (ly0 + r) * kTbW + lx0) = f4(w);
+    if (HOLES) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const bool ok = rowin && ((inx >> k) & 1u);
+        m[r] |= (ok && solid[base + k] ? 1u : 0u) << k;
+      }
+    }
+  }
+
+  // per-cell hole codes (bit 0 tissue, bits 1-2 x pattern, bits 3-4 y
+  // pattern), from the tissue bits of the cell and its mirrored neighbours
+  uint32_t code[kR];
+#pragma unroll
+  for (int r = 0; r < kR; ++r) code[r] = 0u;
+  if (HOLES) {
+    uint32_t *eb = reinterpret_cast<uint32_t *>(edge);
+    eb[wy * 32 + lane] = m[0];                       // bottom rows
+    eb[kTbWarps * 32 + wy * 32 + lane] = m[kR - 1];  // top rows
+    __syncthreads();
+    const uint32_t mS = wy > 0 ? eb[kTbWarps * 32 + (wy - 1) * 32 + lane] : m[0];
+    const uint32_t mN = wy < kTbWarps - 1 ? eb[(wy + 1) * 32 + lane] : m[kR - 1];
+#pragma unroll
+    for (int r = 0; r < kR; ++r) {
+      const uint32_t left = __shfl_up_sync(0xffffffffu, m[r], 1);
+      const uint32_t right = __shfl_down_sync(0xffffffffu, m[r], 1);
+      const uint32_t below = r > 0 ? m[r - 1] : mS;
+      const uint32_t above = r < kR - 1 ? m[r + 1] : mN;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        bool sw = k > 0 ? (m[r] >> (k - 1)) & 1u : (left >> 3) & 1u;
+        bool se = k < 3 ? (m[r] >> (k + 1)) & 1u : right & 1u;
+        bool ss = (below >> k) & 1u, sn = (above >> k) & 1u;
+        const bool tw = sw, ts = ss;
+        if ((xw >> k) & 1u) sw = se;  // mirror: W of the first column is E
+        if ((xe >> k) & 1u) se = tw;
+        if ((ys >> r) & 1u) ss = sn;
+        if ((yn >> r) & 1u) sn = ts;
+        const bool sc = (m[r] >> k) & 1u;
+        const uint32_t px = hole_pattern(sw, sc, se);
+        const uint32_t py = hole_pattern(sn, sc, ss);
         code[r] |= ((sc ? 1u : 0u) | (px << 1) | (py << 3)) << (8 * k);
       }
     }
     __syncthreads();
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        ms[(wy * 4 + r) * kTbW + lane + 32 * k] = (uint8_t)(code[r] >> (8 * k));
-    __syncthreads();
   }
 
   for (int s = 0; s < K; ++s) {
-    const float *src = (s & 1) ? us1 : us0;
-    float *dst = (s & 1) ? us0 : us1;
+    float *bot = edge + (s & 1) * 2 * kTbWarps * kTbW;
+    float *top = bot + kTbWarps * kTbW;
+    *reinterpret_cast<float4 *>(bot + wy * kTbW + lx0) = f4(u[0]);
+    *reinterpret_cast<float4 *>(top + wy * kTbW + lx0) = f4(u[kR - 1]);
+    __syncthreads();
+    const float4 qs = wy > 0 ? *reinterpret_cast<const float4 *>(top + (wy - 1) * kTbW + lx0)
+                             : f4(u[0]);
+    const float4 qn = wy < kTbWarps - 1
+                          ? *reinterpret_cast<const float4 *>(bot + (wy + 1) * kTbW + lx0)
+                          : f4(u[kR - 1]);
+    const float rowN[4] = {qn.x, qn.y, qn.z, qn.w};
+    // rows are updated in place, bottom to top: `prev` keeps the old values
+    // of the row below, which its own update has overwritten
+    float prev[4] = {qs.x, qs.y, qs.z, qs.w};
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int ly = wy * 4 + r, gy = y0 + ly;
-      const int lyS = min(max(gy == 0 ? ly + 1 : ly - 1, 0), kTbH - 1);
-      const int lyN = min(max(gy == ny - 1 ? ly - 1 : ly + 1, 0), kTbH - 1);
+    for (int r = 0; r < kR; ++r) {
+      const float left = __shfl_up_sync(0xffffffffu, u[r][3], 1);
+      const float right = __shfl_down_sync(0xffffffffu, u[r][0], 1);
+      float4 *vp = reinterpret_cast<float4 *>(vs + (ly0 + r) * kTbW + lx0);
+      float4 *wp = reinterpret_cast<float4 *>(ws + (ly0 + r) * kTbW + lx0);
+      const float4 v4 = *vp;
+      const float4 w4 = W3 ? *wp : make_float4(0.f, 0.f, 0.f, 0.f);
+      float v[4] = {v4.x, v4.y, v4.z, v4.w};
+      float w[4] = {w4.x, w4.y, w4.z, w4.w};
+      float un[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        const int lx = lane + 32 * k, gx = x0 + lx;
-        const bool inside = (unsigned)gx < (unsigned)nx && (unsigned)gy < (unsigned)ny;
-        const int lxW = min(max(gx == 0 ? lx + 1 : lx - 1, 0), kTbW - 1);
-        const int lxE = min(max(gx == nx - 1 ? lx - 1 : lx + 1, 0), kTbW - 1);
-        const float uc = src[ly * kTbW + lx];
-        const float uW = src[ly * kTbW + lxW], uE = src[ly * kTbW + lxE];
-        const float uN = src[lyN * kTbW + lx], uS = src[lyS * kTbW + lx];
+        const float uc = u[r][k];
+        float uW = k > 0 ? u[r][k - 1] : left;
+        float uE = k < 3 ? u[r][k + 1] : right;
+        float uS = prev[k];
+        float uN = r < kR - 1 ? u[r + 1][k] : rowN[k];
+        const float tW = uW, tS = uS;
+        if ((xw >> k) & 1u) uW = uE;
+        if ((xe >> k) & 1u) uE = tW;
+        if ((ys >> r) & 1u) uS = uN;
+        if ((yn >> r) & 1u) uN = tS;
         float du;
         bool sc = true;
         if (HOLES) {
-          const uint32_t c = ms[ly * kTbW + lx];
+          const uint32_t c = code[r] >> (8 * k);
           sc = (c & 1u) != 0u;
           float cxw, cxc, cxe, cyn, cyc, cys;
           pattern_weights((c >> 1) & 3u, cxw, cxc, cxe);
@@ -135,42 +212,47 @@ __global__ void __launch_bounds__(kTbThreads, 1)
         float ru, rv, rw;
         if (W3) {
           float J, gv, gw;
-          fk3v_rates(a, uc, v[r][k], w[r][k], J, gv, gw);
+          fk3v_rates(a, uc, v[k], w[k], J, gv, gw);
           ru = du - a.dt * J;
           rv = a.dt * gv;
           rw = a.dt * gw;
         } else {
           float I_sum, I_v;
-          ref2v_currents(a, uc, v[r][k], I_sum, I_v);
+          ref2v_currents(a, uc, v[k], I_sum, I_v);
           ru = du - a.dt * I_sum;
           rv = 0.f - a.dt * I_v;
           rw = 0.f;
         }
-        const bool live = inside && sc;
-        const float un = live ? uc + a.tc * ru : 0.f;
-        v[r][k] = live ? v[r][k] + a.tc * rv : 0.f;
-        if (W3) w[r][k] = live ? w[r][k] + a.tc * rw : 0.f;
-        dst[ly * kTbW + lx] = un;
+        const bool live = sc && ((inx >> k) & 1u) && ((iny >> r) & 1u);
+        un[k] = live ? uc + a.tc * ru : 0.f;
+        v[k] = live ? v[k] + a.tc * rv : 0.f;
+        if (W3) w[k] = live ? w[k] + a.tc * rw : 0.f;
+      }
+      *vp = f4(v);
+      if (W3) *wp = f4(w);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        prev[k] = u[r][k];
+        u[r][k] = un[k];
       }
     }
-    __syncthreads();
   }
 
-  // store the interior; the last sub-step wrote us1 when K is odd
-  const float *ufin = (K & 1) ? us1 : us0;
+  // store the interior
 #pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int ly = wy * 4 + r, gy = y0 + ly;
+  for (int r = 0; r < kR; ++r) {
+    const int ly = ly0 + r;
+    if (ly < K || ly >= kTbH - K || !((iny >> r) & 1u)) continue;
+    const size_t base = (size_t)(gy0 + r) * nx + gx0;
+    const float *vr = vs + ly * kTbW + lx0;
+    const float *wr = ws + ly * kTbW + lx0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const int lx = lane + 32 * k, gx = x0 + lx;
-      const bool keep = lx >= K && lx < kTbW - K && ly >= K && ly < kTbH - K &&
-                        (unsigned)gx < (unsigned)nx && (unsigned)gy < (unsigned)ny;
-      if (keep) {
-        const size_t idx = (size_t)gy * nx + gx;
-        out.f[0][idx] = ufin[ly * kTbW + lx];
-        out.f[1][idx] = v[r][k];
-        if (W3) out.f[2][idx] = w[r][k];
+      const int lx = lx0 + k;
+      if (lx >= K && lx < kTbW - K && ((inx >> k) & 1u)) {
+        out.f[0][base + k] = u[r][k];
+        out.f[1][base + k] = vr[k];
+        if (W3) out.f[2][base + k] = wr[k];
       }
     }
   }

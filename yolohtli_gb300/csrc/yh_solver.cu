@@ -417,7 +417,7 @@ extern "C" int yh_track_tips(yh_solver *h) {
   cudaError_t e = cudaMemsetAsync(h->tip_count, 0, sizeof(int), h->s);
   if (e != cudaSuccess) return st(e);
   // plain mode: x = new u (present), y = old u (past) (main.cu:963)
-  e = launch_tips<float>(h->p, h->nxt.f[0], h->cur.f[0], h->solid,
+  e = launch_tips<float>(h->p, h->nxt.f[0], h->cur.f[0], h->p.solidSwitch,
                          h->p.dt * (double)h->step, h->tip_count, h->tips,
                          kTipCapacity, nullptr, nullptr, h->s);
   if (e == cudaSuccess) h->launches += 1;
@@ -531,7 +531,7 @@ static cudaError_t enqueue_sr_step(yh_solver *h, bool first) {
   if (e == cudaSuccess)  // 1. RD with tangent: cur -> nxt
     e = launch_rd_step<float>(a, h->cur, h->nxt, h->tan, h->solid, h->s);
   if (e == cudaSuccess)  // 2. tips x = pre-RD u, y = post-RD u; centre
-    e = launch_tips<float>(h->p, h->nxt.f[0], h->cur.f[0], h->solid, 0.0,
+    e = launch_tips<float>(h->p, h->nxt.f[0], h->cur.f[0], h->p.solidSwitch, 0.0,
                            h->tip_count, h->tips, kTipCapacity, h->sym,
                            h->tip_done, h->s);
   const int reps = first ? 2 : 1;  // main.cu:910-926

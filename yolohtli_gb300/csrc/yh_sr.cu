@@ -204,8 +204,8 @@ __global__ void pick_centre_kernel(const int *count, const yh_tip *vec,
 // otherwise they are stamped `ptime`. `done` is a zeroed counter.
 template <typename Real>
 cudaError_t launch_tips(const yh_param_var &p, const Real *past,
-                        const Real *present, const uint8_t *solid,
-                        double ptime, int *count, yh_tip *vec, int cap,
+                        const Real *present, bool holes, double ptime,
+                        int *count, yh_tip *vec, int cap,
                         yh_sym_state *sym_pick, unsigned int *done,
                         cudaStream_t s) {
   TipArgs a;
@@ -217,7 +217,6 @@ cudaError_t launch_tips(const yh_param_var &p, const Real *past,
   a.ptime = ptime;
   const dim3 block(32, 8);
   const dim3 grid((p.nx + 31) / 32, (p.ny + 7) / 8);
-  const bool holes = p.solidSwitch && solid;
   if (holes)
     tip_kernel<Real, true><<<grid, block, 0, s>>>(a, past, present, count,
                                                   vec, cap, sym_pick, done);
@@ -260,51 +259,6 @@ template <typename Real>
 __device__ __forceinline__ Real c4(Real p1, Real p2, Real m1, Real m2,
                                    Real inv) {
   return (p2 - Real(8) * p1 + Real(8) * m1 - m2) * inv * Real(1.0 / 6.0);
-}
-
-// FP64 3x3 solve of the drift/rotation system with partial pivoting.
-// Row r: [I[3r] cos(pt) + I[3r+1] sin(pt), I[3r+1] cos(pt) - I[3r] sin(pt),
-// I[3r+2]] . c = I[9+r]  (symmetryReduction.cu:390-396). Returns YH_OK, or
-// YH_ESINGULAR when a pivot is below 1e-13 of the largest entry (the
-// reference divides by unpivoted entries, symmetryReduction.cu:398-412).
-__device__ int solve3(const double I[12], double pt, double c[3]) {
-  double cs, sn;
-  sincos(pt, &sn, &cs);
-  double A[3][4];
-  double amax = 0.0;
-  for (int r = 0; r < 3; ++r) {
-    A[r][0] = I[3 * r] * cs + I[3 * r + 1] * sn;
-    A[r][1] = I[3 * r + 1] * cs - I[3 * r] * sn;
-    A[r][2] = I[3 * r + 2];
-    A[r][3] = I[9 + r];
-    for (int k = 0; k < 3; ++k) amax = fmax(amax, fabs(A[r][k]));
-  }
-  if (!(amax > 0.0) || !isfinite(amax)) return YH_ESINGULAR;
-  const double tol = 1e-13 * amax;
-  for (int col = 0; col < 3; ++col) {
-    int piv = col;
-    for (int r = col + 1; r < 3; ++r)
-      if (fabs(A[r][col]) > fabs(A[piv][col])) piv = r;
-    if (!(fabs(A[piv][col]) > tol)) return YH_ESINGULAR;
-    if (piv != col)
-      for (int k = 0; k < 4; ++k) {
-        const double t = A[col][k];
-        A[col][k] = A[piv][k];
-        A[piv][k] = t;
-      }
-    for (int r = col + 1; r < 3; ++r) {
-      const double m = A[r][col] / A[col][col];
-      for (int k = col; k < 4; ++k) A[r][k] -= m * A[col][k];
-    }
-  }
-  double x[3];
-  for (int r = 2; r >= 0; --r) {
-    double s = A[r][3];
-    for (int k = r + 1; k < 3; ++k) s -= A[r][k] * x[k];
-    x[r] = s / A[r][r];
-  }
-  for (int k = 0; k < 3; ++k) c[k] = x[k];
-  return YH_OK;
 }
 
 // One block covers a 32x8 tile of the disc's bounding box, placed by the
@@ -672,7 +626,10 @@ __device__ __forceinline__ void bfecc_ratios(const BfeccArgs<Real> &a, Real ax,
   Ry = sy * cy * a.dt / a.hy;
 }
 
-template <int PASS, int NF, typename Real, bool HOLES>
+// ADV2D: the comoving field as full nx*ny arrays (adv_rows = adv.x,
+// adv_cols = adv.y, the reference's layout); otherwise as the separable
+// vectors adv_rows[ny], adv_cols[nx].
+template <int PASS, int NF, typename Real, bool HOLES, bool ADV2D>
 __global__ void __launch_bounds__(256)
     bfecc_pass(const BfeccArgs<Real> a, const Fld<Real> in, const Fld<Real> uf,
                const Fld<Real> ue, const Fld<Real> out,
@@ -687,8 +644,9 @@ __global__ void __launch_bounds__(256)
   bool sc;
   const BIdx n = bfecc_idx<HOLES>(i, j, nx, ny, solid, sc);
   Real cx, cy, Rx, Ry;
-  bfecc_ratios(a, sc ? adv_rows[j] : Real(0), sc ? adv_cols[i] : Real(0), cx,
-               cy, Rx, Ry);
+  const Real ax = ADV2D ? adv_rows[C] : adv_rows[j];
+  const Real ay = ADV2D ? adv_cols[C] : adv_cols[i];
+  bfecc_ratios(a, sc ? ax : Real(0), sc ? ay : Real(0), cx, cy, Rx, Ry);
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
     if (PASS == 1) {
@@ -713,7 +671,7 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-template <int NF, typename Real, bool HOLES>
+template <int NF, typename Real, bool HOLES, bool ADV2D>
 static cudaError_t bfecc_nf(const BfeccArgs<Real> &a, const Fld<Real> &in,
                             const Fld<Real> &out, const Real *ar,
                             const Real *ac, const uint8_t *solid,
@@ -721,21 +679,21 @@ static cudaError_t bfecc_nf(const BfeccArgs<Real> &a, const Fld<Real> &in,
                             cudaStream_t s) {
   const dim3 block(32, 8);
   const dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8);
-  bfecc_pass<1, NF, Real, HOLES>
+  bfecc_pass<1, NF, Real, HOLES, ADV2D>
       <<<grid, block, 0, s>>>(a, in, uf, ue, out, ar, ac, solid);
-  bfecc_pass<2, NF, Real, HOLES>
+  bfecc_pass<2, NF, Real, HOLES, ADV2D>
       <<<grid, block, 0, s>>>(a, in, uf, ue, out, ar, ac, solid);
-  bfecc_pass<3, NF, Real, HOLES>
+  bfecc_pass<3, NF, Real, HOLES, ADV2D>
       <<<grid, block, 0, s>>>(a, in, uf, ue, out, ar, ac, solid);
   return cudaGetLastError();
 }
 
-template <typename Real>
-cudaError_t launch_bfecc(const yh_param_var &p, int nf, const Fld<Real> &in,
-                         const Fld<Real> &out, const Real *adv_rows,
-                         const Real *adv_cols, const uint8_t *solid,
-                         const Fld<Real> &uf, const Fld<Real> &ue,
-                         cudaStream_t s) {
+template <typename Real, bool ADV2D>
+static cudaError_t bfecc_dispatch(const yh_param_var &p, int nf,
+                                  const Fld<Real> &in, const Fld<Real> &out,
+                                  const Real *ar, const Real *ac,
+                                  const uint8_t *solid, const Fld<Real> &uf,
+                                  const Fld<Real> &ue, cudaStream_t s) {
   BfeccArgs<Real> a;
   a.nx = p.nx;
   a.ny = p.ny;
@@ -745,21 +703,40 @@ cudaError_t launch_bfecc(const yh_param_var &p, int nf, const Fld<Real> &in,
   a.tc = (Real)p.tc;
   const bool holes = p.solidSwitch && solid;
   if (nf == 2)
-    return holes ? bfecc_nf<2, Real, true>(a, in, out, adv_rows, adv_cols,
-                                           solid, uf, ue, s)
-                 : bfecc_nf<2, Real, false>(a, in, out, adv_rows, adv_cols,
-                                            solid, uf, ue, s);
-  return holes ? bfecc_nf<3, Real, true>(a, in, out, adv_rows, adv_cols, solid,
-                                         uf, ue, s)
-               : bfecc_nf<3, Real, false>(a, in, out, adv_rows, adv_cols,
-                                          solid, uf, ue, s);
+    return holes ? bfecc_nf<2, Real, true, ADV2D>(a, in, out, ar, ac, solid,
+                                                  uf, ue, s)
+                 : bfecc_nf<2, Real, false, ADV2D>(a, in, out, ar, ac, solid,
+                                                   uf, ue, s);
+  return holes ? bfecc_nf<3, Real, true, ADV2D>(a, in, out, ar, ac, solid, uf,
+                                                ue, s)
+               : bfecc_nf<3, Real, false, ADV2D>(a, in, out, ar, ac, solid,
+                                                 uf, ue, s);
+}
+
+template <typename Real>
+cudaError_t launch_bfecc(const yh_param_var &p, int nf, const Fld<Real> &in,
+                         const Fld<Real> &out, const Real *adv_rows,
+                         const Real *adv_cols, const uint8_t *solid,
+                         const Fld<Real> &uf, const Fld<Real> &ue,
+                         cudaStream_t s) {
+  return bfecc_dispatch<Real, false>(p, nf, in, out, adv_rows, adv_cols,
+                                     solid, uf, ue, s);
+}
+
+template <typename Real>
+cudaError_t launch_bfecc_2d(const yh_param_var &p, int nf,
+                            const Fld<Real> &in, const Fld<Real> &out,
+                            const Real *adv_x, const Real *adv_y,
+                            const uint8_t *solid, const Fld<Real> &uf,
+                            const Fld<Real> &ue, cudaStream_t s) {
+  return bfecc_dispatch<Real, true>(p, nf, in, out, adv_x, adv_y, solid, uf,
+                                    ue, s);
 }
 
 #define YH_INST(Real)                                                         \
   template cudaError_t launch_tips<Real>(                                     \
-      const yh_param_var &, const Real *, const Real *, const uint8_t *,      \
-      double, int *, yh_tip *, int, yh_sym_state *, unsigned int *,           \
-      cudaStream_t);                                                          \
+      const yh_param_var &, const Real *, const Real *, bool, double, int *,  \
+      yh_tip *, int, yh_sym_state *, unsigned int *, cudaStream_t);           \
   template cudaError_t launch_phase<Real>(                                    \
       const yh_param_var &, int, const Fld<Real> &, const Fld<Real> &,        \
       const Fld<Real> &, const Fld<Real> &, const Fld<Real> &,                \
@@ -769,6 +746,10 @@ cudaError_t launch_bfecc(const yh_param_var &p, int nf, const Fld<Real> &in,
       const yh_param_var &, int, const Fld<Real> &, const Fld<Real> &,        \
       const Fld<Real> &, const Fld<Real> &, cudaStream_t);                    \
   template cudaError_t launch_bfecc<Real>(                                    \
+      const yh_param_var &, int, const Fld<Real> &, const Fld<Real> &,        \
+      const Real *, const Real *, const uint8_t *, const Fld<Real> &,         \
+      const Fld<Real> &, cudaStream_t);                                       \
+  template cudaError_t launch_bfecc_2d<Real>(                                 \
       const yh_param_var &, int, const Fld<Real> &, const Fld<Real> &,        \
       const Real *, const Real *, const uint8_t *, const Fld<Real> &,         \
       const Fld<Real> &, cudaStream_t);
