@@ -49,6 +49,16 @@ StepCoeffs<Real> make_step_coeffs(const yh_param_var &p, int model,
     a.inv_tv2m = (Real)(1.0 / fk->tau_v2_minus);
     a.inv_twp = (Real)(1.0 / fk->tau_w_plus);
     a.inv_twm = (Real)(1.0 / fk->tau_w_minus);
+    const double s = p.tc * p.dt;
+    a.s_td = (Real)(s / fk->tau_d);
+    a.s_tr = (Real)(s / fk->tau_r);
+    a.s_to = (Real)(s / fk->tau_0);
+    a.s_tsi = (Real)(s / fk->tau_si);
+    a.s_tvp = (Real)(s / fk->tau_v_plus);
+    a.s_tv1m = (Real)(s / fk->tau_v1_minus);
+    a.s_tv2m = (Real)(s / fk->tau_v2_minus);
+    a.s_twp = (Real)(s / fk->tau_w_plus);
+    a.s_twm = (Real)(s / fk->tau_w_minus);
   }
   return a;
 }

@@ -53,6 +53,8 @@ struct StepCoeffs {
   Real k_exp2;      // -2*k*log2(e): 1 + tanh(k x) = 2/(1 + 2^(k_exp2 x))
   Real inv_td, inv_tr, inv_to, inv_tsi, inv_tvp, inv_tv1m, inv_tv2m;
   Real inv_twp, inv_twm;
+  // the same rates pre-multiplied by tc*dt (FP32 update, fk3v_update)
+  Real s_td, s_tr, s_to, s_tsi, s_tvp, s_tv1m, s_tv2m, s_twp, s_twm;
 };
 
 // Hole coefficients along one axis (reactionDiffusion.cu:162-169):
@@ -115,6 +117,27 @@ __device__ __forceinline__ void fk3v_rates(const StepCoeffs<Real> &a, Real u,
   const Real itvm = q ? a.inv_tv1m : a.inv_tv2m;
   gv = p ? -v * a.inv_tvp : (Real(1) - v) * itvm;
   gw = p ? -w * a.inv_twp : (Real(1) - w) * a.inv_twm;
+}
+
+// One FK3V Euler update in FP32 with the rates pre-scaled by tc*dt:
+//   u' = u + tc*du - tc*dt*J,  v' = v + tc*dt*dv/dt,  w' = w + tc*dt*dw/dt
+// (the same step as fk3v_rates + the reference's update
+// u0 += tc*rhs, reactionDiffusion.cu:498-513, with fewer operations).
+// du is the scaled Laplacian rx*(..) + ry*(..). Returns the tangent rhs/dt
+// pieces through ru, rv, rw when the caller needs them.
+__device__ __forceinline__ void fk3v_update(const StepCoeffs<float> &a,
+                                            float u, float v, float w,
+                                            float du, float &un, float &vn,
+                                            float &wn) {
+  const bool p = u >= a.u_c;
+  const bool q = u >= a.u_v;
+  const float sig = fk_sigmoid(a, u);
+  const float jfi = -v * ((1.f - u) * (u - a.u_c)) * a.s_td;
+  const float Jd = (p ? jfi + a.s_tr : u * a.s_to) - w * sig * a.s_tsi;
+  un = fmaf(a.tc, du, u) - Jd;
+  const float sv = q ? a.s_tv1m : a.s_tv2m;
+  vn = p ? v - v * a.s_tvp : fmaf(1.f - v, sv, v);
+  wn = p ? w - w * a.s_twp : fmaf(1.f - w, a.s_twm, w);
 }
 
 // Parameters of the symmetry-reduction kernels.

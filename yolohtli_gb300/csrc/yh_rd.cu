@@ -42,6 +42,30 @@ __device__ __forceinline__ float tangent(const StepCoeffs<float> &a, float r) {
   return r * a.inv_dt;
 }
 
+// New values nv of one cell from its scaled Laplacians du, dv, and the
+// tangent rhs/dt when TAN. The FP32 FK3V update without tangent takes the
+// pre-scaled form (fk3v_update); every other case follows the reference's
+// rhs / u0 += tc*rhs form (reactionDiffusion.cu:498-513).
+template <int MODEL, bool TAN, typename Real>
+__device__ __forceinline__ void cell_update(const StepCoeffs<Real> &a, Real u,
+                                            Real v, Real w, Real du, Real dv,
+                                            Real nv[kMaxFields],
+                                            Real tv[kMaxFields]) {
+  if constexpr (MODEL == YH_MODEL_FK3V && std::is_same<Real, float>::value &&
+                !TAN) {
+    fk3v_update(a, u, v, w, du, nv[0], nv[1], nv[2]);
+  } else {
+    Real r[kMaxFields];
+    reaction<MODEL>(a, u, v, w, du, dv, r);
+    const Real x0[3] = {u, v, w};
+#pragma unroll
+    for (int f = 0; f < kMaxFields; ++f) {
+      nv[f] = x0[f] + a.tc * r[f];
+      if (TAN) tv[f] = tangent(a, r[f]);
+    }
+  }
+}
+
 template <int MODEL, typename Real, bool HOLES, bool TAN>
 __global__ void __launch_bounds__(256)
     rd_step_scalar(const StepCoeffs<Real> a, const Fld<Real> in,
@@ -82,13 +106,12 @@ __global__ void __launch_bounds__(256)
       dv = (__ldg(V + W) - Real(2) * v + __ldg(V + E)) * a.rx * a.rscale +
            (__ldg(V + N) - Real(2) * v + __ldg(V + S)) * a.ry * a.rscale;
   }
-  Real r[kMaxFields];
-  reaction<MODEL>(a, u, v, w, du, dv, r);
-  const Real x0[3] = {u, v, w};
+  Real nv[kMaxFields], tv[kMaxFields];
+  cell_update<MODEL, TAN>(a, u, v, w, du, dv, nv, tv);
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
-    out.f[f][C] = sc ? x0[f] + a.tc * r[f] : Real(0);
-    if (TAN) tan.f[f][C] = sc ? tangent(a, r[f]) : Real(0);
+    out.f[f][C] = sc ? nv[f] : Real(0);
+    if (TAN) tan.f[f][C] = sc ? tv[f] : Real(0);
   }
 }
 
@@ -190,12 +213,12 @@ __global__ void __launch_bounds__(256)
              (vnv[k] - 2.f * vcv[k] + vsv[k]) * a.ry * a.rscale;
       }
     }
-    float r[kMaxFields];
-    reaction<MODEL>(a, x[0], x[1], x[2], du, dv, r);
+    float nv[kMaxFields], tv[kMaxFields];
+    cell_update<MODEL, TAN>(a, x[0], x[1], x[2], du, dv, nv, tv);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
-      res[f][k] = sc ? x[f] + a.tc * r[f] : 0.f;
-      if (TAN) tres[f][k] = sc ? tangent(a, r[f]) : 0.f;
+      res[f][k] = sc ? nv[f] : 0.f;
+      if (TAN) tres[f][k] = sc ? tv[f] : 0.f;
     }
   }
 #pragma unroll

@@ -49,11 +49,29 @@ __device__ __forceinline__ float4 f4(const float x[4]) {
   return make_float4(x[0], x[1], x[2], x[3]);
 }
 
+// New u, v, w of one cell from its scaled Laplacian du: the FP32 FK3V
+// update of the single-step kernels (fk3v_update), or the reference form
+// for REF2V without gate diffusion (reactionDiffusion.cu:131-141,498-513).
+template <int MODEL>
+__device__ __forceinline__ void tb_update(const StepCoeffs<float> &a, float u,
+                                          float v, float w, float du,
+                                          float &un, float &vn, float &wn) {
+  if (MODEL == YH_MODEL_FK3V) {
+    fk3v_update(a, u, v, w, du, un, vn, wn);
+  } else {
+    float I_sum, I_v;
+    ref2v_currents(a, u, v, I_sum, I_v);
+    un = u + a.tc * (du - a.dt * I_sum);
+    vn = v + a.tc * (0.f - a.dt * I_v);
+    wn = 0.f;
+  }
+}
+
 template <int MODEL, bool HOLES>
 __global__ void __launch_bounds__(kTbThreads, 1)
     rd_tb_kernel(const StepCoeffs<float> a, const Fld<float> in,
                  const Fld<float> out, const uint8_t *__restrict__ solid,
-                 const int K) {
+                 const int K, const bool vec_ok) {
   extern __shared__ float4 smem4[];
   float *edge = reinterpret_cast<float *>(smem4);  // [2][2][16][128]
   float *vs = edge + kTbEdge;                      // [64][128]
@@ -86,7 +104,10 @@ __global__ void __launch_bounds__(kTbThreads, 1)
 
   float u[kR][4], v[4], w[4];
   uint32_t m[kR];  // tissue bits of the 4 cells of a row
-  const bool vec = ((x0 & 3) == 0) && inx == 0xFu;
+  // float4 loads need a 16-byte aligned address: every row start is one
+  // only when nx % 4 == 0 and the fields are 16-byte aligned (vec_ok, from
+  // the host), and this thread's first column must be a multiple of 4
+  const bool vec = vec_ok && ((x0 & 3) == 0) && inx == 0xFu;
 #pragma unroll
   for (int r = 0; r < kR; ++r) {
     m[r] = 0u;
@@ -158,6 +179,17 @@ __global__ void __launch_bounds__(kTbThreads, 1)
     __syncthreads();
   }
 
+  // rows whose 4 cells are inside the domain, off its edges, tissue with
+  // tissue neighbours: the common case, updated without selects
+  uint32_t plain = 0u;
+#pragma unroll
+  for (int r = 0; r < kR; ++r) {
+    const bool p = xw == 0u && xe == 0u && inx == 0xFu && ((iny >> r) & 1u) &&
+                   !((ys >> r) & 1u) && !((yn >> r) & 1u) &&
+                   (!HOLES || code[r] == 0x01010101u);
+    plain |= (p ? 1u : 0u) << r;
+  }
+
   for (int s = 0; s < K; ++s) {
     float *bot = edge + (s & 1) * 2 * kTbWarps * kTbW;
     float *top = bot + kTbWarps * kTbW;
@@ -184,49 +216,51 @@ __global__ void __launch_bounds__(kTbThreads, 1)
       float v[4] = {v4.x, v4.y, v4.z, v4.w};
       float w[4] = {w4.x, w4.y, w4.z, w4.w};
       float un[4];
+      if ((plain >> r) & 1u) {
+        // interior tissue row away from the domain edge: no selects
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float uc = u[r][k];
-        float uW = k > 0 ? u[r][k - 1] : left;
-        float uE = k < 3 ? u[r][k + 1] : right;
-        float uS = prev[k];
-        float uN = r < kR - 1 ? u[r + 1][k] : rowN[k];
-        const float tW = uW, tS = uS;
-        if ((xw >> k) & 1u) uW = uE;
-        if ((xe >> k) & 1u) uE = tW;
-        if ((ys >> r) & 1u) uS = uN;
-        if ((yn >> r) & 1u) uN = tS;
-        float du;
-        bool sc = true;
-        if (HOLES) {
-          const uint32_t c = code[r] >> (8 * k);
-          sc = (c & 1u) != 0u;
-          float cxw, cxc, cxe, cyn, cyc, cys;
-          pattern_weights((c >> 1) & 3u, cxw, cxc, cxe);
-          pattern_weights((c >> 3) & 3u, cyn, cyc, cys);
-          du = (cxw * uW - cxc * uc + cxe * uE) * a.rx +
-               (cyn * uN - cyc * uc + cys * uS) * a.ry;
-        } else {
-          du = (uW - 2.f * uc + uE) * a.rx + (uN - 2.f * uc + uS) * a.ry;
+        for (int k = 0; k < 4; ++k) {
+          const float uc = u[r][k];
+          const float uW = k > 0 ? u[r][k - 1] : left;
+          const float uE = k < 3 ? u[r][k + 1] : right;
+          const float uN = r < kR - 1 ? u[r + 1][k] : rowN[k];
+          const float du =
+              (uW - 2.f * uc + uE) * a.rx + (uN - 2.f * uc + prev[k]) * a.ry;
+          tb_update<MODEL>(a, uc, v[k], w[k], du, un[k], v[k], w[k]);
         }
-        float ru, rv, rw;
-        if (W3) {
-          float J, gv, gw;
-          fk3v_rates(a, uc, v[k], w[k], J, gv, gw);
-          ru = du - a.dt * J;
-          rv = a.dt * gv;
-          rw = a.dt * gw;
-        } else {
-          float I_sum, I_v;
-          ref2v_currents(a, uc, v[k], I_sum, I_v);
-          ru = du - a.dt * I_sum;
-          rv = 0.f - a.dt * I_v;
-          rw = 0.f;
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float uc = u[r][k];
+          float uW = k > 0 ? u[r][k - 1] : left;
+          float uE = k < 3 ? u[r][k + 1] : right;
+          float uS = prev[k];
+          float uN = r < kR - 1 ? u[r + 1][k] : rowN[k];
+          const float tW = uW, tS = uS;
+          if ((xw >> k) & 1u) uW = uE;
+          if ((xe >> k) & 1u) uE = tW;
+          if ((ys >> r) & 1u) uS = uN;
+          if ((yn >> r) & 1u) uN = tS;
+          float du;
+          bool sc = true;
+          if (HOLES) {
+            const uint32_t c = code[r] >> (8 * k);
+            sc = (c & 1u) != 0u;
+            float cxw, cxc, cxe, cyn, cyc, cys;
+            pattern_weights((c >> 1) & 3u, cxw, cxc, cxe);
+            pattern_weights((c >> 3) & 3u, cyn, cyc, cys);
+            du = (cxw * uW - cxc * uc + cxe * uE) * a.rx +
+                 (cyn * uN - cyc * uc + cys * uS) * a.ry;
+          } else {
+            du = (uW - 2.f * uc + uE) * a.rx + (uN - 2.f * uc + uS) * a.ry;
+          }
+          float nu, nv, nw;
+          tb_update<MODEL>(a, uc, v[k], w[k], du, nu, nv, nw);
+          const bool live = sc && ((inx >> k) & 1u) && ((iny >> r) & 1u);
+          un[k] = live ? nu : 0.f;
+          v[k] = live ? nv : 0.f;
+          w[k] = live ? nw : 0.f;
         }
-        const bool live = sc && ((inx >> k) & 1u) && ((iny >> r) & 1u);
-        un[k] = live ? uc + a.tc * ru : 0.f;
-        v[k] = live ? v[k] + a.tc * rv : 0.f;
-        if (W3) w[k] = live ? w[k] + a.tc * rw : 0.f;
       }
       *vp = f4(v);
       if (W3) *wp = f4(w);
@@ -272,8 +306,9 @@ static cudaError_t launch_tb_t(const StepCoeffs<float> &a,
   }
   const int TX = kTbW - 2 * K, TY = kTbH - 2 * K;
   const dim3 grid((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY);
+  const bool vec_ok = (a.nx % 4) == 0 && aligned16(in, MODEL);
   rd_tb_kernel<MODEL, HOLES>
-      <<<grid, kTbThreads, kTbSmem, s>>>(a, in, out, solid, K);
+      <<<grid, kTbThreads, kTbSmem, s>>>(a, in, out, solid, K, vec_ok);
   return cudaGetLastError();
 }
 
