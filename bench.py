@@ -148,14 +148,14 @@ def cpu_baseline(wl, seconds=10.0):
                           elapsed)}
 
 
-def config_of(wl, args, tb, autotuned=False):
+def config_of(wl, args, tb, autotuned=False, engine="cpu"):
     state_mb = 12.0 * wl.cells / 2 ** 20
     return {"workload": wl.name, "grid": [wl.p.nx, wl.p.ny],
             "steps_per_solve": wl.nsteps, "model": "FK3V",
             "holes": int(round(300 * wl.cells / 2 ** 20)),
             "s2_patches": len(wl.stims),
             "cells": wl.cells, "dt_ms": wl.p.dt, "dx_cm": wl.p.hx,
-            "time_block": tb, "time_block_autotuned": autotuned,
+            "engine": engine, "time_block": tb, "engine_autotuned": autotuned,
             "l2": "256 MB write between solves; %.1f MB state%s within a solve" % (
                 state_mb, " L2-resident" if 2 * state_mb < 100 else ""),
             "parallelism": "replicas x%d" % args.gpus}
@@ -204,8 +204,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--time-block", type=int, default=0,
-                    help="steps per kernel launch (0: autotuned before timing)")
+    ap.add_argument("--engine", default="auto",
+                    choices=["auto", "step", "blocked", "resident"],
+                    help="how the solver advances (auto: the library's "
+                         "autotuner picks engine and depth before timing)")
+    ap.add_argument("--time-block", type=int, default=4,
+                    help="steps per launch of the blocked engine")
     ap.add_argument("--nsteps", type=int, default=20000,
                     help="explicit steps per solve (the workload's 20,000)")
     ap.add_argument("--grid", type=int, default=1024,
@@ -238,14 +242,16 @@ def main():
     stream = torch.cuda.Stream()
     m = Monodomain(wl.p, wl.model, wl.fk, solid=wl.solid, stream=stream.cuda_stream)
     ic = [torch.tensor(x, device="cuda") for x in wl.state0()]
-    autotuned = args.time_block <= 0
+    autotuned = args.engine == "auto"
     if autotuned:
         # the library's autotuner, on the workload's initial state (restored)
         m.set_state(*wl.state0())
-        tb = m.autotune_time_block(512)
+        engine, tb = m.autotune(512)
     else:
-        m.set_time_block(args.time_block)
-        tb = m.time_block()
+        engine = {"step": A.YH_ENGINE_STEP, "blocked": A.YH_ENGINE_BLOCKED,
+                  "resident": A.YH_ENGINE_RESIDENT}[args.engine]
+        m.set_engine(engine, args.time_block)
+        engine, tb = m.engine()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     lib = m.lib
 
@@ -312,14 +318,16 @@ def main():
     bytes_alg = 25.0 * wl.cells * steps_per_launch
     achieved = bytes_alg / avg_launch_s / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = profiled_traffic("%s_tb%d" % (wl.name, tb))
+    traffic = profiled_traffic("%s_%s%d" % (wl.name, A.ENGINE_NAMES[engine], tb))
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "traffic": traffic, "peak_kind": peak_kind,
                 "alg_bytes_per_cell_step": 25,
                 "steps_per_launch": round(steps_per_launch, 3),
                 "mean_launch_us": round(avg_launch_s * 1e6, 3),
-                "kernel": "rd_tb_kernel" if tb > 1 else "rd_step_vec4",
+                "kernel": {A.YH_ENGINE_STEP: "rd_step_vec4",
+                           A.YH_ENGINE_BLOCKED: "rd_tb_kernel",
+                           A.YH_ENGINE_RESIDENT: "rd_resident_kernel"}[engine],
                 "note": "achieved = 25 B x cells x steps_per_launch / mean launch "
                         "time; frac > 1 is possible: the state stays in L2 and "
                         "temporal blocking re-reads it once per steps_per_launch"}
@@ -361,7 +369,8 @@ def main():
             "ms_per_step": round(ms_max / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": config_of(wl, args, tb, autotuned),
+            "config": config_of(wl, args, tb, autotuned,
+                                A.ENGINE_NAMES[engine]),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clk,
         }

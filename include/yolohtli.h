@@ -49,7 +49,9 @@ enum {
   YH_EOVERFLOW = -6,     /* tip buffer full; extra tips were dropped         */
   YH_EUNSUPPORTED = -7,  /* option off this path: RK2/RK4, lap4, anisotropy,
                             Dirichlet boundaries                             */
-  YH_ENOTREADY = -8      /* call order (e.g. yh_sr_step before yh_sr_begin)  */
+  YH_ENOTREADY = -8,     /* call order (e.g. yh_sr_step before yh_sr_begin)  */
+  YH_ETIMEOUT = -9       /* a bounded device-side wait gave up (resident
+                            solver); the state is not valid                  */
 };
 
 enum { YH_MODEL_REF2V = 0,   /* the reference's 2-variable cubic model
@@ -338,10 +340,27 @@ int yh_state_device(yh_solver *h, yh_fields *cur);
 int yh_set_time_block(yh_solver *h, int steps_per_launch);
 int yh_get_time_block(yh_solver *h, int *steps_per_launch);
 
+/* How yh_run advances the plain solver:
+ *  STEP      one launch per step (graph-replayed);
+ *  BLOCKED   steps_per_launch steps per launch (temporal blocking in
+ *            registers and shared memory);
+ *  RESIDENT  the whole run in one cooperative launch: each SM keeps its
+ *            stripe of the state in shared memory for all steps, stimulus
+ *            events are applied in the kernel; only for grids that fit
+ *            (about 1.7M cells on a GB300). A bounded wait between blocks
+ *            that gives up makes yh_synchronize / yh_get_state return
+ *            YH_ETIMEOUT.
+ * BLOCKED and RESIDENT need a model where only u diffuses (FK3V, or REF2V
+ * without gateDiff); YH_EUNSUPPORTED otherwise. */
+enum { YH_ENGINE_STEP = 0, YH_ENGINE_BLOCKED = 1, YH_ENGINE_RESIDENT = 2 };
+int yh_set_engine(yh_solver *h, int engine, int steps_per_launch);
+int yh_get_engine(yh_solver *h, int *engine, int *steps_per_launch);
+
 /* Autotuner: times probe_steps plain steps from the current state for each
- * allowed depth, restores the state and counters, keeps the fastest depth
- * and returns it in *best. */
-int yh_autotune_time_block(yh_solver *h, int probe_steps, int *best);
+ * engine and depth the model allows, restores the state and counters, and
+ * keeps the fastest (returned in *engine, *steps_per_launch). */
+int yh_autotune(yh_solver *h, int probe_steps, int *engine,
+                int *steps_per_launch);
 
 /* nsteps plain explicit steps with the stimulus events of `stims` whose step
  * lies in [h.step, h.step + nsteps), captured and replayed as a CUDA graph. */

@@ -63,15 +63,16 @@ def test_blocked_protocol_with_stimuli_matches_oracle():
     assert np.all(got[0][solid == 0] == 0)
 
 
-def test_autotune_picks_a_depth_and_restores_the_state():
+def test_autotune_picks_an_engine_and_restores_the_state():
     p, st, solid = fk_case(512, 512, True)
     m = Monodomain(p, A.YH_MODEL_FK3V, A.fk_defaults(), solid=solid)
     m.set_state(*st)
     before = m.get_state()
     n0 = m.launch_count()
-    k = m.autotune_time_block(128)
+    e, k = m.autotune(128)
     after = m.get_state()
-    assert 1 <= k <= 8 and m.time_block() == k
+    assert e in A.ENGINE_NAMES and 1 <= k <= 8 and m.engine() == (e, k)
+    print("autotune 512^2 FK3V with holes: engine %s, depth %d" % (A.ENGINE_NAMES[e], k))
     assert m.step_count() == 0 and m.launch_count() == n0
     for f in range(3):
         assert np.array_equal(before[f], after[f])

@@ -15,13 +15,21 @@ YH_ENONFINITE = -5
 YH_EOVERFLOW = -6
 YH_EUNSUPPORTED = -7
 YH_ENOTREADY = -8
+YH_ETIMEOUT = -9
 
 STATUS_NAMES = {
     YH_OK: "YH_OK", YH_EINVAL: "YH_EINVAL", YH_ECUDA: "YH_ECUDA",
     YH_ENOMEM: "YH_ENOMEM", YH_ESINGULAR: "YH_ESINGULAR",
     YH_ENONFINITE: "YH_ENONFINITE", YH_EOVERFLOW: "YH_EOVERFLOW",
     YH_EUNSUPPORTED: "YH_EUNSUPPORTED", YH_ENOTREADY: "YH_ENOTREADY",
+    YH_ETIMEOUT: "YH_ETIMEOUT",
 }
+
+YH_ENGINE_STEP = 0
+YH_ENGINE_BLOCKED = 1
+YH_ENGINE_RESIDENT = 2
+ENGINE_NAMES = {YH_ENGINE_STEP: "step", YH_ENGINE_BLOCKED: "blocked",
+                YH_ENGINE_RESIDENT: "resident"}
 
 YH_MODEL_REF2V = 0
 YH_MODEL_FK3V = 1

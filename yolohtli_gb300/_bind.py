@@ -43,7 +43,9 @@ SIGNATURES = {
     "yh_state_device": (_i, [_v, _P(A.Fields)]),
     "yh_set_time_block": (_i, [_v, _i]),
     "yh_get_time_block": (_i, [_v, _P(_i)]),
-    "yh_autotune_time_block": (_i, [_v, _i, _P(_i)]),
+    "yh_set_engine": (_i, [_v, _i, _i]),
+    "yh_get_engine": (_i, [_v, _P(_i), _P(_i)]),
+    "yh_autotune": (_i, [_v, _i, _P(_i), _P(_i)]),
     "yh_run": (_i, [_v, _i, _P(A.Stim), _i]),
     "yh_track_tips": (_i, [_v]),
     "yh_get_tips": (_i, [_v, _P(A.Tip), _i, _P(_i)]),

@@ -25,6 +25,30 @@ cudaError_t launch_stimulate(Real *u, const uint8_t *solid, int nx, int ny,
                              int i0, int j0, int i1, int j1, Real value,
                              cudaStream_t s);
 
+// yh_rd_tb.cu
+int rd_tb_max_steps();
+cudaError_t launch_rd_tb(const StepCoeffs<float> &a, const Fld<float> &in,
+                         const Fld<float> &out, const uint8_t *solid,
+                         int nsteps, cudaStream_t s);
+
+// yh_rd_resident.cu
+constexpr int kResMaxStims = 32;  // stimulus events per resident launch
+struct ResidentPlan {
+  bool ok;
+  int nb, rq, rrem, rmax;  // blocks, rows per block (rq or rq+1), max rows
+  size_t smem;             // dynamic shared memory per block
+};
+ResidentPlan resident_plan(const StepCoeffs<float> &a, int device);
+// io: the state, updated in place; prev_u (may be null): receives u of the
+// level before the last step.
+cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
+                               float *prev_u, const uint8_t *solid,
+                               int nsteps, int step0,
+                               const yh_stim *stims, int nstims,
+                               const ResidentPlan &pl, float *halo,
+                               unsigned int *flags, int *error,
+                               cudaStream_t s);
+
 // yh_sr.cu
 // holes: the hole-domain branch of the reference (a disc around the grid
 // centre, tipTracker.cu:47-122); it does not read the mask itself.

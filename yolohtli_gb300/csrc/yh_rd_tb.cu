@@ -32,39 +32,8 @@ constexpr int kTbSmem = (kTbEdge + 2 * kTbW * kTbH) * 4;
 
 int rd_tb_max_steps() { return kTbMaxK; }
 
-// Hole pattern of one axis as 2 bits: 0 (1,2,1), 1 (2,2,0), 2 (0,2,2),
-// 3 (0,0,0) — the coefficient triples of reactionDiffusion.cu:162-169.
-__device__ __forceinline__ uint32_t hole_pattern(bool lo, bool c, bool hi) {
-  if (!c) return 3u;
-  return lo ? (hi ? 0u : 1u) : (hi ? 2u : 3u);
-}
-__device__ __forceinline__ void pattern_weights(uint32_t pat, float &wlo,
-                                                float &wc, float &whi) {
-  wlo = pat == 0u ? 1.f : (pat == 1u ? 2.f : 0.f);
-  whi = pat == 0u ? 1.f : (pat == 2u ? 2.f : 0.f);
-  wc = pat == 3u ? 0.f : 2.f;
-}
-
 __device__ __forceinline__ float4 f4(const float x[4]) {
   return make_float4(x[0], x[1], x[2], x[3]);
-}
-
-// New u, v, w of one cell from its scaled Laplacian du: the FP32 FK3V
-// update of the single-step kernels (fk3v_update), or the reference form
-// for REF2V without gate diffusion (reactionDiffusion.cu:131-141,498-513).
-template <int MODEL>
-__device__ __forceinline__ void tb_update(const StepCoeffs<float> &a, float u,
-                                          float v, float w, float du,
-                                          float &un, float &vn, float &wn) {
-  if (MODEL == YH_MODEL_FK3V) {
-    fk3v_update(a, u, v, w, du, un, vn, wn);
-  } else {
-    float I_sum, I_v;
-    ref2v_currents(a, u, v, I_sum, I_v);
-    un = u + a.tc * (du - a.dt * I_sum);
-    vn = v + a.tc * (0.f - a.dt * I_v);
-    wn = 0.f;
-  }
 }
 
 template <int MODEL, bool HOLES>

@@ -13,10 +13,6 @@
 
 namespace yh {
 int check_params(const yh_param_var *p, int model, const yh_fk_params *fk);
-cudaError_t launch_rd_tb(const StepCoeffs<float> &a, const Fld<float> &in,
-                         const Fld<float> &out, const uint8_t *solid,
-                         int nsteps, cudaStream_t s);
-int rd_tb_max_steps();
 }  // namespace yh
 
 using namespace yh;
@@ -67,6 +63,11 @@ struct yh_solver {
   bool frozen = false;
   long long launches = 0;  // kernels enqueued by this handle
   bool own_stream = false;
+  int engine = YH_ENGINE_STEP;
+  ResidentPlan plan{};       // resident solver layout (plan.ok: usable)
+  float *res_halo = nullptr;
+  unsigned int *res_flags = nullptr;
+  int *res_error = nullptr;  // device flag set when a bounded wait gave up
   GraphCache plain[2];
   GraphCache sr[2];
 };
@@ -127,6 +128,18 @@ extern "C" int yh_create(const yh_param_var *p, int model,
     e = cudaMalloc(&h->tips, (size_t)kTipCapacity * sizeof(yh_tip));
   if (e == cudaSuccess) h->tip_done = (unsigned int *)(h->tip_count + 32);
   if (e == cudaSuccess) e = cudaMalloc(&h->sym, sizeof(yh_sym_state));
+  if (e == cudaSuccess) {
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+      h->plan = resident_plan(make_step_coeffs<float>(h->p, h->model, &h->fk), dev);
+  }
+  if (e == cudaSuccess && h->plan.ok) {
+    e = cudaMalloc(&h->res_halo, (size_t)2 * h->plan.nb * 2 * p->nx * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&h->res_flags, (size_t)h->plan.nb * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&h->res_error, 256);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->res_error, 0, 256, h->s);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
   if (e != cudaSuccess) {
     yh_destroy(h);
@@ -150,14 +163,29 @@ extern "C" int yh_destroy(yh_solver *h) {
   cudaFree(h->ws);
   cudaFree(h->adv_d);
   cudaFree(h->adv_f);
+  cudaFree(h->res_halo);
+  cudaFree(h->res_flags);
+  cudaFree(h->res_error);
   if (h->own_stream) cudaStreamDestroy(h->s);
   delete h;
   return YH_OK;
 }
 
+// YH_ETIMEOUT if a resident launch gave up waiting (after a sync).
+static int resident_status(yh_solver *h) {
+  if (!h->res_error) return YH_OK;
+  int err = 0;
+  cudaError_t e = cudaMemcpyAsync(&err, h->res_error, sizeof(int),
+                                  cudaMemcpyDeviceToHost, h->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  if (e != cudaSuccess) return st(e);
+  return err ? YH_ETIMEOUT : YH_OK;
+}
+
 extern "C" int yh_synchronize(yh_solver *h) {
   if (!h) return YH_EINVAL;
-  return st(cudaStreamSynchronize(h->s));
+  const int rc = st(cudaStreamSynchronize(h->s));
+  return rc ? rc : resident_status(h);
 }
 
 extern "C" int yh_set_state(yh_solver *h, const float *u, const float *v,
@@ -182,7 +210,8 @@ extern "C" int yh_get_state(yh_solver *h, float *u, float *v, float *w) {
                                     cudaMemcpyDefault, h->s);
     if (e != cudaSuccess) return st(e);
   }
-  return st(cudaStreamSynchronize(h->s));
+  const int rc = st(cudaStreamSynchronize(h->s));
+  return rc ? rc : resident_status(h);
 }
 
 extern "C" int yh_state_device(yh_solver *h, yh_fields *cur) {
@@ -211,12 +240,67 @@ extern "C" int yh_set_time_block(yh_solver *h, int k) {
   if (k < 1) k = 1;
   const int kmax = max_time_block(h);
   h->time_block = k > kmax ? kmax : k;
+  h->engine = h->time_block > 1 ? YH_ENGINE_BLOCKED : YH_ENGINE_STEP;
   return YH_OK;
 }
 
 extern "C" int yh_get_time_block(yh_solver *h, int *k) {
   if (!h || !k) return YH_EINVAL;
   *k = h->time_block;
+  return YH_OK;
+}
+
+extern "C" int yh_set_engine(yh_solver *h, int engine, int steps_per_launch) {
+  if (!h) return YH_EINVAL;
+  switch (engine) {
+    case YH_ENGINE_STEP:
+      h->engine = engine;
+      h->time_block = 1;
+      return YH_OK;
+    case YH_ENGINE_BLOCKED: {
+      if (max_time_block(h) < 2) return YH_EUNSUPPORTED;
+      yh_set_time_block(h, steps_per_launch < 2 ? 2 : steps_per_launch);
+      return YH_OK;
+    }
+    case YH_ENGINE_RESIDENT:
+      if (!h->plan.ok) return YH_EUNSUPPORTED;
+      h->engine = engine;
+      h->time_block = 1;
+      return YH_OK;
+  }
+  return YH_EINVAL;
+}
+
+extern "C" int yh_get_engine(yh_solver *h, int *engine, int *steps_per_launch) {
+  if (!h) return YH_EINVAL;
+  if (engine) *engine = h->engine;
+  if (steps_per_launch) *steps_per_launch = h->time_block;
+  return YH_OK;
+}
+
+// nsteps resident steps from h->cur in place, events in [step, step+nsteps)
+// applied inside the kernel (at most kResMaxStims per launch).
+static int run_resident(yh_solver *h, int nsteps, const yh_stim *ev,
+                        int nev) {
+  const StepCoeffs<float> a = make_step_coeffs<float>(h->p, h->model, &h->fk);
+  int done = 0, k = 0;
+  while (done < nsteps) {
+    int len = nsteps - done, m = nev - k;
+    if (m > kResMaxStims) {  // stop before the first event that does not fit
+      m = kResMaxStims;
+      len = ev[k + m].step - (h->step);
+    }
+    // the state stays in h->cur; the previous u level goes to h->nxt (tips)
+    cudaError_t e = launch_rd_resident(a, h->cur, h->nxt.f[0], h->solid, len,
+                                       h->step, ev + k, m, h->plan,
+                                       h->res_halo, h->res_flags,
+                                       h->res_error, h->s);
+    if (e != cudaSuccess) return st(e);
+    h->launches += 1;
+    h->step += len;
+    done += len;
+    k += m;
+  }
   return YH_OK;
 }
 
@@ -332,12 +416,12 @@ static int run_plain(yh_solver *h, int len) {
   return YH_OK;
 }
 
-// Times `probe_steps` plain steps from the current state for every time
-// block depth the model allows (one warm-up run each, CUDA events on the
-// handle's stream), restores the state, step and launch counters, and keeps
-// the fastest depth. Returns it in *best.
-extern "C" int yh_autotune_time_block(yh_solver *h, int probe_steps,
-                                      int *best) {
+// Times `probe_steps` plain steps from the current state for every engine
+// and time block depth the model allows (a warm-up run each, CUDA events on
+// the handle's stream), restores the state, step and launch counters, and
+// keeps the fastest. Returns it in *engine, *steps_per_launch.
+extern "C" int yh_autotune(yh_solver *h, int probe_steps, int *engine,
+                           int *steps_per_launch) {
   if (!h || probe_steps < 1) return YH_EINVAL;
   const size_t bytes = h->n * sizeof(float);
   float *save = nullptr;
@@ -351,25 +435,35 @@ extern "C" int yh_autotune_time_block(yh_solver *h, int probe_steps,
   const int step0 = h->step;
   const long long launches0 = h->launches;
   const int kmax = max_time_block(h);
-  int best_k = 1;
+  // candidates: (engine, depth)
+  std::vector<std::pair<int, int>> cand;
+  cand.push_back({YH_ENGINE_STEP, 1});
+  for (int k = 2; k <= kmax; ++k) cand.push_back({YH_ENGINE_BLOCKED, k});
+  if (h->plan.ok) cand.push_back({YH_ENGINE_RESIDENT, 1});
+  std::pair<int, int> best_c = cand[0];
   float best_ms = 1e30f;
   int rc = st(e);
-  for (int k = 1; k <= kmax && rc == YH_OK; ++k) {
-    h->time_block = k;
+  for (size_t c = 0; c < cand.size() && rc == YH_OK; ++c) {
+    h->engine = cand[c].first;
+    h->time_block = cand[c].second;
     float ms = 0.f;
     for (int rep = 0; rep < 2 && rc == YH_OK; ++rep) {
       for (int f = 0; f < h->nf && rc == YH_OK; ++f)
         rc = st(cudaMemcpyAsync(h->cur.f[f], save + f * h->n, bytes,
                                 cudaMemcpyDeviceToDevice, h->s));
       if (rc == YH_OK) rc = st(cudaEventRecord(e0, h->s));
-      if (rc == YH_OK) rc = run_plain(h, probe_steps);
+      if (rc == YH_OK)
+        rc = h->engine == YH_ENGINE_RESIDENT
+                 ? run_resident(h, probe_steps, nullptr, 0)
+                 : run_plain(h, probe_steps);
       if (rc == YH_OK) rc = st(cudaEventRecord(e1, h->s));
       if (rc == YH_OK) rc = st(cudaEventSynchronize(e1));
       if (rc == YH_OK) rc = st(cudaEventElapsedTime(&ms, e0, e1));
+      if (rc == YH_OK) rc = resident_status(h);
     }
     if (rc == YH_OK && ms < best_ms) {
       best_ms = ms;
-      best_k = k;
+      best_c = cand[c];
     }
   }
   for (int f = 0; f < h->nf && rc == YH_OK; ++f)
@@ -378,8 +472,10 @@ extern "C" int yh_autotune_time_block(yh_solver *h, int probe_steps,
   if (rc == YH_OK) rc = st(cudaStreamSynchronize(h->s));
   h->step = step0;
   h->launches = launches0;
-  h->time_block = best_k;
-  if (best) *best = best_k;
+  h->engine = best_c.first;
+  h->time_block = best_c.second;
+  if (engine) *engine = best_c.first;
+  if (steps_per_launch) *steps_per_launch = best_c.second;
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   cudaFree(save);
@@ -395,6 +491,10 @@ extern "C" int yh_run(yh_solver *h, int nsteps, const yh_stim *stims,
     if (stims[k].step >= h->step && stims[k].step < end) ev.push_back(stims[k]);
   std::stable_sort(ev.begin(), ev.end(),
                    [](const yh_stim &a, const yh_stim &b) { return a.step < b.step; });
+  if (h->engine == YH_ENGINE_RESIDENT && nsteps > 0) {
+    const int rc = run_resident(h, nsteps, ev.data(), (int)ev.size());
+    return rc ? rc : st(cudaGetLastError());
+  }
   size_t k = 0;
   while (h->step < end) {
     while (k < ev.size() && ev[k].step == h->step) {

@@ -81,11 +81,22 @@ class Monodomain:
         check("yh_get_time_block", self.lib.yh_get_time_block(self.h, C.byref(k)))
         return k.value
 
-    def autotune_time_block(self, probe_steps=256):
-        k = C.c_int()
-        check("yh_autotune_time_block", self.lib.yh_autotune_time_block(
-            self.h, int(probe_steps), C.byref(k)))
-        return k.value
+    def set_engine(self, engine, steps_per_launch=1):
+        check("yh_set_engine", self.lib.yh_set_engine(
+            self.h, int(engine), int(steps_per_launch)))
+
+    def engine(self):
+        e, k = C.c_int(), C.c_int()
+        check("yh_get_engine", self.lib.yh_get_engine(self.h, C.byref(e), C.byref(k)))
+        return e.value, k.value
+
+    def autotune(self, probe_steps=256):
+        """Picks the fastest engine/depth on the current state (restored);
+        returns (engine, steps_per_launch)."""
+        e, k = C.c_int(), C.c_int()
+        check("yh_autotune", self.lib.yh_autotune(
+            self.h, int(probe_steps), C.byref(e), C.byref(k)))
+        return e.value, k.value
 
     def run(self, nsteps, stims=()):
         arr = (A.Stim * max(1, len(stims)))(*stims)
