@@ -278,6 +278,29 @@ int yh_phase_integrals(const yh_param_var *p, int model, yh_fields state,
                        const uint8_t *solid, yh_sym_state *sym,
                        void *workspace, void *stream);
 
+/* yh_phase_integrals without the workspace argument, for callers that may
+ * not allocate device memory themselves: a host application whose device
+ * memory is owned by its own pool, or a caller in a section where a
+ * cudaMalloc (which can synchronize the device) is not allowed. No
+ * counterpart in the reference (its trapz_wrapper allocates and frees
+ * scratch on every call, integralTrapz.cu:89-92,181-182).
+ * The scratch is a fixed array of yh_phase_integrals_noalloc_limit() bytes
+ * (384 KiB + 256 B) compiled into the library: every GPU that loads the
+ * library holds it until the process exits. A disc needing more than 4096
+ * blocks of partial sums is rejected with YH_EINVAL. The first call on each
+ * device looks up the array's device address, so make it before capturing
+ * a stream into a CUDA graph. All calls share the one array and it keeps
+ * the last call's partial sums: calls that may overlap on the GPU (on
+ * different streams) race and give wrong results; serialize them. Never
+ * calls cudaMalloc or cudaFree. */
+int yh_phase_integrals_noalloc(const yh_param_var *p, int model,
+                               yh_fields state, yh_fields vel_tan,
+                               yh_fields templ_x, yh_fields templ_y,
+                               yh_fields templ_t, const double *adv_x_rows,
+                               const double *adv_y_cols, const uint8_t *solid,
+                               yh_sym_state *sym, void *stream);
+size_t yh_phase_integrals_noalloc_limit(void);
+
 /* Template derivative fields (negated 4th-order central, as the reference's
  * convCentral2X/Y, symmetryReduction.cu:224-240) of a state over the whole
  * grid; used to freeze a template. */

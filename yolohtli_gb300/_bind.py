@@ -27,6 +27,10 @@ SIGNATURES = {
     "yh_phase_integrals": (_i, [_P(A.ParamVar), _i, A.Fields, A.Fields,
                                 A.Fields, A.Fields, A.Fields, _v, _v, _v, _v,
                                 _v, _v]),
+    "yh_phase_integrals_noalloc": (_i, [_P(A.ParamVar), _i, A.Fields,
+                                        A.Fields, A.Fields, A.Fields,
+                                        A.Fields, _v, _v, _v, _v, _v]),
+    "yh_phase_integrals_noalloc_limit": (C.c_size_t, []),
     "yh_template_slices": (_i, [_P(A.ParamVar), _i, A.Fields, A.Fields,
                                 A.Fields, A.Fields, _v]),
     "yh_comoving_field": (_i, [_P(A.ParamVar), _v, _v, _v, _v, _v, _i, _v]),
