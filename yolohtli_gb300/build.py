@@ -19,9 +19,10 @@ SOURCES = ["yh_rd.cu", "yh_rd_tb.cu", "yh_rd_resident.cu", "yh_sr.cu", "yh_api.c
            "yh_solver.cu", "yh_compat.cu"]
 
 
-def _compile(src):
-    obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
-    cmd = [NVCC] + ARCH + FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+def _compile(src, out_dir=OUT_DIR, defines=()):
+    obj = os.path.join(out_dir, src.replace(".cu", ".o"))
+    cmd = ([NVCC] + ARCH + FLAGS + ["-D" + d for d in defines] +
+           ["-c", os.path.join(CSRC, src), "-o", obj])
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed on %s:\n%s\n%s" % (src, " ".join(cmd),
@@ -29,21 +30,24 @@ def _compile(src):
     return obj, r.stderr
 
 
-def build(verbose=False):
-    os.makedirs(OUT_DIR, exist_ok=True)
+def build(verbose=False, out_dir=OUT_DIR, defines=()):
+    """Compiles every source into out_dir and links
+    out_dir/libyolohtli_gb300.so; `defines` are extra -D macros."""
+    os.makedirs(out_dir, exist_ok=True)
+    lib = os.path.join(out_dir, os.path.basename(LIB))
     srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
     with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
-        results = list(ex.map(_compile, srcs))
+        results = list(ex.map(lambda s: _compile(s, out_dir, defines), srcs))
     if verbose:
         for obj, err in results:
             if err.strip():
                 sys.stderr.write(err)
     objs = [o for o, _ in results]
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
     subprocess.check_call(cmd)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

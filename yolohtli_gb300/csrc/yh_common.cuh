@@ -80,6 +80,20 @@ __device__ __forceinline__ void ref2v_currents(const StepCoeffs<Real> &a,
   I_v = -(a.eps * (a.delta * (u - a.gamma) * (a.beta - u) - v - a.theta));
 }
 
+// Programmatic dependent launch (PTX griddepcontrol, sm_90+). A kernel
+// launched with programmatic stream serialization may start while its
+// predecessor drains; grid_dep_wait blocks until the predecessor grid has
+// completed and its writes are visible, so it goes before the first global
+// access. grid_dep_launch lets the successor's blocks be scheduled once
+// every block of this grid has issued it. Both are no-ops in a kernel
+// launched without the attribute.
+__device__ __forceinline__ void grid_dep_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void grid_dep_launch() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // PTX approximate base-2 exponential and reciprocal (one MUFU operation
 // each; relative error below 2^-22), enough for the 1e-5 FP32 budget.
 __device__ __forceinline__ float ex2_approx(float x) {

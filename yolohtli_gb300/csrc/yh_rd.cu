@@ -115,8 +115,43 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+#ifndef YH_PDL
+#define YH_PDL 1
+#endif
+
+// Per-cell hole codes of a mask, computed once per grid: bit 0 tissue,
+// bits 1-2 the x pattern and bits 3-4 the y pattern of hole_pattern (the
+// coefficient triples of reactionDiffusion.cu:162-169 with mirrored
+// neighbours at the domain edge). 0x01 is a tissue cell with four tissue
+// neighbours.
+__global__ void hole_codes_kernel(const uint8_t *__restrict__ solid, int nx,
+                                  int ny, uint8_t *__restrict__ codes) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const size_t row = (size_t)nx * j;
+  const bool sc = solid[row + i] != 0;
+  const bool sw = solid[row + mirror(i - 1, nx)] != 0;
+  const bool se = solid[row + mirror(i + 1, nx)] != 0;
+  const bool sn = solid[(size_t)nx * mirror(j + 1, ny) + i] != 0;
+  const bool ss = solid[(size_t)nx * mirror(j - 1, ny) + i] != 0;
+  codes[row + i] = (uint8_t)((sc ? 1u : 0u) | (hole_pattern(sw, sc, se) << 1) |
+                             (hole_pattern(sn, sc, ss) << 3));
+}
+
+cudaError_t launch_hole_codes(const uint8_t *solid, int nx, int ny,
+                              uint8_t *codes, cudaStream_t s) {
+  const dim3 block(32, 8);
+  const dim3 grid((nx + 31) / 32, (ny + 7) / 8);
+  hole_codes_kernel<<<grid, block, 0, s>>>(solid, nx, ny, codes);
+  return cudaGetLastError();
+}
+
 // FP32 fast path: thread (tx, j) owns cells 4*tx .. 4*tx+3 of row j.
-template <int MODEL, bool HOLES, bool TAN>
+// CODES: `solid` holds the per-cell hole codes of hole_codes_kernel instead
+// of the mask; a thread whose 4 cells are all 0x01 takes the select-free
+// expression (the same bits as the coefficient form with (1, 2, 1)).
+template <int MODEL, bool HOLES, bool TAN, bool CODES>
 __global__ void __launch_bounds__(256)
     rd_step_vec4(const StepCoeffs<float> a, const Fld<float> in,
                  const Fld<float> out, const Fld<float> tan,
@@ -131,6 +166,8 @@ __global__ void __launch_bounds__(256)
   const int rowS = nx * mirror(j - 1, ny);
   const int rowN = nx * mirror(j + 1, ny);
   const int iw = mirror(i0 - 1, nx), ie = mirror(i0 + 4, nx);
+  grid_dep_wait();
+  grid_dep_launch();
   const float *__restrict__ U = in.f[0];
   const float4 uc = __ldg(reinterpret_cast<const float4 *>(U + row + i0));
   const float4 un = __ldg(reinterpret_cast<const float4 *>(U + rowN + i0));
@@ -153,13 +190,17 @@ __global__ void __launch_bounds__(256)
   }
   uchar4 mc, mn, ms;
   uint8_t mw = 1, me = 1;
-  if (HOLES) {
+  uint32_t code4 = 0x01010101u;
+  if (HOLES && CODES) {
+    code4 = __ldg(reinterpret_cast<const unsigned int *>(solid + row + i0));
+  } else if (HOLES) {
     mc = *reinterpret_cast<const uchar4 *>(solid + row + i0);
     mn = *reinterpret_cast<const uchar4 *>(solid + rowN + i0);
     ms = *reinterpret_cast<const uchar4 *>(solid + rowS + i0);
     mw = solid[row + iw];
     me = solid[row + ie];
   }
+  const bool plain = HOLES && CODES && code4 == 0x01010101u;
   const float ucv[4] = {uc.x, uc.y, uc.z, uc.w};
   const float unv[4] = {un.x, un.y, un.z, un.w};
   const float usv[4] = {us.x, us.y, us.z, us.w};
@@ -178,16 +219,23 @@ __global__ void __launch_bounds__(256)
     if (NF < 3) x[2] = 0.f;
     bool sc = true;
     float du, dv = 0.f;
-    if (HOLES) {
-      const uint8_t c8[4] = {mc.x, mc.y, mc.z, mc.w};
-      const uint8_t n8[4] = {mn.x, mn.y, mn.z, mn.w};
-      const uint8_t s8[4] = {ms.x, ms.y, ms.z, ms.w};
-      sc = c8[k] != 0;
-      const bool sw = (k == 0 ? mw : c8[k - 1]) != 0;
-      const bool se = (k == 3 ? me : c8[k + 1]) != 0;
+    if (HOLES && !plain) {
       float cxw, cxc, cxe, cyn, cyc, cys;
-      hole_coeffs(sw, sc, se, cxw, cxc, cxe);
-      hole_coeffs(n8[k] != 0, sc, s8[k] != 0, cyn, cyc, cys);
+      if (CODES) {
+        const uint32_t cc = code4 >> (8 * k);
+        sc = (cc & 1u) != 0u;
+        pattern_weights((cc >> 1) & 3u, cxw, cxc, cxe);
+        pattern_weights((cc >> 3) & 3u, cyn, cyc, cys);
+      } else {
+        const uint8_t c8[4] = {mc.x, mc.y, mc.z, mc.w};
+        const uint8_t n8[4] = {mn.x, mn.y, mn.z, mn.w};
+        const uint8_t s8[4] = {ms.x, ms.y, ms.z, ms.w};
+        sc = c8[k] != 0;
+        const bool sw = (k == 0 ? mw : c8[k - 1]) != 0;
+        const bool se = (k == 3 ? me : c8[k + 1]) != 0;
+        hole_coeffs(sw, sc, se, cxw, cxc, cxe);
+        hole_coeffs(n8[k] != 0, sc, s8[k] != 0, cyn, cyc, cys);
+      }
       du = (cxw * uW - cxc * u + cxe * uE) * a.rx +
            (cyn * unv[k] - cyc * u + cys * usv[k]) * a.ry;
       if (vdiff) {
@@ -249,17 +297,32 @@ __global__ void stimulate_box_kernel(Real *u, const uint8_t *solid, int nx,
 template <int MODEL, typename Real, bool HOLES, bool TAN>
 static cudaError_t launch_rd_t(const StepCoeffs<Real> &a, const Fld<Real> &in,
                                const Fld<Real> &out, const Fld<Real> &tan,
-                               const uint8_t *solid, cudaStream_t s) {
+                               const uint8_t *solid, const uint8_t *codes,
+                               cudaStream_t s) {
   if constexpr (std::is_same<Real, float>::value) {
+    const uint8_t *m = HOLES && codes ? codes : solid;
     if ((a.nx % 4) == 0 && aligned16(in, MODEL) && aligned16(out, MODEL) &&
         (!TAN || aligned16(tan, MODEL)) &&
-        (!HOLES || (reinterpret_cast<uintptr_t>(solid) & 3) == 0)) {
+        (!HOLES || (reinterpret_cast<uintptr_t>(m) & 3) == 0)) {
       const dim3 block(64, 4);
       const dim3 grid((a.nx / 4 + block.x - 1) / block.x,
                       (a.ny + block.y - 1) / block.y);
-      rd_step_vec4<MODEL, HOLES, TAN>
-          <<<grid, block, 0, s>>>(a, in, out, tan, solid);
-      return cudaGetLastError();
+      // Programmatic stream serialization: the next step's blocks are
+      // scheduled while this one drains and wait in grid_dep_wait.
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = grid;
+      cfg.blockDim = block;
+      cfg.stream = s;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      attr[0].val.programmaticStreamSerializationAllowed = YH_PDL;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      if (HOLES && codes)
+        return cudaLaunchKernelEx(&cfg, rd_step_vec4<MODEL, HOLES, TAN, true>,
+                                  a, in, out, tan, codes);
+      return cudaLaunchKernelEx(&cfg, rd_step_vec4<MODEL, HOLES, TAN, false>,
+                                a, in, out, tan, solid);
     }
   }
   {
@@ -274,12 +337,13 @@ static cudaError_t launch_rd_t(const StepCoeffs<Real> &a, const Fld<Real> &in,
 template <typename Real>
 cudaError_t launch_rd_step(const StepCoeffs<Real> &a, const Fld<Real> &in,
                            const Fld<Real> &out, const Fld<Real> &tan,
-                           const uint8_t *solid, cudaStream_t s) {
+                           const uint8_t *solid, cudaStream_t s,
+                           const uint8_t *codes) {
   const bool holes = solid != nullptr;
   const bool t = tan.f[0] != nullptr;
 #define YH_RD_CASE(M, H, T)                                             \
   if (a.model == M && holes == H && t == T)                             \
-    return launch_rd_t<M, Real, H, T>(a, in, out, tan, solid, s);
+    return launch_rd_t<M, Real, H, T>(a, in, out, tan, solid, codes, s);
   YH_RD_CASE(YH_MODEL_REF2V, false, false)
   YH_RD_CASE(YH_MODEL_REF2V, false, true)
   YH_RD_CASE(YH_MODEL_REF2V, true, false)
@@ -312,12 +376,14 @@ template cudaError_t launch_rd_step<float>(const StepCoeffs<float> &,
                                            const Fld<float> &,
                                            const Fld<float> &,
                                            const Fld<float> &,
-                                           const uint8_t *, cudaStream_t);
+                                           const uint8_t *, cudaStream_t,
+                                           const uint8_t *);
 template cudaError_t launch_rd_step<double>(const StepCoeffs<double> &,
                                             const Fld<double> &,
                                             const Fld<double> &,
                                             const Fld<double> &,
-                                            const uint8_t *, cudaStream_t);
+                                            const uint8_t *, cudaStream_t,
+                                            const uint8_t *);
 template cudaError_t launch_stimulate<float>(float *, const uint8_t *, int,
                                              int, int, int, int, int, float,
                                              cudaStream_t);

@@ -49,6 +49,7 @@ struct yh_solver {
   float *sr_pool = nullptr;  // tangent, BFECC scratch, template
   Fld<float> cur{}, nxt{}, tan{}, uf{}, ue{}, tx{}, ty{}, tt{};
   uint8_t *solid = nullptr;
+  uint8_t *codes = nullptr;  // per-cell hole codes of solid (same allocation)
   int *tip_count = nullptr;
   yh_tip *tips = nullptr;
   unsigned int *tip_done = nullptr;
@@ -117,10 +118,15 @@ extern "C" int yh_create(const yh_param_var *p, int model,
     h->nxt = carve(h->pool, h->stride, h->nf, 1);
   }
   if (e == cudaSuccess && p->solidSwitch) {
-    e = cudaMalloc(&h->solid, (h->n + 255) & ~(size_t)255);
+    const size_t padded = (h->n + 255) & ~(size_t)255;
+    e = cudaMalloc(&h->solid, 2 * padded);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(h->solid, solid_host, h->n, cudaMemcpyHostToDevice,
                           h->s);
+    if (e == cudaSuccess) {
+      h->codes = h->solid + padded;
+      e = launch_hole_codes(h->solid, p->nx, p->ny, h->codes, h->s);
+    }
   }
   if (e == cudaSuccess) e = cudaMalloc(&h->tip_count, 256);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->tip_count, 0, 256, h->s);
@@ -319,7 +325,8 @@ static cudaError_t enqueue_plain(yh_solver *h, int len) {
       e = launch_rd_tb(a, h->cur, h->nxt, h->solid, k, h->s);
       left -= k;
     } else {
-      e = launch_rd_step<float>(a, h->cur, h->nxt, none, h->solid, h->s);
+      e = launch_rd_step<float>(a, h->cur, h->nxt, none, h->solid, h->s,
+                                h->codes);
       left -= 1;
     }
     if (e != cudaSuccess) return e;
@@ -629,7 +636,8 @@ static cudaError_t enqueue_sr_step(yh_solver *h, bool first) {
   float *advf_rows = h->adv_f, *advf_cols = h->adv_f + h->p.ny;
   cudaError_t e = cudaMemsetAsync(h->tip_count, 0, sizeof(int), h->s);
   if (e == cudaSuccess)  // 1. RD with tangent: cur -> nxt
-    e = launch_rd_step<float>(a, h->cur, h->nxt, h->tan, h->solid, h->s);
+    e = launch_rd_step<float>(a, h->cur, h->nxt, h->tan, h->solid, h->s,
+                              h->codes);
   if (e == cudaSuccess)  // 2. tips x = pre-RD u, y = post-RD u; centre
     e = launch_tips<float>(h->p, h->nxt.f[0], h->cur.f[0], h->p.solidSwitch, 0.0,
                            h->tip_count, h->tips, kTipCapacity, h->sym,
