@@ -137,22 +137,140 @@ __device__ __forceinline__ void fk3v_rates(const StepCoeffs<Real> &a, Real u,
 //   u' = u + tc*du - tc*dt*J,  v' = v + tc*dt*dv/dt,  w' = w + tc*dt*dw/dt
 // (the same step as fk3v_rates + the reference's update
 // u0 += tc*rhs, reactionDiffusion.cu:498-513, with fewer operations).
-// du is the scaled Laplacian rx*(..) + ry*(..). Returns the tangent rhs/dt
-// pieces through ru, rv, rw when the caller needs them.
+// du is the scaled Laplacian (lap5). Every operation is written with its
+// rounding (__f*_rn), so the scalar form and the two-cell f32x2 form
+// (fk3v_update2) give the same bits:
+//   x = (u - u_csi) k2;  sig = 1 / (2^x + 1)
+//   a4 = v ((1 - u)(u - u_c));  J1 = p ? s_tr - a4 s_td : u s_to
+//   Jd = J1 - (w sig) s_tsi;  u' = (u + du tc) - Jd
+//   v' = p ? v - v s_tvp : v + (1 - v) (q ? s_tv1m : s_tv2m)
+//   w' = p ? w - w s_twp : w + (1 - w) s_twm
+// with p = u >= u_c, q = u >= u_v.
 __device__ __forceinline__ void fk3v_update(const StepCoeffs<float> &a,
                                             float u, float v, float w,
                                             float du, float &un, float &vn,
                                             float &wn) {
-  const bool p = u >= a.u_c;
-  const bool q = u >= a.u_v;
-  const float sig = fk_sigmoid(a, u);
-  const float jfi = -v * ((1.f - u) * (u - a.u_c)) * a.s_td;
-  const float Jd = (p ? jfi + a.s_tr : u * a.s_to) - w * sig * a.s_tsi;
-  un = fmaf(a.tc, du, u) - Jd;
-  const float sv = q ? a.s_tv1m : a.s_tv2m;
-  vn = p ? v - v * a.s_tvp : fmaf(1.f - v, sv, v);
-  wn = p ? w - w * a.s_twp : fmaf(1.f - w, a.s_twm, w);
+  const bool p = u >= a.u_c, q = u >= a.u_v;
+  const float x = __fmul_rn(__fsub_rn(u, a.u_csi), a.k_exp2);
+  const float sig = rcp_approx(__fadd_rn(ex2_approx(x), 1.f));
+  const float a4 = __fmul_rn(v, __fmul_rn(__fsub_rn(1.f, u), __fsub_rn(u, a.u_c)));
+  const float jp = __fmaf_rn(a4, -a.s_td, a.s_tr);
+  const float jn = __fmul_rn(u, a.s_to);
+  const float Jd = __fmaf_rn(__fmul_rn(w, sig), -a.s_tsi, p ? jp : jn);
+  un = __fsub_rn(__fmaf_rn(du, a.tc, u), Jd);
+  const float vp = __fmaf_rn(v, -a.s_tvp, v);
+  const float vm = __fmaf_rn(__fsub_rn(1.f, v), q ? a.s_tv1m : a.s_tv2m, v);
+  vn = p ? vp : vm;
+  const float wp = __fmaf_rn(w, -a.s_twp, w);
+  const float wm = __fmaf_rn(__fsub_rn(1.f, w), a.s_twm, w);
+  wn = p ? wp : wm;
 }
+
+// Two FP32 lanes in one 64-bit register for the sm_100+ packed f32x2
+// arithmetic (PTX add/sub/mul/fma .rn.f32x2: each lane rounds as the scalar
+// instruction does, two lanes per issued instruction).
+struct F2 {
+  unsigned long long r;
+};
+__device__ __forceinline__ F2 f2(float lo, float hi) {
+  F2 p;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(p.r) : "f"(lo), "f"(hi));
+  return p;
+}
+__device__ __forceinline__ F2 f2(float x) { return f2(x, x); }
+__device__ __forceinline__ void f2_split(F2 p, float &lo, float &hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(p.r));
+}
+__device__ __forceinline__ F2 add2(F2 a, F2 b) {
+  F2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d.r) : "l"(a.r), "l"(b.r));
+  return d;
+}
+__device__ __forceinline__ F2 sub2(F2 a, F2 b) {
+  F2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d.r) : "l"(a.r), "l"(b.r));
+  return d;
+}
+__device__ __forceinline__ F2 mul2(F2 a, F2 b) {
+  F2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d.r) : "l"(a.r), "l"(b.r));
+  return d;
+}
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
+  F2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d.r) : "l"(a.r), "l"(b.r), "l"(c.r));
+  return d;
+}
+
+// fk3v_update of two cells, the same operations lane by lane in f32x2.
+__device__ __forceinline__ void fk3v_update2(const StepCoeffs<float> &a, F2 U,
+                                             F2 V, F2 W, F2 D, F2 &UN, F2 &VN,
+                                             F2 &WN) {
+  float u0, u1, v0, v1, w0, w1;
+  f2_split(U, u0, u1);
+  const bool p0 = u0 >= a.u_c, p1 = u1 >= a.u_c;
+  const bool q0 = u0 >= a.u_v, q1 = u1 >= a.u_v;
+  const F2 one = f2(1.f);
+  const F2 x = mul2(sub2(U, f2(a.u_csi)), f2(a.k_exp2));
+  float x0, x1, e0, e1;
+  f2_split(x, x0, x1);
+  f2_split(add2(f2(ex2_approx(x0), ex2_approx(x1)), one), e0, e1);
+  const F2 sig = f2(rcp_approx(e0), rcp_approx(e1));
+  const F2 a4 = mul2(V, mul2(sub2(one, U), sub2(U, f2(a.u_c))));
+  float jp0, jp1, jn0, jn1;
+  f2_split(fma2(a4, f2(-a.s_td), f2(a.s_tr)), jp0, jp1);
+  f2_split(mul2(U, f2(a.s_to)), jn0, jn1);
+  const F2 Jd = fma2(mul2(W, sig), f2(-a.s_tsi), f2(p0 ? jp0 : jn0, p1 ? jp1 : jn1));
+  UN = sub2(fma2(D, f2(a.tc), U), Jd);
+  float vp0, vp1, vm0, vm1, wp0, wp1, wm0, wm1;
+  f2_split(fma2(V, f2(-a.s_tvp), V), vp0, vp1);
+  f2_split(fma2(sub2(one, V),
+                f2(q0 ? a.s_tv1m : a.s_tv2m, q1 ? a.s_tv1m : a.s_tv2m), V),
+           vm0, vm1);
+  VN = f2(p0 ? vp0 : vm0, p1 ? vp1 : vm1);
+  f2_split(fma2(W, f2(-a.s_twp), W), wp0, wp1);
+  f2_split(fma2(sub2(one, W), f2(a.s_twm), W), wm0, wm1);
+  WN = f2(p0 ? wp0 : wm0, p1 ? wp1 : wm1);
+  (void)v0; (void)v1; (void)w0; (void)w1;
+}
+
+// Scaled 5-point Laplacian rx (lo - 2c + hi)_x + ry (lo - 2c + hi)_y with
+// explicit rounding: h = (-2 c + lo) + hi per axis, du = hx rx + hy ry. The
+// hole form weights (wlo, wc, whi) per axis, (wlo lo - wc c) + whi hi, gives
+// the same bits for the weights (1, 2, 1).
+__device__ __forceinline__ float lap_axis(float lo, float c, float hi) {
+  return __fadd_rn(__fmaf_rn(-2.f, c, lo), hi);
+}
+__device__ __forceinline__ float lap_axis(float lo, float c, float hi,
+                                          float wlo, float wc, float whi) {
+  return __fmaf_rn(whi, hi, __fmaf_rn(-wc, c, __fmul_rn(wlo, lo)));
+}
+__device__ __forceinline__ float lap5(const StepCoeffs<float> &a, float hx,
+                                      float hy) {
+  return __fmaf_rn(hx, a.rx, __fmul_rn(hy, a.ry));
+}
+__device__ __forceinline__ F2 lap5_2(const StepCoeffs<float> &a, F2 W, F2 C,
+                                     F2 E, F2 N, F2 S) {
+  const F2 m2 = f2(-2.f);
+  const F2 hx = add2(fma2(m2, C, W), E);
+  const F2 hy = add2(fma2(m2, C, N), S);
+  return fma2(hx, f2(a.rx), mul2(hy, f2(a.ry)));
+}
+
+// FK3V update of 4 consecutive cells (u[k], with west/east neighbours uw,
+// ue and the rows above/below un, us). plain: all four cells tissue with
+// tissue neighbours; else `code` holds the four hole codes (byte k: bit 0
+// tissue, bits 1-2 x pattern, bits 3-4 y pattern) and cells outside tissue
+// are set to 0.
+__device__ __forceinline__ void fk3v_cells4(const StepCoeffs<float> &a,
+                                            bool plain, uint32_t code,
+                                            const float (&u)[4], float uw,
+                                            float ue, const float (&un)[4],
+                                            const float (&us)[4],
+                                            const float (&v)[4],
+                                            const float (&w)[4],
+                                            float (&ou)[4], float (&ov)[4],
+                                            float (&ow)[4]);
 
 // Hole pattern of one axis as 2 bits: 0 (1,2,1), 1 (2,2,0), 2 (0,2,2),
 // 3 (0,0,0) — the coefficient triples of reactionDiffusion.cu:162-169.
@@ -165,6 +283,55 @@ __device__ __forceinline__ void pattern_weights(uint32_t pat, float &wlo,
   wlo = pat == 0u ? 1.f : (pat == 1u ? 2.f : 0.f);
   whi = pat == 0u ? 1.f : (pat == 2u ? 2.f : 0.f);
   wc = pat == 3u ? 0.f : 2.f;
+}
+
+__device__ __forceinline__ void fk3v_cells4(const StepCoeffs<float> &a,
+                                            bool plain, uint32_t code,
+                                            const float (&u)[4], float uw,
+                                            float ue, const float (&un)[4],
+                                            const float (&us)[4],
+                                            const float (&v)[4],
+                                            const float (&w)[4],
+                                            float (&ou)[4], float (&ov)[4],
+                                            float (&ow)[4]) {
+  F2 D01, D23;
+  if (plain) {
+    D01 = lap5_2(a, f2(uw, u[0]), f2(u[0], u[1]), f2(u[1], u[2]),
+                 f2(un[0], un[1]), f2(us[0], us[1]));
+    D23 = lap5_2(a, f2(u[1], u[2]), f2(u[2], u[3]), f2(u[3], ue),
+                 f2(un[2], un[3]), f2(us[2], us[3]));
+  } else {
+    float du[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t cc = code >> (8 * k);
+      float cxw, cxc, cxe, cyn, cyc, cys;
+      pattern_weights((cc >> 1) & 3u, cxw, cxc, cxe);
+      pattern_weights((cc >> 3) & 3u, cyn, cyc, cys);
+      const float uW = k == 0 ? uw : u[k - 1];
+      const float uE = k == 3 ? ue : u[k + 1];
+      du[k] = lap5(a, lap_axis(uW, u[k], uE, cxw, cxc, cxe),
+                   lap_axis(un[k], u[k], us[k], cyn, cyc, cys));
+    }
+    D01 = f2(du[0], du[1]);
+    D23 = f2(du[2], du[3]);
+  }
+  F2 un2, vn2, wn2;
+  fk3v_update2(a, f2(u[0], u[1]), f2(v[0], v[1]), f2(w[0], w[1]), D01, un2,
+               vn2, wn2);
+  f2_split(un2, ou[0], ou[1]);
+  f2_split(vn2, ov[0], ov[1]);
+  f2_split(wn2, ow[0], ow[1]);
+  fk3v_update2(a, f2(u[2], u[3]), f2(v[2], v[3]), f2(w[2], w[3]), D23, un2,
+               vn2, wn2);
+  f2_split(un2, ou[2], ou[3]);
+  f2_split(vn2, ov[2], ov[3]);
+  f2_split(wn2, ow[2], ow[3]);
+  if (!plain) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (((code >> (8 * k)) & 1u) == 0u) ou[k] = ov[k] = ow[k] = 0.f;
+  }
 }
 
 // New u, v, w of one cell from its scaled Laplacian du: the FP32 FK3V

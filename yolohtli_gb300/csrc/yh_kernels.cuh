@@ -44,14 +44,16 @@ struct ResidentPlan {
   size_t smem;             // dynamic shared memory per block
 };
 ResidentPlan resident_plan(const StepCoeffs<float> &a, int device);
+// bytes of the tagged boundary-row buffers of a plan
+size_t resident_halo_bytes(const ResidentPlan &pl, int nx);
 // io: the state, updated in place; prev_u (may be null): receives u of the
 // level before the last step.
 cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
                                float *prev_u, const uint8_t *solid,
                                int nsteps, int step0,
                                const yh_stim *stims, int nstims,
-                               const ResidentPlan &pl, float *halo,
-                               unsigned int *flags, int *error,
+                               const ResidentPlan &pl,
+                               unsigned long long *halo, int *error,
                                cudaStream_t s);
 
 // yh_sr.cu

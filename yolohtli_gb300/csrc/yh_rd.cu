@@ -87,21 +87,30 @@ __global__ void __launch_bounds__(256)
   const Real w = NF > 2 ? __ldg(in.f[2] + C) : Real(0);
   bool sc = true;
   Real du, dv = Real(0);
+  constexpr bool F32 = std::is_same<Real, float>::value;
   if (HOLES) {
     sc = solid[C] != 0;
     Real cxw, cxc, cxe, cyn, cyc, cys;
     hole_coeffs(solid[W] != 0, sc, solid[E] != 0, cxw, cxc, cxe);
     hole_coeffs(solid[N] != 0, sc, solid[S] != 0, cyn, cyc, cys);
-    du = (cxw * __ldg(U + W) - cxc * u + cxe * __ldg(U + E)) * a.rx +
-         (cyn * __ldg(U + N) - cyc * u + cys * __ldg(U + S)) * a.ry;
+    if constexpr (F32)
+      du = lap5(a, lap_axis(__ldg(U + W), u, __ldg(U + E), cxw, cxc, cxe),
+                lap_axis(__ldg(U + N), u, __ldg(U + S), cyn, cyc, cys));
+    else
+      du = (cxw * __ldg(U + W) - cxc * u + cxe * __ldg(U + E)) * a.rx +
+           (cyn * __ldg(U + N) - cyc * u + cys * __ldg(U + S)) * a.ry;
     if (MODEL == YH_MODEL_REF2V && a.gate_diff)
       dv = (cxw * __ldg(V + W) - cxc * v + cxe * __ldg(V + E)) * a.rx *
                a.rscale +
            (cyn * __ldg(V + N) - cyc * v + cys * __ldg(V + S)) * a.ry *
                a.rscale;
   } else {
-    du = (__ldg(U + W) - Real(2) * u + __ldg(U + E)) * a.rx +
-         (__ldg(U + N) - Real(2) * u + __ldg(U + S)) * a.ry;
+    if constexpr (F32)
+      du = lap5(a, lap_axis(__ldg(U + W), u, __ldg(U + E)),
+                lap_axis(__ldg(U + N), u, __ldg(U + S)));
+    else
+      du = (__ldg(U + W) - Real(2) * u + __ldg(U + E)) * a.rx +
+           (__ldg(U + N) - Real(2) * u + __ldg(U + S)) * a.ry;
     if (MODEL == YH_MODEL_REF2V && a.gate_diff)
       dv = (__ldg(V + W) - Real(2) * v + __ldg(V + E)) * a.rx * a.rscale +
            (__ldg(V + N) - Real(2) * v + __ldg(V + S)) * a.ry * a.rscale;
@@ -204,6 +213,36 @@ __global__ void __launch_bounds__(256)
   const float ucv[4] = {uc.x, uc.y, uc.z, uc.w};
   const float unv[4] = {un.x, un.y, un.z, un.w};
   const float usv[4] = {us.x, us.y, us.z, us.w};
+  if constexpr (MODEL == YH_MODEL_FK3V && !TAN) {
+    // two f32x2 pairs; the mask form builds the hole codes on the fly
+    if (HOLES && !CODES) {
+      const uint8_t c8[4] = {mc.x, mc.y, mc.z, mc.w};
+      const uint8_t n8[4] = {mn.x, mn.y, mn.z, mn.w};
+      const uint8_t s8[4] = {ms.x, ms.y, ms.z, ms.w};
+      code4 = 0u;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const bool sc = c8[k] != 0;
+        const bool sw = (k == 0 ? mw : c8[k - 1]) != 0;
+        const bool se = (k == 3 ? me : c8[k + 1]) != 0;
+        code4 |= ((sc ? 1u : 0u) | (hole_pattern(sw, sc, se) << 1) |
+                  (hole_pattern(n8[k] != 0, sc, s8[k] != 0) << 3))
+                 << (8 * k);
+      }
+    }
+    const float vv[4] = {fv[1].x, fv[1].y, fv[1].z, fv[1].w};
+    const float ww[4] = {fv[2].x, fv[2].y, fv[2].z, fv[2].w};
+    float ou[4], ov[4], ow[4];
+    fk3v_cells4(a, !HOLES || code4 == 0x01010101u, code4, ucv, uw, ue, unv,
+                usv, vv, ww, ou, ov, ow);
+    *reinterpret_cast<float4 *>(out.f[0] + row + i0) =
+        make_float4(ou[0], ou[1], ou[2], ou[3]);
+    *reinterpret_cast<float4 *>(out.f[1] + row + i0) =
+        make_float4(ov[0], ov[1], ov[2], ov[3]);
+    *reinterpret_cast<float4 *>(out.f[2] + row + i0) =
+        make_float4(ow[0], ow[1], ow[2], ow[3]);
+    return;
+  }
   float res[NF][4], tres[NF][4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
@@ -236,8 +275,8 @@ __global__ void __launch_bounds__(256)
         hole_coeffs(sw, sc, se, cxw, cxc, cxe);
         hole_coeffs(n8[k] != 0, sc, s8[k] != 0, cyn, cyc, cys);
       }
-      du = (cxw * uW - cxc * u + cxe * uE) * a.rx +
-           (cyn * unv[k] - cyc * u + cys * usv[k]) * a.ry;
+      du = lap5(a, lap_axis(uW, u, uE, cxw, cxc, cxe),
+                lap_axis(unv[k], u, usv[k], cyn, cyc, cys));
       if (vdiff) {
         const float4 vc = fv[1];
         const float vcv[4] = {vc.x, vc.y, vc.z, vc.w};
@@ -249,7 +288,7 @@ __global__ void __launch_bounds__(256)
              (cyn * vnv[k] - cyc * vcv[k] + cys * vsv[k]) * a.ry * a.rscale;
       }
     } else {
-      du = (uW - 2.f * u + uE) * a.rx + (unv[k] - 2.f * u + usv[k]) * a.ry;
+      du = lap5(a, lap_axis(uW, u, uE), lap_axis(unv[k], u, usv[k]));
       if (vdiff) {
         const float4 vc = fv[1];
         const float vcv[4] = {vc.x, vc.y, vc.z, vc.w};

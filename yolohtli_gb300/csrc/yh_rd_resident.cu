@@ -6,49 +6,89 @@
 // Block b of nb (one per SM, all co-resident: cooperative launch) owns the
 // rows [r0, r0 + R) of the grid and keeps their u (double-buffered), v, w
 // and hole codes in shared memory for all steps; nothing but two rows of u
-// per block and step leaves the SM. Per step, a block
-//   1. applies the stimulus events of this step to its rows,
-//   2. updates its interior rows 1 .. R-2, which need no other block,
-//   3. waits until both neighbours have published the step's boundary rows
-//      (a per-block step counter, st.release / ld.acquire; the wait is
-//      bounded by 1 s of %globaltimer, then it sets the error flag and the
-//      kernel returns),
-//   4. copies those two rows into its halo rows and updates rows 0, R-1,
-//   5. publishes its new rows 0 and R-1 (double-buffered by step parity)
-//      and its counter.
-// The neighbour wait in 3 overlaps with the interior work of 2. A block can
-// run at most one step ahead of its neighbours, so two halo buffers suffice.
-// The cell update is the one of the single-step kernels (same expression,
-// same bits). The mirror ghost rows at the domain's top and bottom are copies
-// of the block's own rows 1 and R-2 (helper_functions.cu:69-79).
+// per block and step leaves the SM. The block's warps have two roles:
+//   - 16 compute warps update the block's rows for step s, rows 0 and R-1
+//     first, and publish those two rows as soon as they are computed;
+//   - 2 communication warps meanwhile receive the neighbours' boundary rows
+//     of the state after s + 1 steps into the halo rows -1 and R of the
+//     next buffer (the rows step s + 1 reads and step s does not touch).
+// One barrier per step joins the two. A published row is a sequence of
+// 64-bit words (step tag << 32 | bits of u): one relaxed gpu-scope store
+// makes value and tag visible together, so a receiver polls the words
+// themselves and needs no flag and no fence. Every wait is bounded by 1 s
+// of %globaltimer; then the thread sets the error flag and the block
+// returns. A block can run at most one step ahead of its neighbours (it
+// needs their rows of its current step), so two buffers by step parity
+// suffice; the buffers are reset to tag 0xffffffff before each launch, a
+// tag no step uses. The cell update is the one of the single-step kernels
+// (same expression, same bits). The mirror ghost rows at the domain's top
+// and bottom (helper_functions.cu:69-79) are read from the block's own rows
+// 1 and R-2.
 #include "yh_kernels.cuh"
 
 namespace yh {
 
-constexpr int kResThreads = 512;
+#ifndef YH_RES_THREADS
+#define YH_RES_THREADS 512
+#endif
+#ifndef YH_RES_CELLS
+#define YH_RES_CELLS 4
+#endif
+constexpr int kResThreads = YH_RES_THREADS;  // compute threads
+constexpr int kResComm = 64;                 // communication threads
+constexpr int kResBlock = kResThreads + kResComm;
+constexpr int kResBatch = 16;                // halo words per comm thread and pass
+constexpr int kResCells = YH_RES_CELLS;  // cells per work item, rows nx % 4 == 0
 constexpr unsigned long long kResWaitNs = 1000000000ull;  // 1 s
 
 struct ResArgs {
   StepCoeffs<float> a;
-  Fld<float> io;          // state: read at the start, written at the end
-  float *prev_u;          // u before the last step (nullptr: not written)
-  const uint8_t *solid;   // nullptr: no holes
-  float *halo;            // [2][nb][2][nx]: published boundary rows of u
-  unsigned int *flags;    // [nb]: 1 + steps whose boundary rows are published
-  int *error;             // set to 1 when a wait gave up
+  Fld<float> io;                // state: read at the start, written at the end
+  float *prev_u;                // u before the last step (nullptr: not written)
+  const uint8_t *solid;         // nullptr: no holes
+  unsigned long long *halo;     // [2][nb][2][nx] tagged boundary rows of u
+  int *error;                   // set to 1 when a wait gave up
   int nsteps, step0;
   int nb, rq, rrem, rmax;
   int nstims;
   yh_stim stims[kResMaxStims];
 };
 
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
+__device__ __forceinline__ void st_tagged(unsigned long long *p, float v,
+                                          unsigned tag) {
+  const unsigned long long x =
+      ((unsigned long long)tag << 32) | __float_as_uint(v);
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(x)
+               : "memory");
 }
-__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+// CW consecutive tagged words in one relaxed vector store (each 8-byte
+// element is its own single-copy-atomic access); p is 8 * CW byte aligned.
+template <int CW>
+__device__ __forceinline__ void st_tagged_vec(unsigned long long *p,
+                                              const float (&v)[CW],
+                                              unsigned tag) {
+  unsigned long long x[CW];
+#pragma unroll
+  for (int k = 0; k < CW; ++k)
+    x[k] = ((unsigned long long)tag << 32) | __float_as_uint(v[k]);
+  if constexpr (CW == 4)
+    asm volatile("st.relaxed.gpu.global.v4.b64 [%0], {%1, %2, %3, %4};" ::"l"(p),
+                 "l"(x[0]), "l"(x[1]), "l"(x[2]), "l"(x[3])
+                 : "memory");
+  else if constexpr (CW == 2)
+    asm volatile("st.relaxed.gpu.global.v2.b64 [%0], {%1, %2};" ::"l"(p),
+                 "l"(x[0]), "l"(x[1])
+                 : "memory");
+  else
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(x[0])
+                 : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_tagged(
+    const unsigned long long *p) {
+  unsigned long long x;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(x) : "l"(p)
+               : "memory");
+  return x;
 }
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;
@@ -56,95 +96,136 @@ __device__ __forceinline__ unsigned long long globaltimer() {
   return t;
 }
 
-// Updates the cells of rows [lr0, lr1) (local rows) from `cur` into `nxt`.
-// U buffers hold local rows -1 .. R, row lr at offset (lr + 1) * nx.
-template <int MODEL, bool HOLES, bool VEC>
-__device__ __forceinline__ void res_rows(const StepCoeffs<float> &a,
+// One cell update of the single-step kernels from its five u values.
+template <int MODEL, bool HOLES>
+__device__ __forceinline__ void res_cell(const StepCoeffs<float> &a,
+                                         uint32_t cc, float u, float uW,
+                                         float uE, float uN, float uS,
+                                         float v, float w, float &ou,
+                                         float &ov, float &ow) {
+  float du;
+  bool sc = true;
+  if (HOLES && cc != 0x01u) {
+    sc = (cc & 1u) != 0u;
+    float cxw, cxc, cxe, cyn, cyc, cys;
+    pattern_weights((cc >> 1) & 3u, cxw, cxc, cxe);
+    pattern_weights((cc >> 3) & 3u, cyn, cyc, cys);
+    du = lap5(a, lap_axis(uW, u, uE, cxw, cxc, cxe),
+              lap_axis(uN, u, uS, cyn, cyc, cys));
+  } else {
+    du = lap5(a, lap_axis(uW, u, uE), lap_axis(uN, u, uS));
+  }
+  tb_update<MODEL>(a, u, v, w, du, ou, ov, ow);
+  if (HOLES && !sc) ou = ov = ow = 0.f;
+}
+
+// res_cell for any hole code, without branches (weights by selects).
+__device__ __forceinline__ void res_cell_coded(const StepCoeffs<float> &a,
+                                               uint32_t cc, float u, float uW,
+                                               float uE, float uN, float uS,
+                                               float v, float w, float &ou,
+                                               float &ov, float &ow, bool fk) {
+  const bool sc = (cc & 1u) != 0u;
+  float cxw, cxc, cxe, cyn, cyc, cys;
+  pattern_weights((cc >> 1) & 3u, cxw, cxc, cxe);
+  pattern_weights((cc >> 3) & 3u, cyn, cyc, cys);
+  const float du = lap5(a, lap_axis(uW, u, uE, cxw, cxc, cxe),
+                        lap_axis(uN, u, uS, cyn, cyc, cys));
+  if (fk)
+    tb_update<YH_MODEL_FK3V>(a, u, v, w, du, ou, ov, ow);
+  else
+    tb_update<YH_MODEL_REF2V>(a, u, v, w, du, ou, ov, ow);
+  ou = sc ? ou : 0.f;
+  ov = sc ? ov : 0.f;
+  ow = sc ? ow : 0.f;
+}
+
+// CW consecutive floats (CW = 1, 2, 4; 4 CW-byte aligned) as one load/store.
+template <int CW> struct CellVec;
+template <> struct CellVec<1> { using T = float; using C = uint8_t; };
+template <> struct CellVec<2> { using T = float2; using C = uint16_t; };
+template <> struct CellVec<4> { using T = float4; using C = uint32_t; };
+template <int CW>
+__device__ __forceinline__ void ld_cells(const float *p, float (&x)[CW]) {
+  const typename CellVec<CW>::T t = *reinterpret_cast<const typename CellVec<CW>::T *>(p);
+  const float *f = reinterpret_cast<const float *>(&t);
+#pragma unroll
+  for (int k = 0; k < CW; ++k) x[k] = f[k];
+}
+template <int CW>
+__device__ __forceinline__ void st_cells(float *p, const float (&x)[CW]) {
+  typename CellVec<CW>::T t;
+  float *f = reinterpret_cast<float *>(&t);
+#pragma unroll
+  for (int k = 0; k < CW; ++k) f[k] = x[k];
+  *reinterpret_cast<typename CellVec<CW>::T *>(p) = t;
+}
+
+// One work item of a step: CW consecutive cells (from column q * CW) of
+// local row lr. U buffers hold local rows -1 .. R, row lr at offset
+// (lr + 1) * nx. Rows 0 and R-1 are also published, tagged `tag`, into
+// `pub` (row 0 at pub[0 .. nx), row R-1 at pub[nx .. 2 nx)) when a
+// neighbour reads them.
+template <int MODEL, bool HOLES, int CW>
+__device__ __forceinline__ void res_item(const StepCoeffs<float> &a, int lr,
+                                         int q, int R, bool bottom, bool top,
                                          const float *cur, float *nxt,
                                          float *Vs, float *Ws,
-                                         const uint8_t *Cs, int lr0, int lr1) {
+                                         const uint8_t *Cs,
+                                         unsigned long long *pub,
+                                         unsigned tag) {
   const int nx = a.nx;
   constexpr bool W3 = MODEL == YH_MODEL_FK3V;
-  if (VEC) {
-    const int nq = nx >> 2;
-    const int items = (lr1 - lr0) * nq;
-    for (int it = threadIdx.x; it < items; it += kResThreads) {
-      const int lr = lr0 + it / nq;
-      const int i0 = (it - (lr - lr0) * nq) << 2;
-      const float *rc = cur + (lr + 1) * nx;
-      const float4 c = *reinterpret_cast<const float4 *>(rc + i0);
-      const float4 n = *reinterpret_cast<const float4 *>(rc + nx + i0);
-      const float4 s = *reinterpret_cast<const float4 *>(rc - nx + i0);
-      const float uw = rc[mirror(i0 - 1, nx)], ue = rc[mirror(i0 + 4, nx)];
-      float4 *vp = reinterpret_cast<float4 *>(Vs + lr * nx + i0);
-      float4 *wp = reinterpret_cast<float4 *>(Ws + lr * nx + i0);
-      const float4 v4 = *vp;
-      const float4 w4 = W3 ? *wp : make_float4(0.f, 0.f, 0.f, 0.f);
-      uint32_t code = 0x01010101u;
-      if (HOLES) code = *reinterpret_cast<const uint32_t *>(Cs + lr * nx + i0);
-      const float uc[4] = {c.x, c.y, c.z, c.w};
-      const float un_[4] = {n.x, n.y, n.z, n.w};
-      const float us_[4] = {s.x, s.y, s.z, s.w};
-      const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
-      const float ww[4] = {w4.x, w4.y, w4.z, w4.w};
-      float ou[4], ov[4], ow[4];
+  const float *rc = cur + (lr + 1) * nx;
+  const float *rn = (top && lr == R - 1) ? rc - nx : rc + nx;   // mirror
+  const float *rs = (bottom && lr == 0) ? rc + nx : rc - nx;    // mirror
+  const bool publish = (lr == 0 && !bottom) || (lr == R - 1 && !top);
+  unsigned long long *pp = pub + (lr == 0 ? 0 : nx);
+  const int i0 = q * CW;
+  float uc[CW], un_[CW], us_[CW], vv[CW], ww[CW];
+  ld_cells<CW>(rc + i0, uc);
+  ld_cells<CW>(rn + i0, un_);
+  ld_cells<CW>(rs + i0, us_);
+  const float uw = rc[mirror(i0 - 1, nx)], ue = rc[mirror(i0 + CW, nx)];
+  float *vp = Vs + lr * nx + i0;
+  float *wp = Ws + lr * nx + i0;
+  ld_cells<CW>(vp, vv);
+  if (W3) ld_cells<CW>(wp, ww);
+  else
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float uW = k == 0 ? uw : uc[k - 1];
-        const float uE = k == 3 ? ue : uc[k + 1];
-        float du;
-        bool sc = true;
-        if (HOLES && code != 0x01010101u) {
-          const uint32_t cc = code >> (8 * k);
-          sc = (cc & 1u) != 0u;
-          float cxw, cxc, cxe, cyn, cyc, cys;
-          pattern_weights((cc >> 1) & 3u, cxw, cxc, cxe);
-          pattern_weights((cc >> 3) & 3u, cyn, cyc, cys);
-          du = (cxw * uW - cxc * uc[k] + cxe * uE) * a.rx +
-               (cyn * un_[k] - cyc * uc[k] + cys * us_[k]) * a.ry;
-        } else {
-          du = (uW - 2.f * uc[k] + uE) * a.rx +
-               (un_[k] - 2.f * uc[k] + us_[k]) * a.ry;
-        }
-        tb_update<MODEL>(a, uc[k], vv[k], ww[k], du, ou[k], ov[k], ow[k]);
-        if (HOLES && !sc) ou[k] = ov[k] = ow[k] = 0.f;
-      }
-      *reinterpret_cast<float4 *>(nxt + (lr + 1) * nx + i0) =
-          make_float4(ou[0], ou[1], ou[2], ou[3]);
-      *vp = make_float4(ov[0], ov[1], ov[2], ov[3]);
-      if (W3) *wp = make_float4(ow[0], ow[1], ow[2], ow[3]);
+    for (int k = 0; k < CW; ++k) ww[k] = 0.f;
+  uint32_t code = 0;
+  if (HOLES)
+    code = *reinterpret_cast<const typename CellVec<CW>::C *>(Cs + lr * nx + i0);
+  float ou[CW], ov[CW], ow[CW];
+  // all CW cells tissue with tissue neighbours: one branch for the item,
+  // straight-line code over its cells
+  constexpr uint32_t kPlain = CW == 4 ? 0x01010101u : (CW == 2 ? 0x0101u : 0x01u);
+  if constexpr (CW == 4 && MODEL == YH_MODEL_FK3V) {
+    fk3v_cells4(a, !HOLES || code == kPlain, code, uc, uw, ue, un_, us_, vv,
+                ww, ou, ov, ow);
+  } else if (!HOLES || code == kPlain) {
+#pragma unroll
+    for (int k = 0; k < CW; ++k) {
+      const float uW = k == 0 ? uw : uc[k - 1];
+      const float uE = k == CW - 1 ? ue : uc[k + 1];
+      res_cell<MODEL, false>(a, 0x01u, uc[k], uW, uE, un_[k], us_[k], vv[k],
+                             ww[k], ou[k], ov[k], ow[k]);
     }
   } else {
-    const int items = (lr1 - lr0) * nx;
-    for (int it = threadIdx.x; it < items; it += kResThreads) {
-      const int lr = lr0 + it / nx;
-      const int i = it - (lr - lr0) * nx;
-      const float *rc = cur + (lr + 1) * nx;
-      const float uc = rc[i];
-      const float uW = rc[mirror(i - 1, nx)], uE = rc[mirror(i + 1, nx)];
-      const float uN = rc[nx + i], uS = rc[-nx + i];
-      const int C = lr * nx + i;
-      float du;
-      bool sc = true;
-      if (HOLES && Cs[C] != 0x01u) {
-        const uint32_t cc = Cs[C];
-        sc = (cc & 1u) != 0u;
-        float cxw, cxc, cxe, cyn, cyc, cys;
-        pattern_weights((cc >> 1) & 3u, cxw, cxc, cxe);
-        pattern_weights((cc >> 3) & 3u, cyn, cyc, cys);
-        du = (cxw * uW - cxc * uc + cxe * uE) * a.rx +
-             (cyn * uN - cyc * uc + cys * uS) * a.ry;
-      } else {
-        du = (uW - 2.f * uc + uE) * a.rx + (uN - 2.f * uc + uS) * a.ry;
-      }
-      float ou, ov, ow;
-      tb_update<MODEL>(a, uc, Vs[C], W3 ? Ws[C] : 0.f, du, ou, ov, ow);
-      if (HOLES && !sc) ou = ov = ow = 0.f;
-      nxt[(lr + 1) * nx + i] = ou;
-      Vs[C] = ov;
-      if (W3) Ws[C] = ow;
+#pragma unroll
+    for (int k = 0; k < CW; ++k) {
+      const float uW = k == 0 ? uw : uc[k - 1];
+      const float uE = k == CW - 1 ? ue : uc[k + 1];
+      res_cell_coded(a, (code >> (8 * k)) & 0xffu, uc[k], uW, uE, un_[k],
+                     us_[k], vv[k], ww[k], ou[k], ov[k], ow[k],
+                     MODEL == YH_MODEL_FK3V);
     }
   }
+  st_cells<CW>(nxt + (lr + 1) * nx + i0, ou);
+  st_cells<CW>(vp, ov);
+  if (W3) st_cells<CW>(wp, ow);
+  if (publish) st_tagged_vec<CW>(pp + i0, ou, tag);
 }
 
 // u = value on the tissue cells of global row gy held in local buffer row
@@ -154,12 +235,94 @@ __device__ __forceinline__ void res_stim_row(float *row, int gy, int nx,
                                              const uint8_t *solid) {
   if (gy < e.j0 || gy >= e.j1) return;
   const int i0 = e.i0 < 0 ? 0 : e.i0, i1 = e.i1 > nx ? nx : e.i1;
-  for (int i = i0 + (int)threadIdx.x; i < i1; i += kResThreads)
+  for (int i = i0 + (int)threadIdx.x; i < i1; i += kResBlock)
     if (!solid || solid[(size_t)gy * nx + i]) row[i] = e.value;
 }
 
-template <int MODEL, bool HOLES, bool VEC>
-__global__ void __launch_bounds__(kResThreads, 1)
+// Whether any stimulus event of the launch falls on step gs.
+__device__ __forceinline__ bool step_has_stim(const ResArgs &A, int gs) {
+  bool any = false;
+  for (int e = 0; e < A.nstims; ++e) any |= A.stims[e].step == gs;
+  return any;
+}
+
+// u of halo cell (gy, i) after the stimulus events of step gs.
+__device__ __forceinline__ float res_stim_cell(const ResArgs &A, int gs,
+                                               int gy, int i, float u) {
+  for (int e = 0; e < A.nstims; ++e) {
+    const yh_stim &ev = A.stims[e];
+    if (ev.step == gs && gy >= ev.j0 && gy < ev.j1 && i >= ev.i0 &&
+        i < ev.i1 && (!A.solid || A.solid[(size_t)gy * A.a.nx + i]))
+      u = ev.value;
+  }
+  return u;
+}
+
+// Communication threads: receive the halo rows of the state after s steps
+// (words [0, nx): row R-1 of block b-1 into local row -1; [nx, 2 nx): row 0
+// of block b+1 into local row R) into the U buffer `dst`, applying the
+// stimulus events of step gs. Thread c of kResComm reads words
+// p * kResBatch * kResComm + k * kResComm + c of pass p, consecutive threads
+// consecutive words; each pass keeps kResBatch loads in flight and polls
+// stale words until they carry tag s. Returns false when a wait gave up.
+template <int CW>
+__device__ __forceinline__ bool res_receive(const ResArgs &A, int s, int gs,
+                                            int b, int r0, int R, bool bottom,
+                                            bool top, bool stim, float *dst,
+                                            int c) {
+  const int nx = A.a.nx;
+  const unsigned long long *hp =
+      A.halo + (size_t)(s & 1) * ((size_t)A.nb * 2 * nx);
+  const unsigned long long *below = hp + ((size_t)(b - 1) * 2 + 1) * nx;
+  const unsigned long long *above = hp + ((size_t)(b + 1) * 2) * nx;
+  const unsigned want = (unsigned)s;
+  for (int base = 0; base < 2 * nx; base += kResBatch * kResComm) {
+    unsigned long long x[kResBatch];
+#pragma unroll
+    for (int k = 0; k < kResBatch; ++k) {
+      const int e = base + k * kResComm + c;
+      const bool up = e >= nx;
+      const bool need = e < 2 * nx && (up ? !top : !bottom);
+      x[k] = need ? ld_tagged(up ? above + (e - nx) : below + e)
+                  : ((unsigned long long)want << 32);
+    }
+    unsigned long long t0 = 0;  // read on the first miss only
+    for (int spin = 0;; ++spin) {
+      bool ok = true;
+#pragma unroll
+      for (int k = 0; k < kResBatch; ++k) ok &= (unsigned)(x[k] >> 32) == want;
+      if (ok) break;
+      if (spin == 0) t0 = globaltimer();
+      if (((spin & 15) == 15 && *(volatile int *)A.error) ||
+          globaltimer() - t0 > kResWaitNs) {
+        atomicExch(A.error, 1);
+        return false;
+      }
+      __nanosleep(64);
+#pragma unroll
+      for (int k = 0; k < kResBatch; ++k)
+        if ((unsigned)(x[k] >> 32) != want) {
+          const int e = base + k * kResComm + c;
+          const bool up = e >= nx;
+          x[k] = ld_tagged(up ? above + (e - nx) : below + e);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kResBatch; ++k) {
+      const int e = base + k * kResComm + c;
+      const bool up = e >= nx;
+      if (!(e < 2 * nx && (up ? !top : !bottom))) continue;
+      const int i = up ? e - nx : e;
+      float u = __uint_as_float((unsigned)x[k]);
+      if (stim) u = res_stim_cell(A, gs, up ? r0 + R : r0 - 1, i, u);
+      dst[(up ? R + 1 : 0) * nx + i] = u;
+    }
+  }
+  return true;
+}
+
+template <int MODEL, bool HOLES, int CW>
+__global__ void __launch_bounds__(kResBlock, 1)
     rd_resident_kernel(const ResArgs A) {
   extern __shared__ float4 sm4[];
   const StepCoeffs<float> &a = A.a;
@@ -167,19 +330,29 @@ __global__ void __launch_bounds__(kResThreads, 1)
   const int b = blockIdx.x, nb = A.nb, RM = A.rmax;
   const int r0 = b * A.rq + min(b, A.rrem);
   const int R = A.rq + (b < A.rrem ? 1 : 0);
+  const bool bottom = b == 0, top = b == nb - 1;
   float *U0 = reinterpret_cast<float *>(sm4);
   float *U1 = U0 + (RM + 2) * nx;
   float *Vs = U1 + (RM + 2) * nx;
   float *Ws = Vs + RM * nx;
   uint8_t *Cs = reinterpret_cast<uint8_t *>(Ws + RM * nx);
   constexpr bool W3 = MODEL == YH_MODEL_FK3V;
+  const int t = threadIdx.x;
+  const bool comm = t >= kResThreads;  // warps 16, 17
+  const int c = t - kResThreads;
+  const int nq = nx / CW;
+  const int vr0 = t / nq, q0 = t - vr0 * nq;
+  const size_t par_stride = (size_t)nb * 2 * nx;  // words per step parity
   __shared__ int s_abort;
+  if (t == 0) s_abort = 0;
+  __syncthreads();
 
   // load the block's rows; hole codes from the mask with mirrored neighbours
-  for (int idx = threadIdx.x; idx < R * nx; idx += kResThreads) {
+  for (int idx = t; idx < R * nx; idx += kResBlock) {
     const int lr = idx / nx, i = idx - lr * nx, gy = r0 + lr;
     const size_t g = (size_t)gy * nx + i;
-    U0[(lr + 1) * nx + i] = A.io.f[0][g];
+    const float u = A.io.f[0][g];
+    U0[(lr + 1) * nx + i] = u;
     Vs[idx] = A.io.f[1][g];
     if (W3) Ws[idx] = A.io.f[2][g];
     if (HOLES) {
@@ -192,90 +365,60 @@ __global__ void __launch_bounds__(kResThreads, 1)
       Cs[idx] = (uint8_t)((sc ? 1u : 0u) | (hole_pattern(sw, sc, se) << 1) |
                           (hole_pattern(sn, sc, ss) << 3));
     }
+    // the boundary rows of the state after 0 steps, tag 0, buffer 0
+    if (lr == 0 && !bottom) st_tagged(A.halo + (size_t)b * 2 * nx + i, u, 0u);
+    if (lr == R - 1 && !top)
+      st_tagged(A.halo + (size_t)b * 2 * nx + nx + i, u, 0u);
   }
-  // publish the initial boundary rows (state after 0 steps) in halo[0]
-  {
-    float *hb = A.halo + ((size_t)0 * nb + b) * 2 * nx;
-    for (int i = threadIdx.x; i < nx; i += kResThreads) {
-      hb[i] = A.io.f[0][(size_t)r0 * nx + i];
-      hb[nx + i] = A.io.f[0][(size_t)(r0 + R - 1) * nx + i];
-    }
-  }
-  __threadfence();
-  if (threadIdx.x == 0) s_abort = 0;
+  // halo rows of the state after 0 steps
+  if (comm && !res_receive<CW>(A, 0, A.step0, b, r0, R, bottom, top,
+                               step_has_stim(A, A.step0), U0, c))
+    s_abort = 1;
   __syncthreads();
-  if (threadIdx.x == 0) st_release(A.flags + b, 1u);
+  if (s_abort) return;
 
   for (int s = 0; s < A.nsteps; ++s) {
     const int gs = A.step0 + s;
     float *cur = (s & 1) ? U1 : U0;
     float *nxt = (s & 1) ? U0 : U1;
-    // 1. stimulus events of this step on the block's own rows
-    for (int e = 0; e < A.nstims; ++e)
-      if (A.stims[e].step == gs)
-        for (int lr = 0; lr < R; ++lr)
-          res_stim_row(cur + (lr + 1) * nx, r0 + lr, nx, A.stims[e], A.solid);
-    __syncthreads();
-    // 2. interior rows
-    if (R > 2) res_rows<MODEL, HOLES, VEC>(a, cur, nxt, Vs, Ws, Cs, 1, R - 1);
-    // 3. neighbours' boundary rows of the state after s steps
-    if (threadIdx.x == 0) {
-      const unsigned need = (unsigned)s + 1u;
-      const unsigned long long t0 = globaltimer();
-      for (;;) {
-        const bool lo = b == 0 || ld_acquire(A.flags + b - 1) >= need;
-        const bool hi = b == nb - 1 || ld_acquire(A.flags + b + 1) >= need;
-        if (lo && hi) break;
-        if (*(volatile int *)A.error || globaltimer() - t0 > kResWaitNs) {
-          atomicExch(A.error, 1);
-          s_abort = 1;
-          break;
+    // stimulus events of this step on the block's own rows (the halo rows
+    // got theirs when they were received)
+    if (step_has_stim(A, gs)) {
+      for (int e = 0; e < A.nstims; ++e)
+        if (A.stims[e].step == gs)
+          for (int lr = 0; lr < R; ++lr)
+            res_stim_row(cur + (lr + 1) * nx, r0 + lr, nx, A.stims[e], A.solid);
+      __syncthreads();
+    }
+    if (!comm) {
+      // rows 0 and R-1 (published, tag s + 1), then the interior rows, in
+      // the order rows 0, R-1, 1 .. R-2 (virtual row vr), nq items per row,
+      // thread t taking items t, t + T, ...
+      unsigned long long *pub =
+          A.halo + (size_t)((s + 1) & 1) * par_stride + (size_t)b * 2 * nx;
+      for (int vr = vr0, q = q0; vr < R;) {
+        const int lr = vr == 0 ? 0 : (vr == 1 ? R - 1 : vr - 1);
+        res_item<MODEL, HOLES, CW>(a, lr, q, R, bottom, top, cur, nxt, Vs, Ws,
+                                   Cs, pub, (unsigned)s + 1u);
+        q += kResThreads;
+        while (q >= nq) {
+          q -= nq;
+          ++vr;
         }
-        __nanosleep(64);
       }
+    } else if (s + 1 < A.nsteps) {
+      if (!res_receive<CW>(A, s + 1, gs + 1, b, r0, R, bottom, top,
+                           step_has_stim(A, gs + 1), nxt, c))
+        s_abort = 1;
     }
     __syncthreads();
     if (s_abort) return;
-    // 4. halo rows, then the block's first and last rows
-    {
-      const float *hp = A.halo + (size_t)(s & 1) * nb * 2 * nx;
-      float *below = cur;                 // local row -1
-      float *above = cur + (R + 1) * nx;  // local row R
-      for (int i = threadIdx.x; i < nx; i += kResThreads) {
-        below[i] = b > 0 ? __ldcg(hp + ((size_t)(b - 1) * 2 + 1) * nx + i)
-                         : cur[2 * nx + i];          // mirror: row 1
-        above[i] = b < nb - 1 ? __ldcg(hp + ((size_t)(b + 1) * 2) * nx + i)
-                              : cur[(R - 1) * nx + i];  // mirror: row R-2
-      }
-      __syncthreads();
-      for (int e = 0; e < A.nstims; ++e)
-        if (A.stims[e].step == gs) {
-          if (b > 0) res_stim_row(below, r0 - 1, nx, A.stims[e], A.solid);
-          if (b < nb - 1) res_stim_row(above, r0 + R, nx, A.stims[e], A.solid);
-        }
-      __syncthreads();
-      res_rows<MODEL, HOLES, VEC>(a, cur, nxt, Vs, Ws, Cs, 0, 1);
-      if (R > 1)
-        res_rows<MODEL, HOLES, VEC>(a, cur, nxt, Vs, Ws, Cs, R - 1, R);
-    }
-    __syncthreads();
-    // 5. publish the new boundary rows (state after s + 1 steps)
-    {
-      float *hb = A.halo + ((size_t)((s + 1) & 1) * nb + b) * 2 * nx;
-      for (int i = threadIdx.x; i < nx; i += kResThreads) {
-        __stcg(hb + i, nxt[nx + i]);
-        __stcg(hb + nx + i, nxt[R * nx + i]);
-      }
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) st_release(A.flags + b, (unsigned)s + 2u);
   }
 
   // write the state back (and u of the level before the last step)
   const float *fin = (A.nsteps & 1) ? U1 : U0;
   const float *pre = (A.nsteps & 1) ? U0 : U1;
-  for (int idx = threadIdx.x; idx < R * nx; idx += kResThreads) {
+  for (int idx = t; idx < R * nx; idx += kResBlock) {
     const int lr = idx / nx, i = idx - lr * nx;
     const size_t g = (size_t)(r0 + lr) * nx + i;
     A.io.f[0][g] = fin[(lr + 1) * nx + i];
@@ -309,24 +452,28 @@ ResidentPlan resident_plan(const StepCoeffs<float> &a, int device) {
   return pl;
 }
 
-template <int MODEL, bool HOLES, bool VEC>
+size_t resident_halo_bytes(const ResidentPlan &pl, int nx) {
+  return (size_t)2 * pl.nb * 2 * nx * sizeof(unsigned long long);
+}
+
+template <int MODEL, bool HOLES, int CW>
 static cudaError_t launch_res_t(const ResArgs &A, size_t smem,
                                 cudaStream_t s) {
-  auto fn = rd_resident_kernel<MODEL, HOLES, VEC>;
+  auto fn = rd_resident_kernel<MODEL, HOLES, CW>;
   cudaError_t e =
       cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   void *args[] = {const_cast<ResArgs *>(&A)};
   return cudaLaunchCooperativeKernel((const void *)fn, dim3(A.nb),
-                                     dim3(kResThreads), args, smem, s);
+                                     dim3(kResBlock), args, smem, s);
 }
 
 cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
                                float *prev_u, const uint8_t *solid,
                                int nsteps, int step0,
                                const yh_stim *stims, int nstims,
-                               const ResidentPlan &pl, float *halo,
-                               unsigned int *flags, int *error,
+                               const ResidentPlan &pl,
+                               unsigned long long *halo, int *error,
                                cudaStream_t s) {
   if (!pl.ok || nstims > kResMaxStims || nsteps < 0) return cudaErrorInvalidValue;
   if (nsteps == 0) return cudaSuccess;
@@ -336,7 +483,6 @@ cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
   A.prev_u = prev_u;
   A.solid = solid;
   A.halo = halo;
-  A.flags = flags;
   A.error = error;
   A.nsteps = nsteps;
   A.step0 = step0;
@@ -346,13 +492,13 @@ cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
   A.rmax = pl.rmax;
   A.nstims = nstims;
   for (int k = 0; k < nstims; ++k) A.stims[k] = stims[k];
-  cudaError_t e = cudaMemsetAsync(flags, 0, (size_t)pl.nb * sizeof(unsigned), s);
+  cudaError_t e = cudaMemsetAsync(halo, 0xff, resident_halo_bytes(pl, a.nx), s);
   if (e != cudaSuccess) return e;
-  const bool vec = (a.nx % 4) == 0;
+  const bool vec = (a.nx % kResCells) == 0;
   const bool holes = solid != nullptr;
 #define YH_RES(M, H, V)                                         \
   if (a.model == M && holes == H && vec == V)                   \
-    return launch_res_t<M, H, V>(A, pl.smem, s);
+    return launch_res_t<M, H, V ? kResCells : 1>(A, pl.smem, s);
   YH_RES(YH_MODEL_FK3V, false, true)
   YH_RES(YH_MODEL_FK3V, true, true)
   YH_RES(YH_MODEL_FK3V, false, false)

@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(kTbThreads, 1)
           const float uE = k < 3 ? u[r][k + 1] : right;
           const float uN = r < kR - 1 ? u[r + 1][k] : rowN[k];
           const float du =
-              (uW - 2.f * uc + uE) * a.rx + (uN - 2.f * uc + prev[k]) * a.ry;
+              lap5(a, lap_axis(uW, uc, uE), lap_axis(uN, uc, prev[k]));
           tb_update<MODEL>(a, uc, v[k], w[k], du, un[k], v[k], w[k]);
         }
       } else {
@@ -218,10 +218,10 @@ __global__ void __launch_bounds__(kTbThreads, 1)
             float cxw, cxc, cxe, cyn, cyc, cys;
             pattern_weights((c >> 1) & 3u, cxw, cxc, cxe);
             pattern_weights((c >> 3) & 3u, cyn, cyc, cys);
-            du = (cxw * uW - cxc * uc + cxe * uE) * a.rx +
-                 (cyn * uN - cyc * uc + cys * uS) * a.ry;
+            du = lap5(a, lap_axis(uW, uc, uE, cxw, cxc, cxe),
+                      lap_axis(uN, uc, uS, cyn, cyc, cys));
           } else {
-            du = (uW - 2.f * uc + uE) * a.rx + (uN - 2.f * uc + uS) * a.ry;
+            du = lap5(a, lap_axis(uW, uc, uE), lap_axis(uN, uc, uS));
           }
           float nu, nv, nw;
           tb_update<MODEL>(a, uc, v[k], w[k], du, nu, nv, nw);

@@ -66,8 +66,7 @@ struct yh_solver {
   bool own_stream = false;
   int engine = YH_ENGINE_STEP;
   ResidentPlan plan{};       // resident solver layout (plan.ok: usable)
-  float *res_halo = nullptr;
-  unsigned int *res_flags = nullptr;
+  unsigned long long *res_halo = nullptr;  // tagged boundary rows
   int *res_error = nullptr;  // device flag set when a bounded wait gave up
   GraphCache plain[2];
   GraphCache sr[2];
@@ -141,8 +140,7 @@ extern "C" int yh_create(const yh_param_var *p, int model,
       h->plan = resident_plan(make_step_coeffs<float>(h->p, h->model, &h->fk), dev);
   }
   if (e == cudaSuccess && h->plan.ok) {
-    e = cudaMalloc(&h->res_halo, (size_t)2 * h->plan.nb * 2 * p->nx * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&h->res_flags, (size_t)h->plan.nb * sizeof(unsigned));
+    e = cudaMalloc(&h->res_halo, resident_halo_bytes(h->plan, p->nx));
     if (e == cudaSuccess) e = cudaMalloc(&h->res_error, 256);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->res_error, 0, 256, h->s);
   }
@@ -170,7 +168,6 @@ extern "C" int yh_destroy(yh_solver *h) {
   cudaFree(h->adv_d);
   cudaFree(h->adv_f);
   cudaFree(h->res_halo);
-  cudaFree(h->res_flags);
   cudaFree(h->res_error);
   if (h->own_stream) cudaStreamDestroy(h->s);
   delete h;
@@ -299,8 +296,7 @@ static int run_resident(yh_solver *h, int nsteps, const yh_stim *ev,
     // the state stays in h->cur; the previous u level goes to h->nxt (tips)
     cudaError_t e = launch_rd_resident(a, h->cur, h->nxt.f[0], h->solid, len,
                                        h->step, ev + k, m, h->plan,
-                                       h->res_halo, h->res_flags,
-                                       h->res_error, h->s);
+                                       h->res_halo, h->res_error, h->s);
     if (e != cudaSuccess) return st(e);
     h->launches += 1;
     h->step += len;
