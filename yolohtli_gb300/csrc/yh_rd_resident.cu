@@ -24,6 +24,8 @@
 // (same expression, same bits). The mirror ghost rows at the domain's top
 // and bottom (helper_functions.cu:69-79) are read from the block's own rows
 // 1 and R-2.
+#include <algorithm>
+
 #include "yh_kernels.cuh"
 
 namespace yh {
@@ -34,7 +36,7 @@ namespace yh {
 #ifndef YH_RES_CELLS
 #define YH_RES_CELLS 4
 #endif
-constexpr int kResThreads = YH_RES_THREADS;  // compute threads
+constexpr int kResThreads = YH_RES_THREADS;  // most compute threads
 constexpr int kResComm = 64;                 // communication threads
 constexpr int kResBlock = kResThreads + kResComm;
 constexpr int kResBatch = 16;                // halo words per comm thread and pass
@@ -235,24 +237,28 @@ __device__ __forceinline__ void res_stim_row(float *row, int gy, int nx,
                                              const uint8_t *solid) {
   if (gy < e.j0 || gy >= e.j1) return;
   const int i0 = e.i0 < 0 ? 0 : e.i0, i1 = e.i1 > nx ? nx : e.i1;
-  for (int i = i0 + (int)threadIdx.x; i < i1; i += kResBlock)
+  for (int i = i0 + (int)threadIdx.x; i < i1; i += (int)blockDim.x)
     if (!solid || solid[(size_t)gy * nx + i]) row[i] = e.value;
 }
 
-// Whether any stimulus event of the launch falls on step gs.
-__device__ __forceinline__ bool step_has_stim(const ResArgs &A, int gs) {
-  bool any = false;
-  for (int e = 0; e < A.nstims; ++e) any |= A.stims[e].step == gs;
-  return any;
+// Events of the launch are sorted by step (stable, so events of one step
+// keep their order). [e0, e1) is the run of events on step gs, found from
+// cursor `ev` (the first event not before gs) in the block's copy of the
+// event steps; empty when no event falls on gs.
+__device__ __forceinline__ void stim_run(const int *ev_step, int nstims,
+                                         int ev, int gs, int &e0, int &e1) {
+  e0 = e1 = ev;
+  while (e1 < nstims && ev_step[e1] == gs) ++e1;
 }
 
-// u of halo cell (gy, i) after the stimulus events of step gs.
-__device__ __forceinline__ float res_stim_cell(const ResArgs &A, int gs,
-                                               int gy, int i, float u) {
-  for (int e = 0; e < A.nstims; ++e) {
+// u of halo cell (gy, i) after the stimulus events [e0, e1) of one step.
+__device__ __forceinline__ float res_stim_cell(const ResArgs &A, int e0,
+                                               int e1, int gy, int i,
+                                               float u) {
+  for (int e = e0; e < e1; ++e) {
     const yh_stim &ev = A.stims[e];
-    if (ev.step == gs && gy >= ev.j0 && gy < ev.j1 && i >= ev.i0 &&
-        i < ev.i1 && (!A.solid || A.solid[(size_t)gy * A.a.nx + i]))
+    if (gy >= ev.j0 && gy < ev.j1 && i >= ev.i0 && i < ev.i1 &&
+        (!A.solid || A.solid[(size_t)gy * A.a.nx + i]))
       u = ev.value;
   }
   return u;
@@ -261,14 +267,14 @@ __device__ __forceinline__ float res_stim_cell(const ResArgs &A, int gs,
 // Communication threads: receive the halo rows of the state after s steps
 // (words [0, nx): row R-1 of block b-1 into local row -1; [nx, 2 nx): row 0
 // of block b+1 into local row R) into the U buffer `dst`, applying the
-// stimulus events of step gs. Thread c of kResComm reads words
+// stimulus events [e0, e1). Thread c of kResComm reads words
 // p * kResBatch * kResComm + k * kResComm + c of pass p, consecutive threads
 // consecutive words; each pass keeps kResBatch loads in flight and polls
 // stale words until they carry tag s. Returns false when a wait gave up.
 template <int CW>
-__device__ __forceinline__ bool res_receive(const ResArgs &A, int s, int gs,
-                                            int b, int r0, int R, bool bottom,
-                                            bool top, bool stim, float *dst,
+__device__ __forceinline__ bool res_receive(const ResArgs &A, int s, int e0,
+                                            int e1, int b, int r0, int R,
+                                            bool bottom, bool top, float *dst,
                                             int c) {
   const int nx = A.a.nx;
   const unsigned long long *hp =
@@ -314,7 +320,7 @@ __device__ __forceinline__ bool res_receive(const ResArgs &A, int s, int gs,
       if (!(e < 2 * nx && (up ? !top : !bottom))) continue;
       const int i = up ? e - nx : e;
       float u = __uint_as_float((unsigned)x[k]);
-      if (stim) u = res_stim_cell(A, gs, up ? r0 + R : r0 - 1, i, u);
+      if (e1 > e0) u = res_stim_cell(A, e0, e1, up ? r0 + R : r0 - 1, i, u);
       dst[(up ? R + 1 : 0) * nx + i] = u;
     }
   }
@@ -338,17 +344,20 @@ __global__ void __launch_bounds__(kResBlock, 1)
   uint8_t *Cs = reinterpret_cast<uint8_t *>(Ws + RM * nx);
   constexpr bool W3 = MODEL == YH_MODEL_FK3V;
   const int t = threadIdx.x;
-  const bool comm = t >= kResThreads;  // warps 16, 17
-  const int c = t - kResThreads;
+  const int T = (int)blockDim.x - kResComm;  // compute threads (plan.threads)
+  const bool comm = t >= T;  // the last two warps
+  const int c = t - T;
   const int nq = nx / CW;
   const int vr0 = t / nq, q0 = t - vr0 * nq;
   const size_t par_stride = (size_t)nb * 2 * nx;  // words per step parity
   __shared__ int s_abort;
+  __shared__ int s_ev_step[kResMaxStims];
   if (t == 0) s_abort = 0;
+  if (t < A.nstims) s_ev_step[t] = A.stims[t].step;
   __syncthreads();
 
   // load the block's rows; hole codes from the mask with mirrored neighbours
-  for (int idx = t; idx < R * nx; idx += kResBlock) {
+  for (int idx = t; idx < R * nx; idx += (int)blockDim.x) {
     const int lr = idx / nx, i = idx - lr * nx, gy = r0 + lr;
     const size_t g = (size_t)gy * nx + i;
     const float u = A.io.f[0][g];
@@ -371,9 +380,13 @@ __global__ void __launch_bounds__(kResBlock, 1)
       st_tagged(A.halo + (size_t)b * 2 * nx + nx + i, u, 0u);
   }
   // halo rows of the state after 0 steps
-  if (comm && !res_receive<CW>(A, 0, A.step0, b, r0, R, bottom, top,
-                               step_has_stim(A, A.step0), U0, c))
-    s_abort = 1;
+  int ev = 0;  // first event not before the current step
+  {
+    int e0, e1;
+    stim_run(s_ev_step, A.nstims, ev, A.step0, e0, e1);
+    if (comm && !res_receive<CW>(A, 0, e0, e1, b, r0, R, bottom, top, U0, c))
+      s_abort = 1;
+  }
   __syncthreads();
   if (s_abort) return;
 
@@ -383,13 +396,15 @@ __global__ void __launch_bounds__(kResBlock, 1)
     float *nxt = (s & 1) ? U0 : U1;
     // stimulus events of this step on the block's own rows (the halo rows
     // got theirs when they were received)
-    if (step_has_stim(A, gs)) {
-      for (int e = 0; e < A.nstims; ++e)
-        if (A.stims[e].step == gs)
-          for (int lr = 0; lr < R; ++lr)
-            res_stim_row(cur + (lr + 1) * nx, r0 + lr, nx, A.stims[e], A.solid);
+    int e0, e1;
+    stim_run(s_ev_step, A.nstims, ev, gs, e0, e1);
+    if (e1 > e0) {
+      for (int e = e0; e < e1; ++e)
+        for (int lr = 0; lr < R; ++lr)
+          res_stim_row(cur + (lr + 1) * nx, r0 + lr, nx, A.stims[e], A.solid);
       __syncthreads();
     }
+    ev = e1;
     if (!comm) {
       // rows 0 and R-1 (published, tag s + 1), then the interior rows, in
       // the order rows 0, R-1, 1 .. R-2 (virtual row vr), nq items per row,
@@ -400,15 +415,16 @@ __global__ void __launch_bounds__(kResBlock, 1)
         const int lr = vr == 0 ? 0 : (vr == 1 ? R - 1 : vr - 1);
         res_item<MODEL, HOLES, CW>(a, lr, q, R, bottom, top, cur, nxt, Vs, Ws,
                                    Cs, pub, (unsigned)s + 1u);
-        q += kResThreads;
+        q += T;
         while (q >= nq) {
           q -= nq;
           ++vr;
         }
       }
     } else if (s + 1 < A.nsteps) {
-      if (!res_receive<CW>(A, s + 1, gs + 1, b, r0, R, bottom, top,
-                           step_has_stim(A, gs + 1), nxt, c))
+      int n0, n1;
+      stim_run(s_ev_step, A.nstims, ev, gs + 1, n0, n1);
+      if (!res_receive<CW>(A, s + 1, n0, n1, b, r0, R, bottom, top, nxt, c))
         s_abort = 1;
     }
     __syncthreads();
@@ -418,7 +434,7 @@ __global__ void __launch_bounds__(kResBlock, 1)
   // write the state back (and u of the level before the last step)
   const float *fin = (A.nsteps & 1) ? U1 : U0;
   const float *pre = (A.nsteps & 1) ? U0 : U1;
-  for (int idx = t; idx < R * nx; idx += kResBlock) {
+  for (int idx = t; idx < R * nx; idx += (int)blockDim.x) {
     const int lr = idx / nx, i = idx - lr * nx;
     const size_t g = (size_t)(r0 + lr) * nx + i;
     A.io.f[0][g] = fin[(lr + 1) * nx + i];
@@ -449,6 +465,15 @@ ResidentPlan resident_plan(const StepCoeffs<float> &a, int device) {
   pl.smem = (size_t)(2 * (pl.rmax + 2) + 2 * pl.rmax) * a.nx * sizeof(float) +
             (size_t)pl.rmax * a.nx + 64;
   pl.ok = pl.smem <= (size_t)smem_optin && pl.rq >= 2;
+  // compute threads: the fewest rounds of work items at up to kResThreads
+  // threads, then the fewest warps that keep that number of rounds (every
+  // thread the same number of items where the rows allow it)
+  const int cw = (a.nx % kResCells) == 0 ? kResCells : 1;
+  const int items = pl.rmax * (a.nx / cw);
+  const int rounds = (items + kResThreads - 1) / kResThreads;
+  const int per = (items + rounds - 1) / rounds;
+  pl.threads = ((per + 31) / 32) * 32;
+  if (pl.threads > kResThreads) pl.threads = kResThreads;
   return pl;
 }
 
@@ -457,7 +482,7 @@ size_t resident_halo_bytes(const ResidentPlan &pl, int nx) {
 }
 
 template <int MODEL, bool HOLES, int CW>
-static cudaError_t launch_res_t(const ResArgs &A, size_t smem,
+static cudaError_t launch_res_t(const ResArgs &A, size_t smem, int threads,
                                 cudaStream_t s) {
   auto fn = rd_resident_kernel<MODEL, HOLES, CW>;
   cudaError_t e =
@@ -465,7 +490,7 @@ static cudaError_t launch_res_t(const ResArgs &A, size_t smem,
   if (e != cudaSuccess) return e;
   void *args[] = {const_cast<ResArgs *>(&A)};
   return cudaLaunchCooperativeKernel((const void *)fn, dim3(A.nb),
-                                     dim3(kResBlock), args, smem, s);
+                                     dim3(threads + kResComm), args, smem, s);
 }
 
 cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
@@ -492,13 +517,17 @@ cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
   A.rmax = pl.rmax;
   A.nstims = nstims;
   for (int k = 0; k < nstims; ++k) A.stims[k] = stims[k];
+  // by step, stable: events of one step keep their order (a later event
+  // overrides an earlier one on the cells both cover)
+  std::stable_sort(A.stims, A.stims + nstims,
+                   [](const yh_stim &x, const yh_stim &y) { return x.step < y.step; });
   cudaError_t e = cudaMemsetAsync(halo, 0xff, resident_halo_bytes(pl, a.nx), s);
   if (e != cudaSuccess) return e;
   const bool vec = (a.nx % kResCells) == 0;
   const bool holes = solid != nullptr;
 #define YH_RES(M, H, V)                                         \
   if (a.model == M && holes == H && vec == V)                   \
-    return launch_res_t<M, H, V ? kResCells : 1>(A, pl.smem, s);
+    return launch_res_t<M, H, V ? kResCells : 1>(A, pl.smem, pl.threads, s);
   YH_RES(YH_MODEL_FK3V, false, true)
   YH_RES(YH_MODEL_FK3V, true, true)
   YH_RES(YH_MODEL_FK3V, false, false)
