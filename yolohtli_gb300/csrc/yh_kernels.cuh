@@ -41,7 +41,7 @@ constexpr int kResMaxStims = 32;  // stimulus events per resident launch
 struct ResidentPlan {
   bool ok;
   int nb, rq, rrem, rmax;  // blocks, rows per block (rq or rq+1), max rows
-  int threads;             // compute threads per block (+ 64 receiving)
+  int threads;             // compute threads per block (+ 64 or 128 receiving)
   size_t smem;             // dynamic shared memory per block
 };
 ResidentPlan resident_plan(const StepCoeffs<float> &a, int device);

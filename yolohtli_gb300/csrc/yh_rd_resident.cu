@@ -7,9 +7,9 @@
 // rows [r0, r0 + R) of the grid and keeps their u (double-buffered), v, w
 // and hole codes in shared memory for all steps; nothing but two rows of u
 // per block and step leaves the SM. The block's warps have two roles:
-//   - 16 compute warps update the block's rows for step s, rows 0 and R-1
+//   - up to 16 compute warps update the block's rows for step s, rows 0 and R-1
 //     first, and publish those two rows as soon as they are computed;
-//   - 2 communication warps meanwhile receive the neighbours' boundary rows
+//   - 2 or 4 communication warps meanwhile receive the neighbours' boundary rows
 //     of the state after s + 1 steps into the halo rows -1 and R of the
 //     next buffer (the rows step s + 1 reads and step s does not touch).
 // One barrier per step joins the two. A published row is a sequence of
@@ -37,8 +37,7 @@ namespace yh {
 #define YH_RES_CELLS 4
 #endif
 constexpr int kResThreads = YH_RES_THREADS;  // most compute threads
-constexpr int kResComm = 64;                 // communication threads
-constexpr int kResBlock = kResThreads + kResComm;
+constexpr int kResCommMax = 128;  // communication threads (64 or 128)
 constexpr int kResBatch = 16;                // halo words per comm thread and pass
 constexpr int kResCells = YH_RES_CELLS;  // cells per work item, rows nx % 4 == 0
 constexpr unsigned long long kResWaitNs = 1000000000ull;  // 1 s
@@ -50,6 +49,7 @@ struct ResArgs {
   const uint8_t *solid;         // nullptr: no holes
   unsigned long long *halo;     // [2][nb][2][nx] tagged boundary rows of u
   int *error;                   // set to 1 when a wait gave up
+  int threads;            // compute threads; the rest of the block receives
   int nsteps, step0;
   int nb, rq, rrem, rmax;
   int nstims;
@@ -267,26 +267,26 @@ __device__ __forceinline__ float res_stim_cell(const ResArgs &A, int e0,
 // Communication threads: receive the halo rows of the state after s steps
 // (words [0, nx): row R-1 of block b-1 into local row -1; [nx, 2 nx): row 0
 // of block b+1 into local row R) into the U buffer `dst`, applying the
-// stimulus events [e0, e1). Thread c of kResComm reads words
-// p * kResBatch * kResComm + k * kResComm + c of pass p, consecutive threads
+// stimulus events [e0, e1). Thread c of nc reads words
+// p * kResBatch * nc + k * nc + c of pass p, consecutive threads
 // consecutive words; each pass keeps kResBatch loads in flight and polls
 // stale words until they carry tag s. Returns false when a wait gave up.
 template <int CW>
 __device__ __forceinline__ bool res_receive(const ResArgs &A, int s, int e0,
                                             int e1, int b, int r0, int R,
                                             bool bottom, bool top, float *dst,
-                                            int c) {
+                                            int c, int nc) {
   const int nx = A.a.nx;
   const unsigned long long *hp =
       A.halo + (size_t)(s & 1) * ((size_t)A.nb * 2 * nx);
   const unsigned long long *below = hp + ((size_t)(b - 1) * 2 + 1) * nx;
   const unsigned long long *above = hp + ((size_t)(b + 1) * 2) * nx;
   const unsigned want = (unsigned)s;
-  for (int base = 0; base < 2 * nx; base += kResBatch * kResComm) {
+  for (int base = 0; base < 2 * nx; base += kResBatch * nc) {
     unsigned long long x[kResBatch];
 #pragma unroll
     for (int k = 0; k < kResBatch; ++k) {
-      const int e = base + k * kResComm + c;
+      const int e = base + k * nc + c;
       const bool up = e >= nx;
       const bool need = e < 2 * nx && (up ? !top : !bottom);
       x[k] = need ? ld_tagged(up ? above + (e - nx) : below + e)
@@ -304,18 +304,20 @@ __device__ __forceinline__ bool res_receive(const ResArgs &A, int s, int e0,
         atomicExch(A.error, 1);
         return false;
       }
-      __nanosleep(64);
+      // back off (64 ns doubling to 1 us) so that polling takes few issue
+      // slots from the compute warps
+      __nanosleep(64u << (spin < 4 ? spin : 4));
 #pragma unroll
       for (int k = 0; k < kResBatch; ++k)
         if ((unsigned)(x[k] >> 32) != want) {
-          const int e = base + k * kResComm + c;
+          const int e = base + k * nc + c;
           const bool up = e >= nx;
           x[k] = ld_tagged(up ? above + (e - nx) : below + e);
         }
     }
 #pragma unroll
     for (int k = 0; k < kResBatch; ++k) {
-      const int e = base + k * kResComm + c;
+      const int e = base + k * nc + c;
       const bool up = e >= nx;
       if (!(e < 2 * nx && (up ? !top : !bottom))) continue;
       const int i = up ? e - nx : e;
@@ -327,8 +329,8 @@ __device__ __forceinline__ bool res_receive(const ResArgs &A, int s, int e0,
   return true;
 }
 
-template <int MODEL, bool HOLES, int CW>
-__global__ void __launch_bounds__(kResBlock, 1)
+template <int MODEL, bool HOLES, int CW, int NC>
+__global__ void __launch_bounds__(kResThreads + NC, 1)
     rd_resident_kernel(const ResArgs A) {
   extern __shared__ float4 sm4[];
   const StepCoeffs<float> &a = A.a;
@@ -344,8 +346,9 @@ __global__ void __launch_bounds__(kResBlock, 1)
   uint8_t *Cs = reinterpret_cast<uint8_t *>(Ws + RM * nx);
   constexpr bool W3 = MODEL == YH_MODEL_FK3V;
   const int t = threadIdx.x;
-  const int T = (int)blockDim.x - kResComm;  // compute threads (plan.threads)
-  const bool comm = t >= T;  // the last two warps
+  const int T = A.threads;  // compute threads
+  constexpr int nc = NC;    // receiving threads: the last warps
+  const bool comm = t >= T;
   const int c = t - T;
   const int nq = nx / CW;
   const int vr0 = t / nq, q0 = t - vr0 * nq;
@@ -384,7 +387,7 @@ __global__ void __launch_bounds__(kResBlock, 1)
   {
     int e0, e1;
     stim_run(s_ev_step, A.nstims, ev, A.step0, e0, e1);
-    if (comm && !res_receive<CW>(A, 0, e0, e1, b, r0, R, bottom, top, U0, c))
+    if (comm && !res_receive<CW>(A, 0, e0, e1, b, r0, R, bottom, top, U0, c, nc))
       s_abort = 1;
   }
   __syncthreads();
@@ -424,7 +427,7 @@ __global__ void __launch_bounds__(kResBlock, 1)
     } else if (s + 1 < A.nsteps) {
       int n0, n1;
       stim_run(s_ev_step, A.nstims, ev, gs + 1, n0, n1);
-      if (!res_receive<CW>(A, s + 1, n0, n1, b, r0, R, bottom, top, nxt, c))
+      if (!res_receive<CW>(A, s + 1, n0, n1, b, r0, R, bottom, top, nxt, c, nc))
         s_abort = 1;
     }
     __syncthreads();
@@ -481,16 +484,16 @@ size_t resident_halo_bytes(const ResidentPlan &pl, int nx) {
   return (size_t)2 * pl.nb * 2 * nx * sizeof(unsigned long long);
 }
 
-template <int MODEL, bool HOLES, int CW>
-static cudaError_t launch_res_t(const ResArgs &A, size_t smem, int threads,
+template <int MODEL, bool HOLES, int CW, int NC>
+static cudaError_t launch_res_t(const ResArgs &A, size_t smem,
                                 cudaStream_t s) {
-  auto fn = rd_resident_kernel<MODEL, HOLES, CW>;
+  auto fn = rd_resident_kernel<MODEL, HOLES, CW, NC>;
   cudaError_t e =
       cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   void *args[] = {const_cast<ResArgs *>(&A)};
   return cudaLaunchCooperativeKernel((const void *)fn, dim3(A.nb),
-                                     dim3(threads + kResComm), args, smem, s);
+                                     dim3(A.threads + NC), args, smem, s);
 }
 
 cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
@@ -525,9 +528,15 @@ cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
   if (e != cudaSuccess) return e;
   const bool vec = (a.nx % kResCells) == 0;
   const bool holes = solid != nullptr;
+  A.threads = pl.threads;
+  // Receiving threads: 128 take the halo in one pass of loads; with a hole
+  // mask the compute warps are the critical path and 64 (two passes, fewer
+  // warps beside them) measured faster (FK3V 1024^2 on GB300: 3.41 vs 3.79
+  // us per step with 300 holes; 3.03 vs 2.61 without).
+
 #define YH_RES(M, H, V)                                         \
   if (a.model == M && holes == H && vec == V)                   \
-    return launch_res_t<M, H, V ? kResCells : 1>(A, pl.smem, pl.threads, s);
+    return launch_res_t<M, H, V ? kResCells : 1, H ? 64 : kResCommMax>(A, pl.smem, s);
   YH_RES(YH_MODEL_FK3V, false, true)
   YH_RES(YH_MODEL_FK3V, true, true)
   YH_RES(YH_MODEL_FK3V, false, false)
