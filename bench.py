@@ -306,13 +306,16 @@ def main():
     cell_steps = wl.cells * wl.nsteps * args.steps * world
     value = cell_steps / (ms_max * 1e-3) / 1e9
 
-    # Dominant kernel: the RD step (the 12 stimulus kernels per solve are
-    # the only other launches). Algorithmic bytes: 25 B per cell-step
+    # Dominant kernel: the RD step (the stimulus kernels of the events that
+    # fire are the only other launches; the resident engine applies the
+    # events inside its own launch). Algorithmic bytes: 25 B per cell-step
     # (u, v, w read + write in FP32 and the 1-byte hole mask); one launch
     # advances all cells by steps_per_launch steps. The mean launch time is
     # taken over the whole timed region, so it also carries the stimulus
     # kernels, the L2 flushes and the gaps between launches.
-    rd_launches = max(1, launches - args.steps * len(wl.stims))
+    fired = sum(1 for s in wl.stims if s.step < wl.nsteps)
+    stim_launches = 0 if engine == A.YH_ENGINE_RESIDENT else fired
+    rd_launches = max(1, launches - args.steps * stim_launches)
     steps_per_launch = wl.nsteps * args.steps / rd_launches
     avg_launch_s = ms * 1e-3 / rd_launches
     bytes_alg = 25.0 * wl.cells * steps_per_launch
