@@ -161,6 +161,66 @@ def config_of(wl, args, tb, autotuned=False, engine="cpu"):
             "parallelism": "replicas x%d" % args.gpus}
 
 
+def max_over_ranks(x, dist, device):
+    """The largest of one float per rank (the job's time is its slowest
+    rank's); x itself without a process group."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(cells, nsteps, solves, world, seconds):
+    """Whole-job Gcell-steps/s: every rank advances its own replica of
+    `cells` cells by nsteps steps, `solves` times, in `seconds` (the
+    slowest rank's time)."""
+    return cells * nsteps * solves * world / seconds / 1e9
+
+
+def reference_gpu(n=1024, steps=200, warmup=20):
+    """The reference's own reactionDiffusion_kernel (built from its sources
+    into oracle/_ref, launched headless with its 16x16 blocks, one launch per
+    step as reactionDiffusion_wrapper does) on the GB300: REF2V in FP64, the
+    reference's model and precision (it has no FK3V), n x n cells, the
+    reference's default parameters and cross-field initial condition. None
+    without a GPU or without the built reference."""
+    try:
+        import torch
+        from oracle import refgpu as R
+    except Exception:
+        return None
+    if not torch.cuda.is_available() or not R.available():
+        return None
+    from yolohtli_gb300 import _abi as A
+    from yolohtli_gb300 import workloads as W
+    p = A.param_defaults(n, n)
+    p.Lx = p.Ly = 3.0
+    p.hx = p.hy = 3.0 / (n - 1)
+    p = A.param_derive(p)
+    st = W.ref2v_cross(n, n)
+    a = [torch.tensor(np.asarray(x, np.float64), device="cuda") for x in st]
+    b = [torch.zeros_like(a[0]) for _ in range(2)]
+    J = [torch.zeros_like(a[0]) for _ in range(2)]
+    vt = [torch.zeros_like(a[0]) for _ in range(2)]
+    R.set_params(p)
+    for k in range(warmup + steps):
+        if k == warmup:
+            R.sync()
+            t0 = time.perf_counter()
+        R.rd(p, b, a, J, vt)
+        a, b = b, a
+    R.sync()
+    dt = time.perf_counter() - t0
+    return {"value": round(n * n * steps / dt / 1e9, 3), "unit": METRIC,
+            "kernel": "reactionDiffusion_kernel (the reference's own, "
+                      "compiled from its sources for sm_103a)",
+            "model": "REF2V FP64 (the reference's model; it has no FK3V)",
+            "grid": [n, n], "steps": steps,
+            "launch": "16x16 blocks, one launch per step, host-timed over "
+                      "%d launches after %d warm-up" % (steps, warmup)}
+
+
 def run_reference(args, wl):
     rank = env_int("RANK", 0)
     if rank != 0:
@@ -195,6 +255,9 @@ def run_reference(args, wl):
         "e2e": {"value": round(value, 4), "unit": METRIC,
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    rg = reference_gpu()
+    if rg is not None:
+        line["reference_gpu"] = rg
     print(json.dumps(line), flush=True)
 
 
@@ -299,12 +362,9 @@ def main():
         torch.cuda.synchronize()
         clk = clocks.stop()
 
-    t = torch.tensor([ms], device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = max_over_ranks(ms, dist, "cuda")
     cell_steps = wl.cells * wl.nsteps * args.steps * world
-    value = cell_steps / (ms_max * 1e-3) / 1e9
+    value = job_value(wl.cells, wl.nsteps, args.steps, world, ms_max * 1e-3)
 
     # Dominant kernel: the RD step (the stimulus kernels of the events that
     # fire are the only other launches; the resident engine applies the
@@ -354,10 +414,9 @@ def main():
             base[0] += wl.nsteps
             lib.yh_get_state(m.h, C.c_void_p(out_u.data_ptr()), None, None)
         e2e_s = time.perf_counter() - t0
-        et = torch.tensor([e2e_s], device="cuda")
-        if dist:
-            dist.all_reduce(et, op=dist.ReduceOp.MAX)
-        e2e = {"value": round(cell_steps / float(et.item()) / 1e9, 3),
+        e2e_max = max_over_ranks(e2e_s, dist, "cuda")
+        e2e = {"value": round(job_value(wl.cells, wl.nsteps, args.steps, world,
+                                        e2e_max), 3),
                "unit": METRIC, "h2d_bytes_per_step": 3 * 4 * wl.cells,
                "d2h_bytes_per_step": 4 * wl.cells}
 
