@@ -408,6 +408,53 @@ int yh_get_step(yh_solver *h, int *step);
  * every kernel node they run). */
 int yh_get_launch_count(yh_solver *h, long long *n);
 
+/* ------------------------------------------------------------------ */
+/* Layer 3: batched solver (many independent grids, one launch per step)  */
+/* ------------------------------------------------------------------ */
+/* No reference counterpart: the reference solves one grid per process and
+ * keeps its parameters in process-global __constant__ symbols
+ * (main.cu:40-51), which rules out batching. Each instance of a batch has
+ * its own grid size, parameters (D through rx/ry, the FK3V time constants),
+ * hole mask and stimulus events. The instances are packed into groups small
+ * enough to stay in the L2; a run advances each group by all its steps, one
+ * kernel launch per step for the whole group (captured in CUDA graphs), the
+ * groups spread over internal streams that fork from and join the caller's
+ * stream. FK3V in FP32, the same cell update as the single-grid solver
+ * (same bits); nx % 4 == 0. */
+typedef struct yh_batch yh_batch;
+
+/* A stimulus event of one instance of a batch. */
+typedef struct yh_batch_stim {
+  int instance;
+  yh_stim s;
+} yh_batch_stim;
+
+/* count instances: params[k] (nx % 4 == 0, the options of yh_create), fk[k]
+ * and masks[k] (1 byte per cell, nonzero = tissue; NULL: no holes, used
+ * when params[k].solidSwitch). State starts at zero. */
+int yh_batch_create(int count, const yh_param_var *params,
+                    const yh_fk_params *fk, const uint8_t *const *masks,
+                    void *stream, yh_batch **out);
+int yh_batch_destroy(yh_batch *b);
+int yh_batch_synchronize(yh_batch *b);
+/* State of instance k (host or device pointers, nx*ny floats each). */
+int yh_batch_set_state(yh_batch *b, int k, const float *u, const float *v,
+                       const float *w);
+int yh_batch_get_state(yh_batch *b, int k, float *u, float *v, float *w);
+/* Device pointers of instance k's current state (valid until the next step). */
+int yh_batch_state_device(yh_batch *b, int k, yh_fields *cur);
+/* nsteps steps of every instance with the events whose step lies in
+ * [step, step + nsteps); events of one instance and step apply in the
+ * order given. */
+int yh_batch_run(yh_batch *b, int nsteps, const yh_batch_stim *stims,
+                 int nstims);
+/* Schedule of later runs: groups of about group_cells cells (largest
+ * instances first) on `streams` internal streams (1-64). The default is
+ * 1,048,576 cells on 2 streams. */
+int yh_batch_set_schedule(yh_batch *b, long long group_cells, int streams);
+int yh_batch_get_step(yh_batch *b, int *step);
+int yh_batch_get_launch_count(yh_batch *b, long long *n);
+
 #ifdef __cplusplus
 }
 #endif

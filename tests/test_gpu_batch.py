@@ -1,0 +1,139 @@
+"""The batched solver (yh_batch_*): many independent FK3V grids, each with
+its own size, parameters, hole mask and stimulus events, one launch per
+step for the whole batch. Every instance must come out bit for bit as the
+single-grid solver leaves the same grid (the cell update is the same code),
+and within the FP32 budget of the FP64 oracle."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from yolohtli_gb300 import _abi as A
+from yolohtli_gb300 import workloads as W
+from yolohtli_gb300.batch import Batch
+from yolohtli_gb300.ops import YolohtliError
+from yolohtli_gb300.solver import Monodomain
+
+from gpu_util import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _instances(seed=3):
+    """Five grids of different shapes, D, time constants, holes and events."""
+    rng = np.random.default_rng(seed)
+    shapes = [(64, 48), (96, 96), (128, 80), (32, 32), (160, 64)]
+    out = []
+    for k, (nx, ny) in enumerate(shapes):
+        D = float(rng.uniform(5e-4, 1.5e-3))
+        p = A.fk_tissue_params(nx, ny, D=D)
+        fk = A.fk_defaults()
+        for name in W.TAU_NAMES:
+            setattr(fk, name, getattr(fk, name) * float(rng.uniform(0.8, 1.2)))
+        u, v, w = W._ic(nx, ny, rng)
+        solid = None
+        if k % 2 == 0:
+            solid = W.hole_mask(nx, ny, 3 + k, 2.0, 5.0, rng)
+            p.solidSwitch = True
+            for f in (u, v, w):
+                f[solid == 0] = 0.0
+        stims = [W.stim(40 + 37 * k, 0, 0, nx // 2, ny // 2),
+                 W.stim(120 + 11 * k, nx // 3, ny // 3, nx // 3 + 9, ny // 3 + 7, 0.8)]
+        if k == 1:  # two events on one step: the later one wins where both apply
+            stims.append(W.stim(200, 5, 5, 40, 40, 1.0))
+            stims.append(W.stim(200, 20, 20, 60, 60, 0.3))
+        out.append(W.Workload("b%d" % k, p, fk, A.YH_MODEL_FK3V, u, v, w,
+                              solid, stims, 0))
+    return out
+
+
+def _single(wl, runs):
+    m = Monodomain(wl.p, wl.model, wl.fk, solid=wl.solid)
+    m.set_engine(A.YH_ENGINE_STEP, 1)
+    m.set_state(*wl.state0())
+    for n in runs:
+        m.run(n, wl.stims)
+    out = m.get_state()
+    m.close()
+    return out
+
+
+def _batch(insts, runs):
+    b = Batch([w.p for w in insts], [w.fk for w in insts],
+              [w.solid for w in insts])
+    for k, w in enumerate(insts):
+        b.set_state(k, *w.state0())
+    ev = [(k, s) for k, w in enumerate(insts) for s in w.stims]
+    for n in runs:
+        b.run(n, ev)
+    b.synchronize()
+    return b
+
+
+def test_batch_equals_the_single_grid_solver_bitwise():
+    insts = _instances()
+    runs = [130, 170]  # a graph of 64 steps, direct launches, events in both
+    b = _batch(insts, runs)
+    assert b.step_count() == sum(runs)
+    assert b.launch_count() == sum(runs)
+    for k, wl in enumerate(insts):
+        got = b.get_state(k)
+        ref = _single(wl, runs)
+        for f in range(3):
+            assert np.array_equal(got[f], ref[f]), (k, f)
+    b.close()
+
+
+def test_batch_against_the_fp64_oracle():
+    insts = _instances(seed=11)[:3]
+    nsteps = 200
+    b = _batch(insts, [nsteps])
+    for k, wl in enumerate(insts):
+        got = b.get_state(k)
+        ref = O.run(wl.p, wl.model, wl.fk, wl.state0(), nsteps, wl.stims,
+                    wl.solid, dtype=np.float64)
+        assert rel_l2(got[0], ref[0]) < 1e-5, k
+    b.close()
+
+
+def test_more_events_than_one_segment_holds():
+    # 7 events on distinct steps for one instance: the run is split into
+    # segments of at most 4 events per instance
+    wl = _instances()[3]
+    wl.stims = [W.stim(10 + 9 * q, q, q, q + 10, q + 12, 1.0 - 0.1 * q)
+                for q in range(7)]
+    b = _batch([wl], [100])
+    got = b.get_state(0)
+    ref = _single(wl, [100])
+    for f in range(3):
+        assert np.array_equal(got[f], ref[f])
+    b.close()
+
+
+def test_invalid_batches_are_rejected():
+    p = A.fk_tissue_params(30, 32)  # nx % 4 != 0
+    with pytest.raises(YolohtliError) as e:
+        Batch([p], [A.fk_defaults()])
+    assert e.value.status == A.YH_EUNSUPPORTED
+    wl = _instances()[3]
+    b = Batch([wl.p], [wl.fk])
+    crowded = [(0, W.stim(5, 0, 0, 4, 4)) for _ in range(5)]  # 5 on one step
+    with pytest.raises(YolohtliError) as e:
+        b.run(10, crowded)
+    assert e.value.status == A.YH_EOVERFLOW
+    with pytest.raises(YolohtliError) as e:
+        b.run(10, [(1, W.stim(5, 0, 0, 4, 4))])  # no instance 1
+    assert e.value.status == A.YH_EINVAL
+    b.close()
+
+
+def test_config_sized_batch_runs_and_stays_finite():
+    bw = W.fk_batch_256(count=24, nsteps=64)
+    b = Batch([w.p for w in bw.instances], [w.fk for w in bw.instances],
+              [w.solid for w in bw.instances])
+    for k, w in enumerate(bw.instances):
+        b.set_state(k, *w.state0())
+    b.run(bw.nsteps, bw.stims())
+    for k in (0, len(bw.instances) - 1):
+        u = b.get_state(k)[0]
+        assert np.isfinite(u).all()
+    b.close()

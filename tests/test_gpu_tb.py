@@ -54,6 +54,20 @@ def test_blocked_steps_equal_single_steps(nx, ny, holes):
             assert d <= 2e-6, (k, f, d)
 
 
+@pytest.mark.parametrize("nx,ny", [(300, 170), (68, 21), (256, 128), (8, 9)])
+@pytest.mark.parametrize("holes", [False, True])
+def test_two_step_kernel_is_bitwise_two_single_steps(nx, ny, holes):
+    # depth 2 runs rd_2s_kernel (64 x 16 tiles, step 1 on a 1-cell ring from
+    # a 2-cell halo): the tiles at the domain's far edges are cut (300 = 4 x
+    # 64 + 44, 170 = 10 x 16 + 10), the step count is odd (one single step
+    # at the end), and every value must equal the single-step engine's bits
+    p, st, solid = fk_case(nx, ny, holes)
+    ref = run(p, st, solid, 97, 1)
+    got = run(p, st, solid, 97, 2)
+    for f in range(3):
+        assert np.array_equal(got[f], ref[f]), (f, max_abs(got[f], ref[f]))
+
+
 def test_blocked_protocol_with_stimuli_matches_oracle():
     p, st, solid = fk_case(256, 192, True)
     stims = [W.stim(40, 10, 10, 60, 60), W.stim(133, 150, 100, 200, 150)]

@@ -149,6 +149,11 @@ class Stim(C.Structure):
                 ("i1", C.c_int), ("j1", C.c_int), ("value", C.c_float)]
 
 
+class BatchStim(C.Structure):
+    """yh_batch_stim: a stimulus event of one instance of a batch."""
+    _fields_ = [("instance", C.c_int), ("s", Stim)]
+
+
 def param_defaults(nx, ny):
     """The reference's defaults (saveFiles.cu:105-231) for an nx x ny grid,
     with the derived coefficients of main.cu:148-158 (dt not halved).

@@ -58,6 +58,18 @@ SIGNATURES = {
     "yh_get_sym": (_i, [_v, _P(A.SymState)]),
     "yh_get_step": (_i, [_v, _P(_i)]),
     "yh_get_launch_count": (_i, [_v, _P(C.c_longlong)]),
+    # batched solver
+    "yh_batch_create": (_i, [_i, _P(A.ParamVar), _P(A.FKParams), _P(_v), _v,
+                             _P(_v)]),
+    "yh_batch_destroy": (_i, [_v]),
+    "yh_batch_synchronize": (_i, [_v]),
+    "yh_batch_set_state": (_i, [_v, _i, _v, _v, _v]),
+    "yh_batch_get_state": (_i, [_v, _i, _v, _v, _v]),
+    "yh_batch_state_device": (_i, [_v, _i, _P(A.Fields)]),
+    "yh_batch_run": (_i, [_v, _i, _P(A.BatchStim), _i]),
+    "yh_batch_set_schedule": (_i, [_v, C.c_longlong, _i]),
+    "yh_batch_get_step": (_i, [_v, _P(_i)]),
+    "yh_batch_get_launch_count": (_i, [_v, _P(C.c_longlong)]),
 }
 
 

@@ -1,0 +1,105 @@
+"""The batched solver (yh_batch_* in include/yolohtli.h) as a Python class.
+
+Many independent FK3V grids, each with its own size, parameters, hole mask
+and stimulus events, advanced together: one kernel launch per step for each
+group of instances that fits in the L2, the groups on several streams. Host
+arrays are numpy FP32, flat nx*ny, row-major.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+from ._loader import load
+from .ops import check
+
+
+def _f32(x):
+    return np.ascontiguousarray(x, dtype=np.float32)
+
+
+class Batch:
+    """params, fks: one ParamVar / FKParams per instance; masks: one uint8
+    array (nonzero = tissue) or None per instance."""
+
+    def __init__(self, params, fks, masks=None, stream=None):
+        self.lib = load()
+        n = len(params)
+        if masks is None:
+            masks = [None] * n
+        if not (len(fks) == n == len(masks)):
+            raise ValueError("params, fks and masks differ in length")
+        self.params = (A.ParamVar * n)(*[p.copy() for p in params])
+        self.fks = (A.FKParams * n)(*fks)
+        self._masks = [None if m is None else np.ascontiguousarray(m, dtype=np.uint8)
+                       for m in masks]
+        for k, m in enumerate(self._masks):
+            self.params[k].solidSwitch = m is not None
+        mp = (C.c_void_p * n)(*[None if m is None else m.ctypes.data
+                                for m in self._masks])
+        h = C.c_void_p()
+        check("yh_batch_create", self.lib.yh_batch_create(
+            n, self.params, self.fks, mp,
+            C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.h = h
+        self.count = n
+
+    def shape(self, k):
+        return self.params[k].ny, self.params[k].nx
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.yh_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, k, u, v, w):
+        u, v, w = _f32(u), _f32(v), _f32(w)
+        check("yh_batch_set_state", self.lib.yh_batch_set_state(
+            self.h, k, u.ctypes.data, v.ctypes.data, w.ctypes.data))
+
+    def get_state(self, k):
+        ny, nx = self.shape(k)
+        out = [np.empty(nx * ny, np.float32) for _ in range(3)]
+        check("yh_batch_get_state", self.lib.yh_batch_get_state(
+            self.h, k, *[o.ctypes.data for o in out]))
+        return out
+
+    def state_device(self, k):
+        f = A.Fields()
+        check("yh_batch_state_device", self.lib.yh_batch_state_device(
+            self.h, k, C.byref(f)))
+        return f
+
+    def run(self, nsteps, stims=()):
+        """stims: (instance, Stim) pairs."""
+        arr = (A.BatchStim * max(1, len(stims)))()
+        for q, (k, s) in enumerate(stims):
+            arr[q].instance = k
+            arr[q].s = s
+        check("yh_batch_run", self.lib.yh_batch_run(
+            self.h, int(nsteps), arr, len(stims)))
+
+    def set_schedule(self, group_cells, streams):
+        """Groups of about group_cells cells on `streams` internal streams."""
+        check("yh_batch_set_schedule", self.lib.yh_batch_set_schedule(
+            self.h, int(group_cells), int(streams)))
+
+    def synchronize(self):
+        check("yh_batch_synchronize", self.lib.yh_batch_synchronize(self.h))
+
+    def step_count(self):
+        s = C.c_int()
+        check("yh_batch_get_step", self.lib.yh_batch_get_step(self.h, C.byref(s)))
+        return s.value
+
+    def launch_count(self):
+        n = C.c_longlong()
+        check("yh_batch_get_launch_count",
+              self.lib.yh_batch_get_launch_count(self.h, C.byref(n)))
+        return n.value

@@ -1,0 +1,570 @@
+// Batched solver (include/yolohtli.h, layer 3): many independent FK3V grids,
+// each with its own size, parameters, hole mask and stimulus events,
+// advanced together, one kernel launch per step for a whole group of them.
+//
+// Layout: every instance's fields are a slice of three shared arrays
+// (u, v, w), each slice starting on a 256-byte boundary; the hole codes of
+// all instances are one byte array with the same offsets. A unit table
+// assigns each 256-thread block a tile of 8 float4 quads x 32 rows (32 x 32
+// cells) of one instance, so that the rows above and below a thread's quad
+// are mostly its tile's own (L1 reuse); the instance records (coefficients,
+// offsets, this run's events)
+// are copied into shared memory once per block. Stimulus events are applied
+// inside the step (to every u value the step reads, which is what a
+// stimulus kernel before the step would leave there: the reference's
+// stimulus only touches tissue cells, and a non-tissue cell's value enters
+// no tissue cell's update and leaves the step as 0). The step index comes
+// from a device word set before each graph replay plus the node's index.
+// The cell update is fk3v_cells4 of the single-grid kernels: same bits.
+//
+// Schedule: the instances are independent, so a run does not advance them
+// in lockstep. They are packed (largest first) into groups of about
+// `group_cells` cells, small enough that a group's two state levels stay in
+// the L2 for the whole run; each group runs all the run's steps as its own
+// sequence of launches (64-step graphs) on one of `streams` internal
+// streams, so several groups are in flight at once. The streams fork from
+// the caller's stream at the start of a run and join it at the end.
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "yh_kernels.cuh"
+
+namespace yh {
+template <typename Real>
+StepCoeffs<Real> make_step_coeffs(const yh_param_var &p, int model,
+                                  const yh_fk_params *fk);
+int check_params(const yh_param_var *p, int model, const yh_fk_params *fk);
+}  // namespace yh
+
+using namespace yh;
+
+namespace {
+
+constexpr int kBatchEv = 4;          // events per instance and run segment
+constexpr int kBatchThreads = 256;   // threads per block, one quad each
+constexpr int kTileQ = 8;            // tile width in quads (32 cells)
+constexpr int kTileR = 32;           // tile height in rows
+constexpr int kBatchGraphSteps = 64; // even: the state ends where it began
+// default schedule: groups of ~1 M cells (25 MB of state in two levels) on
+// 2 streams, the fastest measured on the 256-instance workload (GB300: 360
+// Gcell-steps/s; 256 K cells x 4 streams 353, 1 M x 4 250, one group 223)
+constexpr long long kBatchGroupCells = 1 << 20;
+constexpr int kBatchStreams = 2;
+
+struct BatchInst {
+  StepCoeffs<float> a;
+  long long off;  // first cell of the instance in the field arrays
+  int holes;      // 1: hole codes at codes + off
+  int nev;        // events of the current run segment
+  yh_stim ev[kBatchEv];
+};
+
+__device__ __forceinline__ bool in_box(const yh_stim &e, int i, int j) {
+  return i >= e.i0 && i < e.i1 && j >= e.j0 && j < e.j1;
+}
+
+__global__ void __launch_bounds__(kBatchThreads)
+    rd_batch_kernel(const BatchInst *__restrict__ insts,
+                    const int2 *__restrict__ units, Fld<float> in,
+                    Fld<float> out, const uint8_t *__restrict__ codes,
+                    const int *__restrict__ base, int di) {
+  __shared__ BatchInst I;
+  const int2 un = units[blockIdx.x];
+  {
+    const int *src = reinterpret_cast<const int *>(insts + un.x);
+    int *dst = reinterpret_cast<int *>(&I);
+    for (int k = threadIdx.x; k < (int)(sizeof(BatchInst) / 4); k += kBatchThreads)
+      dst[k] = __ldg(src + k);
+  }
+  grid_dep_wait();
+  grid_dep_launch();
+  __syncthreads();
+  const StepCoeffs<float> &a = I.a;
+  const int nx = a.nx, ny = a.ny, nq = nx >> 2;
+  // unit.y: tile column (low 16 bits) and tile row (high 16 bits)
+  const int qx = (un.y & 0xffff) * kTileQ + (int)threadIdx.x % kTileQ;
+  const int j = (un.y >> 16) * kTileR + (int)threadIdx.x / kTileQ;
+  if (qx >= nq || j >= ny) return;
+  const int i0 = qx << 2;
+  const int row = nx * j;
+  const int jS = mirror(j - 1, ny), jN = mirror(j + 1, ny);
+  const int rowS = nx * jS, rowN = nx * jN;
+  const int iw = mirror(i0 - 1, nx), ie = mirror(i0 + 4, nx);
+  const float *__restrict__ U = in.f[0] + I.off;
+  const float4 uc = __ldg(reinterpret_cast<const float4 *>(U + row + i0));
+  const float4 unq = __ldg(reinterpret_cast<const float4 *>(U + rowN + i0));
+  const float4 usq = __ldg(reinterpret_cast<const float4 *>(U + rowS + i0));
+  float uw = __ldg(U + row + iw), ue = __ldg(U + row + ie);
+  const float4 v4 = __ldg(reinterpret_cast<const float4 *>(in.f[1] + I.off + row + i0));
+  const float4 w4 = __ldg(reinterpret_cast<const float4 *>(in.f[2] + I.off + row + i0));
+  uint32_t code4 = 0x01010101u;
+  if (I.holes)
+    code4 = __ldg(reinterpret_cast<const unsigned int *>(codes + I.off + row + i0));
+  float u[4] = {uc.x, uc.y, uc.z, uc.w};
+  float uN[4] = {unq.x, unq.y, unq.z, unq.w};
+  float uS[4] = {usq.x, usq.y, usq.z, usq.w};
+  if (I.nev) {
+    const int gs = *base + di;
+    for (int e = 0; e < I.nev; ++e) {
+      const yh_stim &ev = I.ev[e];
+      if (ev.step != gs) continue;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (in_box(ev, i0 + k, j)) u[k] = ev.value;
+        if (in_box(ev, i0 + k, jN)) uN[k] = ev.value;
+        if (in_box(ev, i0 + k, jS)) uS[k] = ev.value;
+      }
+      if (in_box(ev, iw, j)) uw = ev.value;
+      if (in_box(ev, ie, j)) ue = ev.value;
+    }
+  }
+  const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+  const float ww[4] = {w4.x, w4.y, w4.z, w4.w};
+  float ou[4], ov[4], ow[4];
+  fk3v_cells4(a, code4 == 0x01010101u, code4, u, uw, ue, uN, uS, vv, ww, ou,
+              ov, ow);
+  *reinterpret_cast<float4 *>(out.f[0] + I.off + row + i0) =
+      make_float4(ou[0], ou[1], ou[2], ou[3]);
+  *reinterpret_cast<float4 *>(out.f[1] + I.off + row + i0) =
+      make_float4(ov[0], ov[1], ov[2], ov[3]);
+  *reinterpret_cast<float4 *>(out.f[2] + I.off + row + i0) =
+      make_float4(ow[0], ow[1], ow[2], ow[3]);
+}
+
+__global__ void batch_set_base(int *base, int value) { *base = value; }
+
+inline int st(cudaError_t e) {
+  if (e == cudaSuccess) return YH_OK;
+  if (e == cudaErrorMemoryAllocation) return YH_ENOMEM;
+  return YH_ECUDA;
+}
+
+}  // namespace
+
+struct yh_batch {
+  int count = 0;
+  cudaStream_t s = nullptr;
+  bool own_stream = false;
+  std::vector<BatchInst> inst;   // host copy of the records
+  std::vector<size_t> cells;     // nx*ny per instance
+  size_t total = 0;              // cells of the field arrays (padded)
+  float *pool = nullptr;         // [2 levels][3 fields][total]
+  uint8_t *codes = nullptr;      // [total], instances with holes only
+  uint8_t *mask_tmp = nullptr;   // one instance's mask during create
+  BatchInst *d_inst = nullptr;
+  BatchInst *h_stage = nullptr;  // pinned staging copy of inst
+  int2 *d_units = nullptr;
+  int nunits = 0;
+  int *d_base = nullptr;         // one step base per group
+  int cur = 0;                   // level holding the state
+  int step = 0;
+  long long launches = 0;
+  // schedule
+  long long group_cells = 0;
+  int nstreams = 0;
+  std::vector<int> ubeg, uend;   // units of group g: [ubeg[g], uend[g])
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> joins;  // one per internal stream
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaGraphExec_t> graphs;  // [group][starting level]
+  std::vector<int> order;        // instances, largest first
+};
+
+namespace {
+
+Fld<float> level(const yh_batch *b, int l) {
+  Fld<float> f{};
+  for (int k = 0; k < 3; ++k) f.f[k] = b->pool + ((size_t)l * 3 + k) * b->total;
+  return f;
+}
+
+cudaError_t launch_step(yh_batch *b, int g, int lvl, int di, cudaStream_t s) {
+  const Fld<float> in = level(b, lvl), out = level(b, lvl ^ 1);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(b->uend[g] - b->ubeg[g]);
+  cfg.blockDim = dim3(kBatchThreads);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, rd_batch_kernel, b->d_inst,
+                            (const int2 *)(b->d_units + b->ubeg[g]), in, out,
+                            (const uint8_t *)b->codes,
+                            (const int *)(b->d_base + g), di);
+}
+
+// Graph of kBatchGraphSteps steps of group g from level lvl (node k: step
+// base + k); it ends on lvl again.
+int graph_for(yh_batch *b, int g, int lvl, cudaStream_t s,
+              cudaGraphExec_t *out) {
+  cudaGraphExec_t &slot = b->graphs[2 * g + lvl];
+  if (slot) {
+    *out = slot;
+    return YH_OK;
+  }
+  cudaGraph_t gr = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return st(e);
+  cudaError_t eb = cudaSuccess;
+  for (int k = 0; k < kBatchGraphSteps && eb == cudaSuccess; ++k)
+    eb = launch_step(b, g, lvl ^ (k & 1), k, s);
+  e = cudaStreamEndCapture(s, &gr);
+  if (eb != cudaSuccess || e != cudaSuccess) {
+    if (gr) cudaGraphDestroy(gr);
+    return st(eb != cudaSuccess ? eb : e);
+  }
+  e = cudaGraphInstantiate(&slot, gr, 0);
+  cudaGraphDestroy(gr);
+  if (e != cudaSuccess) {
+    slot = nullptr;
+    return st(e);
+  }
+  *out = slot;
+  return YH_OK;
+}
+
+// `len` steps of every group from b->step with the events currently in the
+// records; groups run on the internal streams, forked from and joined to
+// the caller's stream.
+int run_segment(yh_batch *b, int len) {
+  cudaError_t e = cudaEventRecord(b->fork, b->s);
+  for (int q = 0; q < b->nstreams && e == cudaSuccess; ++q)
+    e = cudaStreamWaitEvent(b->streams[q], b->fork, 0);
+  if (e != cudaSuccess) return st(e);
+  const int ngroups = (int)b->ubeg.size();
+  for (int g = 0; g < ngroups; ++g) {
+    cudaStream_t s = b->streams[g % b->nstreams];
+    int lvl = b->cur, step = b->step, left = len;
+    while (left >= kBatchGraphSteps) {
+      cudaGraphExec_t ex = nullptr;
+      int rc = graph_for(b, g, lvl, s, &ex);
+      if (rc) return rc;
+      batch_set_base<<<1, 1, 0, s>>>(b->d_base + g, step);
+      e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaGraphLaunch(ex, s);
+      if (e != cudaSuccess) return st(e);
+      b->launches += kBatchGraphSteps;
+      step += kBatchGraphSteps;
+      left -= kBatchGraphSteps;
+    }
+    if (left > 0) {
+      batch_set_base<<<1, 1, 0, s>>>(b->d_base + g, step);
+      e = cudaGetLastError();
+      for (int k = 0; k < left && e == cudaSuccess; ++k)
+        e = launch_step(b, g, lvl ^ (k & 1), k, s);
+      if (e != cudaSuccess) return st(e);
+      b->launches += left;
+    }
+  }
+  for (int q = 0; q < b->nstreams && e == cudaSuccess; ++q) {
+    e = cudaEventRecord(b->joins[q], b->streams[q]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->s, b->joins[q], 0);
+  }
+  if (e != cudaSuccess) return st(e);
+  if (len & 1) b->cur ^= 1;
+  b->step += len;
+  return YH_OK;
+}
+
+// Packs the instances (largest first) into groups of about group_cells
+// cells and lays out their units; (re)creates the internal streams.
+int plan_schedule(yh_batch *b, long long group_cells, int nstreams) {
+  cudaError_t e = cudaStreamSynchronize(b->s);
+  for (cudaStream_t q : b->streams)
+    if (e == cudaSuccess) e = cudaStreamSynchronize(q);
+  if (e != cudaSuccess) return st(e);
+  for (auto &gx : b->graphs)
+    if (gx) cudaGraphExecDestroy(gx);
+  b->graphs.clear();
+  for (cudaStream_t q : b->streams) cudaStreamDestroy(q);
+  for (cudaEvent_t v : b->joins) cudaEventDestroy(v);
+  b->streams.clear();
+  b->joins.clear();
+  b->group_cells = group_cells;
+  b->nstreams = nstreams;
+  std::vector<int2> units;
+  b->ubeg.clear();
+  b->uend.clear();
+  long long acc = group_cells;  // start a group at the first instance
+  for (int k : b->order) {
+    if (acc >= group_cells) {
+      if (!b->ubeg.empty()) b->uend.push_back((int)units.size());
+      b->ubeg.push_back((int)units.size());
+      acc = 0;
+    }
+    const int tx = (b->inst[k].a.nx / 4 + kTileQ - 1) / kTileQ;
+    const int ty = (b->inst[k].a.ny + kTileR - 1) / kTileR;
+    for (int y = 0; y < ty; ++y)
+      for (int x = 0; x < tx; ++x) units.push_back(make_int2(k, (y << 16) | x));
+    acc += (long long)b->cells[k];
+  }
+  b->uend.push_back((int)units.size());
+  b->nunits = (int)units.size();
+  const int ngroups = (int)b->ubeg.size();
+  b->graphs.assign(2 * ngroups, nullptr);
+  cudaFree(b->d_units);
+  b->d_units = nullptr;
+  cudaFree(b->d_base);
+  b->d_base = nullptr;
+  e = cudaMalloc(&b->d_units, units.size() * sizeof(int2));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_units, units.data(), units.size() * sizeof(int2),
+                        cudaMemcpyHostToDevice, b->s);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_base, ngroups * sizeof(int));
+  for (int q = 0; q < nstreams && e == cudaSuccess; ++q) {
+    cudaStream_t sq = nullptr;
+    cudaEvent_t ev = nullptr;
+    e = cudaStreamCreateWithFlags(&sq, cudaStreamNonBlocking);
+    if (e == cudaSuccess) b->streams.push_back(sq);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) b->joins.push_back(ev);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->s);
+  return st(e);
+}
+
+// Copies the records (with this segment's events) to the device.
+int upload_records(yh_batch *b) {
+  cudaError_t e = cudaStreamSynchronize(b->s);  // the staging copy is free
+  for (cudaStream_t q : b->streams)             // and no group reads d_inst
+    if (e == cudaSuccess) e = cudaStreamSynchronize(q);
+  if (e != cudaSuccess) return st(e);
+  memcpy(b->h_stage, b->inst.data(), b->inst.size() * sizeof(BatchInst));
+  e = cudaMemcpyAsync(b->d_inst, b->h_stage, b->inst.size() * sizeof(BatchInst),
+                      cudaMemcpyHostToDevice, b->s);
+  return st(e);
+}
+
+__global__ void batch_codes(const uint8_t *__restrict__ solid, int nx, int ny,
+                            uint8_t *__restrict__ codes) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const size_t r = (size_t)nx * j;
+  const bool sc = solid[r + i] != 0;
+  const bool sw = solid[r + mirror(i - 1, nx)] != 0;
+  const bool se = solid[r + mirror(i + 1, nx)] != 0;
+  const bool sn = solid[(size_t)nx * mirror(j + 1, ny) + i] != 0;
+  const bool ss = solid[(size_t)nx * mirror(j - 1, ny) + i] != 0;
+  codes[r + i] = (uint8_t)((sc ? 1u : 0u) | (hole_pattern(sw, sc, se) << 1) |
+                           (hole_pattern(sn, sc, ss) << 3));
+}
+
+}  // namespace
+
+extern "C" int yh_batch_destroy(yh_batch *b) {
+  if (!b) return YH_EINVAL;
+  if (b->s) cudaStreamSynchronize(b->s);
+  for (cudaStream_t q : b->streams) cudaStreamSynchronize(q);
+  for (auto &g : b->graphs)
+    if (g) cudaGraphExecDestroy(g);
+  for (cudaStream_t q : b->streams) cudaStreamDestroy(q);
+  for (cudaEvent_t v : b->joins) cudaEventDestroy(v);
+  if (b->fork) cudaEventDestroy(b->fork);
+  cudaFree(b->pool);
+  cudaFree(b->codes);
+  cudaFree(b->mask_tmp);
+  cudaFree(b->d_inst);
+  cudaFreeHost(b->h_stage);
+  cudaFree(b->d_units);
+  cudaFree(b->d_base);
+  if (b->own_stream && b->s) cudaStreamDestroy(b->s);
+  delete b;
+  return YH_OK;
+}
+
+extern "C" int yh_batch_create(int count, const yh_param_var *params,
+                               const yh_fk_params *fk,
+                               const uint8_t *const *masks, void *stream,
+                               yh_batch **out) {
+  if (!out || count <= 0 || !params || !fk) return YH_EINVAL;
+  *out = nullptr;
+  for (int k = 0; k < count; ++k) {
+    const int rc = check_params(&params[k], YH_MODEL_FK3V, &fk[k]);
+    if (rc) return rc;
+    if (params[k].nx % 4 || params[k].nx > (1 << 20) || params[k].ny > (1 << 20))
+      return YH_EUNSUPPORTED;
+    if (params[k].solidSwitch && !masks) return YH_EINVAL;
+  }
+  yh_batch *b = new (std::nothrow) yh_batch();
+  if (!b) return YH_ENOMEM;
+  b->count = count;
+  b->s = (cudaStream_t)stream;
+  cudaError_t e = cudaSuccess;
+  if (!b->s) {
+    e = cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking);
+    b->own_stream = e == cudaSuccess;
+  }
+  b->inst.resize(count);
+  b->cells.resize(count);
+  size_t off = 0, max_cells = 0;
+  bool any_holes = false;
+  for (int k = 0; k < count; ++k) {
+    BatchInst &r = b->inst[k];
+    memset(&r, 0, sizeof(r));
+    r.a = make_step_coeffs<float>(params[k], YH_MODEL_FK3V, &fk[k]);
+    r.off = (long long)off;
+    r.holes = params[k].solidSwitch && masks[k] ? 1 : 0;
+    any_holes |= r.holes != 0;
+    b->cells[k] = (size_t)params[k].nx * params[k].ny;
+    max_cells = std::max(max_cells, b->cells[k]);
+    off += (b->cells[k] + 63) & ~(size_t)63;  // 256-byte slices
+  }
+  b->total = off;
+  b->order.resize(count);
+  for (int k = 0; k < count; ++k) b->order[k] = k;
+  std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) {
+    return b->cells[x] > b->cells[y];
+  });
+  if (e == cudaSuccess)
+    e = cudaMalloc(&b->pool, 2 * 3 * b->total * sizeof(float));
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(b->pool, 0, 2 * 3 * b->total * sizeof(float), b->s);
+  if (e == cudaSuccess && any_holes) e = cudaMalloc(&b->codes, b->total);
+  if (e == cudaSuccess && any_holes) e = cudaMalloc(&b->mask_tmp, max_cells);
+  for (int k = 0; k < count && e == cudaSuccess; ++k) {
+    if (!b->inst[k].holes) continue;
+    const int nx = params[k].nx, ny = params[k].ny;
+    e = cudaMemcpyAsync(b->mask_tmp, masks[k], b->cells[k], cudaMemcpyDefault, b->s);
+    if (e == cudaSuccess) {
+      batch_codes<<<dim3((nx + 31) / 32, (ny + 7) / 8), dim3(32, 8), 0, b->s>>>(
+          b->mask_tmp, nx, ny, b->codes + b->inst[k].off);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->s);  // mask_tmp reused
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_inst, count * sizeof(BatchInst));
+  if (e == cudaSuccess) e = cudaMallocHost(&b->h_stage, count * sizeof(BatchInst));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  int rc = st(e);
+  if (rc == YH_OK) rc = plan_schedule(b, kBatchGroupCells, kBatchStreams);
+  if (rc == YH_OK) rc = upload_records(b);
+  if (rc == YH_OK) rc = st(cudaStreamSynchronize(b->s));
+  if (rc != YH_OK) {
+    yh_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return YH_OK;
+}
+
+extern "C" int yh_batch_synchronize(yh_batch *b) {
+  if (!b) return YH_EINVAL;
+  return st(cudaStreamSynchronize(b->s));
+}
+
+extern "C" int yh_batch_set_state(yh_batch *b, int k, const float *u,
+                                  const float *v, const float *w) {
+  if (!b || k < 0 || k >= b->count || !u || !v || !w) return YH_EINVAL;
+  const Fld<float> f = level(b, b->cur);
+  const float *src[3] = {u, v, w};
+  const size_t n = b->cells[k] * sizeof(float);
+  for (int q = 0; q < 3; ++q) {
+    cudaError_t e = cudaMemcpyAsync(f.f[q] + b->inst[k].off, src[q], n,
+                                    cudaMemcpyDefault, b->s);
+    if (e != cudaSuccess) return st(e);
+  }
+  return st(cudaStreamSynchronize(b->s));
+}
+
+extern "C" int yh_batch_get_state(yh_batch *b, int k, float *u, float *v,
+                                  float *w) {
+  if (!b || k < 0 || k >= b->count) return YH_EINVAL;
+  const Fld<float> f = level(b, b->cur);
+  float *dst[3] = {u, v, w};
+  const size_t n = b->cells[k] * sizeof(float);
+  for (int q = 0; q < 3; ++q) {
+    if (!dst[q]) continue;
+    cudaError_t e = cudaMemcpyAsync(dst[q], f.f[q] + b->inst[k].off, n,
+                                    cudaMemcpyDefault, b->s);
+    if (e != cudaSuccess) return st(e);
+  }
+  return st(cudaStreamSynchronize(b->s));
+}
+
+extern "C" int yh_batch_state_device(yh_batch *b, int k, yh_fields *cur) {
+  if (!b || !cur || k < 0 || k >= b->count) return YH_EINVAL;
+  const Fld<float> f = level(b, b->cur);
+  cur->u = f.f[0] + b->inst[k].off;
+  cur->v = f.f[1] + b->inst[k].off;
+  cur->w = f.f[2] + b->inst[k].off;
+  return YH_OK;
+}
+
+extern "C" int yh_batch_run(yh_batch *b, int nsteps, const yh_batch_stim *stims,
+                            int nstims) {
+  if (!b || nsteps < 0 || nstims < 0 || (nstims && !stims)) return YH_EINVAL;
+  for (int k = 0; k < nstims; ++k)
+    if (stims[k].instance < 0 || stims[k].instance >= b->count) return YH_EINVAL;
+  // events inside this run, by step (stable: the given order within a step)
+  std::vector<yh_batch_stim> ev;
+  for (int k = 0; k < nstims; ++k)
+    if (stims[k].s.step >= b->step && stims[k].s.step < b->step + nsteps)
+      ev.push_back(stims[k]);
+  std::stable_sort(ev.begin(), ev.end(), [](const yh_batch_stim &x,
+                                            const yh_batch_stim &y) {
+    return x.s.step < y.s.step;
+  });
+  const int end = b->step + nsteps;
+  size_t next = 0;
+  bool had_events = true;  // the records may hold a previous run's events
+  while (b->step < end) {
+    // segment: from b->step up to the first step at which some instance
+    // would hold more than kBatchEv events
+    std::vector<int> nev(b->count, 0);
+    size_t k = next;
+    int seg_end = end;
+    while (k < ev.size()) {
+      const int step = ev[k].s.step;
+      size_t k2 = k;
+      while (k2 < ev.size() && ev[k2].s.step == step) ++k2;
+      std::vector<int> trial = nev;
+      bool fits = true;
+      for (size_t q = k; q < k2; ++q) fits &= ++trial[ev[q].instance] <= kBatchEv;
+      if (!fits) {
+        if (k == next) return YH_EOVERFLOW;  // one step holds too many events
+        seg_end = step;
+        break;
+      }
+      nev.swap(trial);
+      k = k2;
+    }
+    if (k != next || had_events) {
+      for (auto &r : b->inst) r.nev = 0;
+      for (size_t q = next; q < k; ++q) {
+        BatchInst &r = b->inst[ev[q].instance];
+        r.ev[r.nev++] = ev[q].s;
+      }
+      const int rc = upload_records(b);
+      if (rc) return rc;
+      had_events = k != next;
+    }
+    next = k;
+    const int rc = run_segment(b, seg_end - b->step);
+    if (rc) return rc;
+  }
+  return YH_OK;
+}
+
+extern "C" int yh_batch_set_schedule(yh_batch *b, long long group_cells,
+                                     int streams) {
+  if (!b || group_cells <= 0 || streams <= 0 || streams > 64) return YH_EINVAL;
+  return plan_schedule(b, group_cells, streams);
+}
+
+extern "C" int yh_batch_get_step(yh_batch *b, int *step) {
+  if (!b || !step) return YH_EINVAL;
+  *step = b->step;
+  return YH_OK;
+}
+
+extern "C" int yh_batch_get_launch_count(yh_batch *b, long long *n) {
+  if (!b || !n) return YH_EINVAL;
+  *n = b->launches;
+  return YH_OK;
+}

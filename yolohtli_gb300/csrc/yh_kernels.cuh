@@ -36,6 +36,13 @@ cudaError_t launch_rd_tb(const StepCoeffs<float> &a, const Fld<float> &in,
                          const Fld<float> &out, const uint8_t *solid,
                          int nsteps, cudaStream_t s);
 
+// yh_rd_2s.cu: two FK3V steps per launch (codes: hole codes or null)
+bool rd_2s_supported(const StepCoeffs<float> &a, const Fld<float> &in,
+                     const Fld<float> &out, bool holes, const uint8_t *codes);
+cudaError_t launch_rd_2s(const StepCoeffs<float> &a, const Fld<float> &in,
+                         const Fld<float> &out, const uint8_t *codes,
+                         cudaStream_t s);
+
 // yh_rd_resident.cu
 constexpr int kResMaxStims = 32;  // stimulus events per resident launch
 struct ResidentPlan {

@@ -318,7 +318,11 @@ static cudaError_t enqueue_plain(yh_solver *h, int len) {
     cudaError_t e;
     if (h->time_block > 1 && left >= 2) {
       const int k = std::min(left, h->time_block);
-      e = launch_rd_tb(a, h->cur, h->nxt, h->solid, k, h->s);
+      if (k == 2 && rd_2s_supported(a, h->cur, h->nxt, h->solid != nullptr,
+                                    h->codes))
+        e = launch_rd_2s(a, h->cur, h->nxt, h->codes, h->s);
+      else
+        e = launch_rd_tb(a, h->cur, h->nxt, h->solid, k, h->s);
       left -= k;
     } else {
       e = launch_rd_step<float>(a, h->cur, h->nxt, none, h->solid, h->s,

@@ -6,8 +6,14 @@ fk_spiral_256      256x256, 10,000 steps, S1 columns 0-9 at t=0, S2 lower-left
 fk_holes_1024      1024x1024, 20,000 steps, 300 circular holes (r ~ U[2,6]
                    cells), 12 S2 patches of 40x40 at uniform positions and
                    times ~ U[200,400] ms: fibrillation-like.
-All use dx = 0.025 cm, D = 0.001 cm^2/ms, dt = 0.05 ms (D dt/dx^2 = 0.08),
-the Fenton-Karma BR-fit parameters, u = U(-0.01, 0.01), v = w = 1.
+fk_batch_256       256 independent square grids, n ~ U{128, 160, ..., 768},
+                   5,000 steps, D ~ U[5e-4, 1.5e-3] cm^2/ms, every FK time
+                   constant scaled by exp(U[ln 0.8, ln 1.2]), 0-100 holes
+                   each (r ~ U[2,6]), S2 on the lower-left quadrant at
+                   t ~ U[280, 360] ms: the batched solver's workload.
+All use dx = 0.025 cm, dt = 0.05 ms, u = U(-0.01, 0.01), v = w = 1, S1 on
+columns 0-9; the single grids D = 0.001 cm^2/ms (D dt/dx^2 = 0.08) and the
+Fenton-Karma BR-fit parameters.
 """
 from dataclasses import dataclass, field
 
@@ -106,3 +112,50 @@ def ref2v_cross(nx, ny):
     u[:, : nx // 8] = 1.0
     v[ny // 2:, :] = 1.0
     return u.ravel(), v.ravel()
+
+
+TAU_NAMES = ("tau_d", "tau_r", "tau_si", "tau_0", "tau_v_plus",
+             "tau_v1_minus", "tau_v2_minus", "tau_w_plus", "tau_w_minus")
+
+
+@dataclass
+class BatchWorkload:
+    name: str
+    instances: list  # of Workload
+    nsteps: int
+
+    @property
+    def cells(self):
+        return sum(w.cells for w in self.instances)
+
+    def stims(self):
+        """(instance, Stim) pairs of every instance."""
+        return [(k, s) for k, w in enumerate(self.instances) for s in w.stims]
+
+
+def fk_batch_256(seed=0, count=256, nsteps=5000, sizes=range(128, 769, 32),
+                 max_holes=100):
+    rng = np.random.default_rng(seed)
+    sizes = list(sizes)
+    inst = []
+    for k in range(count):
+        n = int(sizes[int(rng.integers(0, len(sizes)))])
+        D = float(rng.uniform(5e-4, 1.5e-3))
+        p = A.fk_tissue_params(n, n, D=D)
+        fk = A.fk_defaults()
+        for name in TAU_NAMES:
+            setattr(fk, name, getattr(fk, name) *
+                    float(np.exp(rng.uniform(np.log(0.8), np.log(1.2)))))
+        u, v, w = _ic(n, n, rng)
+        nh = int(rng.integers(0, max_holes + 1))
+        solid = None
+        if nh:
+            solid = hole_mask(n, n, nh, 2.0, 6.0, rng)
+            p.solidSwitch = True
+            for f in (u, v, w):
+                f[solid.ravel() == 0] = 0.0
+        t = float(rng.uniform(280.0, 360.0))
+        s2 = stim(int(round(t / p.dt)), 0, 0, n // 2, n // 2)
+        inst.append(Workload("fk_batch_%d" % k, p, fk, A.YH_MODEL_FK3V,
+                             u, v, w, solid, [s2], nsteps))
+    return BatchWorkload("fk_batch_%d" % count, inst, nsteps)
