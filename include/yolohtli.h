@@ -455,6 +455,44 @@ int yh_batch_set_schedule(yh_batch *b, long long group_cells, int streams);
 int yh_batch_get_step(yh_batch *b, int *step);
 int yh_batch_get_launch_count(yh_batch *b, long long *n);
 
+/* ------------------------------------------------------------------ */
+/* Layer 4: the reference's interchange files                           */
+/* ------------------------------------------------------------------ */
+/* Line for line the files the reference writes for its MATLAB
+ * post-processing (same labels, order and printf conversions: the output of
+ * the same data is byte-identical). Host code, no GPU. Each returns YH_OK
+ * or YH_EINVAL (argument, open or write error). */
+
+/* dataparamcsv.csv: printParameters (printFunctions.cu:266-403). ic_path and
+ * results_path fill the two path lines (NULL: "NA", as the reference writes
+ * when it neither loads nor saves). */
+int yh_write_param_csv(const char *path, const yh_param_var *p,
+                       const char *ic_path, const char *results_path);
+/* Reads it back as loadParamValues does (saveFiles.cu:540-711): the second
+ * field of every line from the third on, as a float, into the fields the
+ * writer wrote; count and physicalTime reset, animate set. */
+int yh_read_param_csv(const char *path, yh_param_var *p);
+/* raw_data.dat: "u v" per cell, row-major (print2D2column,
+ * printFunctions.cu:58-78); the reader is loadData (saveFiles.cu:507-537). */
+int yh_write_raw_data(const char *path, const yh_param_var *p, const float *u,
+                      const float *v);
+int yh_read_raw_data(const char *path, const yh_param_var *p, float *u,
+                     float *v);
+/* raw_data<count>.dat of the symmetry-reduced saves: the window of
+ * 2*tipOffset+2 cells around (tipx, tipy) (print2DSubWindow,
+ * printFunctions.cu:80-103); YH_EINVAL when it leaves the grid. */
+int yh_write_raw_window(const char *path, const yh_param_var *p,
+                        const float *u, const float *v);
+/* dataTip.dat ("x y vx vy t" per tip) and dataTipSize.dat (the count, only
+ * when n > 0), truncated when append == 0 (printTip,
+ * printFunctions.cu:149-197). */
+int yh_write_tips(const char *tip_path, const char *size_path,
+                  const yh_tip *tips, int n, int append);
+/* c_phi_list_sym.dat: "cx cy ctheta phix phiy phitheta" per entry, c and phi
+ * n x 3 (printSym, printFunctions.cu:249-264). */
+int yh_write_sym_list(const char *path, const double *c, const double *phi,
+                      int n);
+
 #ifdef __cplusplus
 }
 #endif

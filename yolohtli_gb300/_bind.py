@@ -70,6 +70,15 @@ SIGNATURES = {
     "yh_batch_set_schedule": (_i, [_v, C.c_longlong, _i]),
     "yh_batch_get_step": (_i, [_v, _P(_i)]),
     "yh_batch_get_launch_count": (_i, [_v, _P(C.c_longlong)]),
+    # the reference's interchange files
+    "yh_write_param_csv": (_i, [C.c_char_p, _P(A.ParamVar), C.c_char_p,
+                                C.c_char_p]),
+    "yh_read_param_csv": (_i, [C.c_char_p, _P(A.ParamVar)]),
+    "yh_write_raw_data": (_i, [C.c_char_p, _P(A.ParamVar), _v, _v]),
+    "yh_read_raw_data": (_i, [C.c_char_p, _P(A.ParamVar), _v, _v]),
+    "yh_write_raw_window": (_i, [C.c_char_p, _P(A.ParamVar), _v, _v]),
+    "yh_write_tips": (_i, [C.c_char_p, C.c_char_p, _P(A.Tip), _i, _i]),
+    "yh_write_sym_list": (_i, [C.c_char_p, _v, _v, _i]),
 }
 
 

@@ -129,6 +129,17 @@ class Monodomain:
         return np.array([[buf[k].x, buf[k].y, buf[k].vx, buf[k].vy, buf[k].t]
                          for k in range(m)], np.float32).reshape(m, 5)
 
+    def save_raw_data(self, path):
+        """The state as the reference's raw_data.dat ("u v" per cell)."""
+        from . import refio
+        u, v = self.get_state()[:2]
+        refio.write_raw_data(path, self.p, u, v)
+
+    def save_param_csv(self, path, ic_path=None, results_path=None):
+        """The parameters as the reference's dataparamcsv.csv."""
+        from . import refio
+        refio.write_param_csv(path, self.p, ic_path, results_path)
+
     def sr_begin(self, template_mode=A.YH_TEMPLATE_CURRENT, template=None):
         t = [None, None, None]
         if template is not None:
