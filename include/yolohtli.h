@@ -199,6 +199,18 @@ typedef struct yh_sym_state {
   int pad_;
 } yh_sym_state;
 
+/* A contour point: the reference's float3 of contour_vector
+ * (spaceAPD.cu:18-153): position (cells) and time. */
+typedef struct yh_contour_pt { float x, y, t; } yh_contour_pt;
+
+/* Per-cell fields of the space-APD tracker (sAPD_kernel, spaceAPD.cu:278):
+ * device arrays of nx*ny; apd1, apd2, back, front and first carry the
+ * tracker's state from call to call (start them at 0). */
+typedef struct yh_apd_fields {
+  float *apd1, *apd2, *sapd, *dapd, *back, *front;
+  uint8_t *first;
+} yh_apd_fields;
+
 /* A stimulus event of a protocol: u = value on tissue cells of the box
  * [i0,i1) x [j0,j1), applied before step `step` is taken. */
 typedef struct yh_stim { int step; int i0, j0, i1, j1; float value; } yh_stim;
@@ -234,12 +246,17 @@ int yh_reaction_diffusion(const yh_param_var *p, int model,
                           yh_fields vel_tan, const uint8_t *solid,
                           void *stream);
 
-/* Spiral-tip detection by the closed-form bilinear isoline intersection
- * (algorithm 1). Resets *tip_count to 0, then appends every tip found between
- * the time levels g_past and g_present (u fields) at time `physical_time`.
- * Replaces tip_wrapper (hostPrototypes.h:26-28, tipTracker.cu:569-611).
- * tip_count and tip_vector are device pointers; at most `capacity` tips are
- * stored, *tip_count keeps the full number found. */
+/* Spiral-tip detection between the time levels g_past and g_present (u
+ * fields) at time `physical_time`: p->tipAlgorithm 1, the closed-form
+ * bilinear isoline intersection (spiralTip_kernel, tipTracker.cu:20-208),
+ * or 2, Newton's method on the same bilinear interpolants in the 2*tipOffset
+ * window around the grid centre (spiralTipNewton_kernel,
+ * tipTracker.cu:244-432); with p->tipGrad each tip carries the gradient of
+ * g_present (gradient, tipTracker.cu:519-566) in vx, vy. Resets *tip_count
+ * to 0, then appends every tip. Replaces tip_wrapper (hostPrototypes.h:26-28,
+ * tipTracker.cu:569-611); tipAlgorithm 3 is yh_filament_mark. tip_count and
+ * tip_vector are device pointers; at most `capacity` tips are stored,
+ * *tip_count keeps the full number found. */
 int yh_spiral_tip(const yh_param_var *p, const float *g_past,
                   const float *g_present, double physical_time,
                   int *tip_count, yh_tip *tip_vector, int capacity,
@@ -407,6 +424,34 @@ int yh_get_step(yh_solver *h, int *step);
 /* Kernel launches this handle has performed so far (graph replays count
  * every kernel node they run). */
 int yh_get_launch_count(yh_solver *h, long long *n);
+
+/* tipAlgorithm 3 (abouzarTip_kernel / abubuFilament,
+ * tipTracker.cu:434-517): marks (sets to 1, never clears) the cells whose
+ * 2x2 corners straddle both u = Uth and u_present = u_past. mark: nx*ny
+ * device bytes. */
+int yh_filament_mark(const yh_param_var *p, const float *past,
+                     const float *present, uint8_t *mark, void *stream);
+
+/* Contour points of field2 (countour_wrapper / countour_kernel,
+ * spaceAPD.cu:18-276): mode 1 its zero level with sub-cell positions (the
+ * space-APD contour), mode 2 the level contourThresh2 where field1 <
+ * contourThresh1, mode 3 the levels 2*contourThresh2 and contourThresh2 -
+ * contourThresh3 in a band around contourThresh2 where field1 <
+ * contourThresh1; stim_area (nx*ny bytes) masks as the reference does.
+ * Resets *count (and plot, when given) first; at most `capacity` points are
+ * stored. All pointers are device pointers. */
+int yh_contour(const yh_param_var *p, const float *field1, const float *field2,
+               const uint8_t *stim_area, int mode, float time, int *count,
+               yh_contour_pt *vec, int capacity, uint8_t *plot, void *stream);
+
+/* One step of the space-APD tracker (sAPD_wrapper / sAPD_kernel,
+ * spaceAPD.cu:278-383) between uold and unew at step `count` (times are
+ * dt * count): upstroke/downstroke times through u = 0.15, two successive
+ * APDs, sapd = sign(APD1 - APD2); with `stimulate` only inside stim_area,
+ * and dapd = APD2 there. */
+int yh_space_apd(const yh_param_var *p, int count, const float *uold,
+                 const float *unew, yh_apd_fields f, const uint8_t *stim_area,
+                 int stimulate, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* Layer 3: batched solver (many independent grids, one launch per step)  */

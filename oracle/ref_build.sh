@@ -33,7 +33,7 @@ __constant__ int lap4_d, timeIntOrder_d;
 paramVar param;
 extern "C" int SOIL_save_screenshot(const char *, int, int, int, int, int) { return 0; }
 STUB
-KERNEL_TUS="reactionDiffusion advFDBFECC symmetryReduction integralTrapz tipTracker helper_functions"
+KERNEL_TUS="reactionDiffusion advFDBFECC symmetryReduction integralTrapz tipTracker helper_functions spaceAPD"
 cubins=""
 for tu in $KERNEL_TUS; do
   nvcc $ARCH -rdc=true -std=c++11 -cubin -w "$REF/$tu.cu" -o "$out/obj/$tu.cubin"

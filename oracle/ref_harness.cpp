@@ -27,6 +27,9 @@ struct alignas(8) Int2 { int x, y; };
 
 CUmodule g_mod = nullptr;
 CUfunction g_rd, g_tip, g_slice, g_trapz, g_cxy, g_bfecc;
+// analysis kernels (tipTracker.cu:244-517, spaceAPD.cu:18-374); null when
+// the cubin predates them
+CUfunction g_newton, g_abouzar, g_contour, g_sapd;
 char g_err[512];
 
 int fail(const char *what, CUresult r) {
@@ -58,6 +61,10 @@ int set_const(const char *name, const T &v) {
 
 int launch(CUfunction f, unsigned gx, unsigned gy, unsigned bx, unsigned by,
            void **args) {
+  if (!f) {
+    snprintf(g_err, sizeof(g_err), "kernel not in the cubin (rebuild oracle/_ref)");
+    return -1;
+  }
   CK(cuLaunchKernel(f, gx, gy, 1, bx, by, 1, 0, nullptr, args, nullptr));
   return 0;
 }
@@ -87,6 +94,18 @@ int refh_open(const char *cubin_path) {
   CK(cuModuleGetFunction(&g_cxy, g_mod, "_Z16Cxy_field_kernel6advVar5REAL3S0_Pb"));
   CK(cuModuleGetFunction(&g_bfecc, g_mod,
                          "_Z17advFDBFECC_kernelm8stateVarS_6advVarS_S_S_Pb"));
+  if (cuModuleGetFunction(&g_newton, g_mod,
+                          "_Z22spiralTipNewton_kernelmPdS_PbPiP7vec5dynd") != CUDA_SUCCESS)
+    g_newton = nullptr;
+  if (cuModuleGetFunction(&g_abouzar, g_mod,
+                          "_Z17abouzarTip_kernelmPdS_PbPiP7vec5dynd") != CUDA_SUCCESS)
+    g_abouzar = nullptr;
+  if (cuModuleGetFunction(&g_contour, g_mod,
+                          "_Z15countour_kernelmPdS_PbS0_PiP6float3fi") != CUDA_SUCCESS)
+    g_contour = nullptr;
+  if (cuModuleGetFunction(&g_sapd, g_mod,
+                          "_Z11sAPD_kernelmiPdS_S_S_S_S_S_S_PbS0_b") != CUDA_SUCCESS)
+    g_sapd = nullptr;
   return 0;
 }
 
@@ -227,6 +246,48 @@ int refh_bfecc(unsigned gx, unsigned gy, unsigned bx, unsigned by,
   bool *sol = reinterpret_cast<bool *>(solid);
   void *args[] = {&pitch, &gout, &gin, &adv, &uf, &ub, &ue, &sol};
   return launch(g_bfecc, gx, gy, bx, by, args);
+}
+
+// spiralTipNewton_kernel (tipTracker.cu:244, tipAlgorithm 2) and
+// abouzarTip_kernel (tipTracker.cu:434, tipAlgorithm 3), the arguments of
+// spiralTip_kernel
+int refh_tip_alg(int alg, unsigned gx, unsigned gy, unsigned bx, unsigned by,
+                 double *g_past, double *g_present, uint8_t *tip_plot,
+                 int *tip_count, void *tip_vector, double ptime) {
+  size_t pitch = 0;
+  bool *plot = reinterpret_cast<bool *>(tip_plot);
+  void *args[] = {&pitch, &g_past, &g_present, &plot, &tip_count, &tip_vector,
+                  &ptime};
+  return launch(alg == 2 ? g_newton : g_abouzar, gx, gy, bx, by, args);
+}
+
+// countour_kernel(pitch, field1, field2, contour_plot, stimArea,
+// contour_count, contour_vector, physicalTime, mode) (spaceAPD.cu:18)
+int refh_contour(unsigned gx, unsigned gy, unsigned bx, unsigned by,
+                 double *field1, double *field2, uint8_t *plot,
+                 uint8_t *stim_area, int *count, void *vec, float ptime,
+                 int mode) {
+  size_t pitch = 0;
+  bool *pl = reinterpret_cast<bool *>(plot);
+  bool *sa = reinterpret_cast<bool *>(stim_area);
+  void *args[] = {&pitch, &field1, &field2, &pl, &sa, &count, &vec, &ptime,
+                  &mode};
+  return launch(g_contour, gx, gy, bx, by, args);
+}
+
+// sAPD_kernel(pitch, count, uold, unew, APD1, APD2, sAPD, dAPD, back, front,
+// first, stimArea, stimulate) (spaceAPD.cu:278)
+int refh_sapd(unsigned gx, unsigned bx, int count, double *uold, double *unew,
+              double *apd1, double *apd2, double *sapd, double *dapd,
+              double *back, double *front, uint8_t *first,
+              uint8_t *stim_area, int stimulate) {
+  size_t pitch = 0;
+  bool *fi = reinterpret_cast<bool *>(first);
+  bool *sa = reinterpret_cast<bool *>(stim_area);
+  bool st = stimulate != 0;
+  void *args[] = {&pitch, &count, &uold, &unew, &apd1, &apd2, &sapd, &dapd,
+                  &back, &front, &fi, &sa, &st};
+  return launch(g_sapd, gx, 1, bx, 1, args);
 }
 
 }  // extern "C"

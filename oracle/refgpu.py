@@ -139,3 +139,29 @@ def tips_to_array(tip_vec_tensor, n):
     """(n, 5) float32 array from a device vec5dyn buffer (int32 view)."""
     raw = tip_vec_tensor[: 5 * n].cpu().numpy()
     return raw.view(np.float32).reshape(n, 5) if raw.dtype != np.float32 else raw.reshape(n, 5)
+
+
+def tip_alg(alg, p, past_u, present_u, tip_plot, tip_count, tip_vec, ptime):
+    """spiralTipNewton_kernel (alg 2) or abouzarTip_kernel (alg 3), the
+    arguments of spiralTip_kernel; zero tip_count first for alg 2."""
+    gx, gy, bx, by = grid2d(p)
+    _ck(lib().refh_tip_alg(int(alg), gx, gy, bx, by, _ptr(past_u),
+                           _ptr(present_u), _ptr(tip_plot), _ptr(tip_count),
+                           _ptr(tip_vec), C.c_double(ptime)))
+
+
+def contour(p, field1, field2, plot, stim_area, count, vec, ptime, mode):
+    """countour_kernel (spaceAPD.cu:18); zero count and plot first."""
+    gx, gy, bx, by = grid2d(p)
+    _ck(lib().refh_contour(gx, gy, bx, by, _ptr(field1), _ptr(field2),
+                           _ptr(plot), _ptr(stim_area), _ptr(count), _ptr(vec),
+                           C.c_float(ptime), int(mode)))
+
+
+def sapd(count, uold, unew, apd1, apd2, sapd_, dapd, back, front, first,
+         stim_area, stimulate):
+    """sAPD_kernel (spaceAPD.cu:278) with GRIDSIZE_1D x BLOCKSIZE_1D."""
+    _ck(lib().refh_sapd(GRID1D, BLOCK1D, int(count), _ptr(uold), _ptr(unew),
+                        _ptr(apd1), _ptr(apd2), _ptr(sapd_), _ptr(dapd),
+                        _ptr(back), _ptr(front), _ptr(first), _ptr(stim_area),
+                        1 if stimulate else 0))

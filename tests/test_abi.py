@@ -35,6 +35,9 @@ REFERENCE_HOST_SYMBOLS = [  # hostPrototypes.h:22-42, as the reference exports t
     "_Z18advFDBFECC_wrapperm4dim3S_8stateVarS0_6advVarS0_S0_S0_Pb",
     "_Z12solve_matrix5REAL3S_Pd",
     "_Z13trapz_wrapper4dim3S_8sliceVarS0_8stateVarPdS2_PiP7vec5dyni",
+    # the contour / space-APD analysis (hostPrototypes.h:46-51)
+    "_Z16countour_wrapperm4dim3S_PdS0_PbS1_PiP6float3fi",
+    "_Z12sAPD_wrapperm4dim3S_iPdS0_S0_S0_S0_S0_S0_S0_PbS1_b",
 ]
 
 

@@ -149,6 +149,17 @@ class Stim(C.Structure):
                 ("i1", C.c_int), ("j1", C.c_int), ("value", C.c_float)]
 
 
+class ContourPt(C.Structure):
+    """yh_contour_pt == the reference's float3 contour point."""
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("t", C.c_float)]
+
+
+class ApdFields(C.Structure):
+    """yh_apd_fields: device pointers of the space-APD tracker."""
+    _fields_ = [(n, C.c_void_p) for n in ("apd1", "apd2", "sapd", "dapd",
+                                           "back", "front", "first")]
+
+
 class BatchStim(C.Structure):
     """yh_batch_stim: a stimulus event of one instance of a batch."""
     _fields_ = [("instance", C.c_int), ("s", Stim)]

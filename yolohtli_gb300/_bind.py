@@ -23,6 +23,11 @@ SIGNATURES = {
                                    A.Fields, A.Fields, _v, _v]),
     "yh_spiral_tip": (_i, [_P(A.ParamVar), _v, _v, _d, _v, _v, _i, _v, _v]),
     "yh_pick_centre": (_i, [_v, _v, _i, _v, _v]),
+    "yh_filament_mark": (_i, [_P(A.ParamVar), _v, _v, _v, _v]),
+    "yh_contour": (_i, [_P(A.ParamVar), _v, _v, _v, _i, _f, _v, _v, _i, _v,
+                        _v]),
+    "yh_space_apd": (_i, [_P(A.ParamVar), _i, _v, _v, A.ApdFields, _v, _i,
+                          _v]),
     "yh_phase_integrals_workspace": (C.c_size_t, [_i, _i]),
     "yh_phase_integrals": (_i, [_P(A.ParamVar), _i, A.Fields, A.Fields,
                                 A.Fields, A.Fields, A.Fields, _v, _v, _v, _v,

@@ -266,6 +266,7 @@ extern "C" int yh_spiral_tip(const yh_param_var *p, const float *g_past,
   if (!p || !g_past || !g_present || !tip_count || !tip_vector || capacity < 0)
     return YH_EINVAL;
   if (p->nx < 5 || p->ny < 5) return YH_EINVAL;
+  if (p->tipAlgorithm != 1 && p->tipAlgorithm != 2) return YH_EUNSUPPORTED;
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(tip_count, 0, sizeof(int), s);
   if (e != cudaSuccess) return cuda_status(e);

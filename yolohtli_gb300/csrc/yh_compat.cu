@@ -226,17 +226,61 @@ void tip_wrapper(size_t pitch, dim3 grid2D, dim3 block2D, stateVar gOut_d,
                  int tipAlgorithm, bool recordTip, bool *tip_plot,
                  int *tip_count, vec5dyn *tip_vector) {
   (void)pitch, (void)grid2D, (void)block2D, (void)velTan, (void)recordTip;
-  (void)tip_plot;
   if (ready()) return;
-  if (tipAlgorithm != 1) {
+  if (tipAlgorithm < 1 || tipAlgorithm > 3) {
     fail(YH_EUNSUPPORTED);
     return;
   }
   cuda_check(cudaMemsetAsync(tip_count, 0, sizeof(int), 0));
-  // spiralTip_kernel(g_past = gIn_d.u, g_present = gOut_d.u) (tipTracker.cu:586-587)
+  uint8_t *plot = reinterpret_cast<uint8_t *>(tip_plot);
+  if (tipAlgorithm == 3) {  // abouzarTip_kernel (tipTracker.cu:601-604)
+    cuda_check(yh::launch_filament<double>(g_p, gIn_d.u, gOut_d.u, plot, 0));
+    return;
+  }
+  // spiralTip_kernel / spiralTipNewton_kernel (g_past = gIn_d.u, g_present =
+  // gOut_d.u) (tipTracker.cu:586-599)
+  yh_param_var q = g_p;
+  q.tipAlgorithm = tipAlgorithm;
   cuda_check(yh::launch_tips<double>(
-      g_p, gIn_d.u, gOut_d.u, g_p.solidSwitch, physicalTime, tip_count,
-      reinterpret_cast<yh_tip *>(tip_vector), kTipVecSize, nullptr, nullptr, 0));
+      q, gIn_d.u, gOut_d.u, g_p.solidSwitch, physicalTime, tip_count,
+      reinterpret_cast<yh_tip *>(tip_vector), kTipVecSize, nullptr, nullptr, 0,
+      plot));
+}
+
+// countour_wrapper (spaceAPD.cu:257-276): count and plot reset, then
+// countour_kernel; the reference's contour_vector holds nx*ny points.
+void countour_wrapper(size_t pitch, dim3 grid2D, dim3 block2D, REAL *field1,
+                      REAL *field2, bool *contour_plot, bool *stimArea,
+                      int *contour_count, float3 *contour_vector,
+                      float physicalTime, int mode) {
+  (void)pitch, (void)grid2D, (void)block2D;
+  if (ready()) return;
+  if (mode < 1 || mode > 3) {
+    fail(YH_EINVAL);
+    return;
+  }
+  static_assert(sizeof(float3) == sizeof(yh_contour_pt), "float3 layout");
+  cuda_check(cudaMemsetAsync(contour_count, 0, sizeof(int), 0));
+  cuda_check(cudaMemsetAsync(contour_plot, 0, (size_t)g_p.nx * g_p.ny, 0));
+  cuda_check(yh::launch_contour<double>(
+      g_p, field1, field2, reinterpret_cast<const uint8_t *>(stimArea), mode,
+      physicalTime, contour_count,
+      reinterpret_cast<yh_contour_pt *>(contour_vector), g_p.nx * g_p.ny,
+      reinterpret_cast<uint8_t *>(contour_plot), 0));
+}
+
+// sAPD_wrapper (spaceAPD.cu:376-383)
+void sAPD_wrapper(size_t pitch, dim3 grid1D, dim3 block1D, int count,
+                  REAL *uold, REAL *unew, REAL *APD1, REAL *APD2, REAL *sAPD,
+                  REAL *dAPD, REAL *back, REAL *front, bool *first,
+                  bool *stimArea, bool stimulate) {
+  (void)pitch, (void)grid1D, (void)block1D;
+  if (ready()) return;
+  yh::ApdFields<double> f{APD1, APD2, sAPD, dAPD, back, front,
+                          reinterpret_cast<uint8_t *>(first)};
+  cuda_check(yh::launch_space_apd<double>(
+      g_p, count, uold, unew, f, reinterpret_cast<const uint8_t *>(stimArea),
+      stimulate, 0));
 }
 
 void slice_wrapper(size_t pitch, dim3 grid2D, dim3 block2D, stateVar g,

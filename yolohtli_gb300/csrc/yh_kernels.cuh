@@ -67,12 +67,37 @@ cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
 // yh_sr.cu
 // holes: the hole-domain branch of the reference (a disc around the grid
 // centre, tipTracker.cu:47-122); it does not read the mask itself.
+// p.tipAlgorithm (1 closed form, 2 Newton) and p.tipGrad select the kernel;
+// plot (may be null) gets the cells of the tips marked.
 template <typename Real>
 cudaError_t launch_tips(const yh_param_var &p, const Real *past,
                         const Real *present, bool holes, double ptime,
                         int *count, yh_tip *vec, int cap,
                         yh_sym_state *sym_pick, unsigned int *done,
-                        cudaStream_t s);
+                        cudaStream_t s, uint8_t *plot = nullptr);
+
+// yh_analysis.cu: tipAlgorithm 3 (filament cells), contours, space APD
+template <typename Real>
+cudaError_t launch_filament(const yh_param_var &p, const Real *past,
+                            const Real *present, uint8_t *mark,
+                            cudaStream_t s);
+template <typename Real>
+cudaError_t launch_contour(const yh_param_var &p, const Real *field1,
+                           const Real *field2, const uint8_t *stim_area,
+                           int mode, float time, int *count,
+                           yh_contour_pt *vec, int cap, uint8_t *plot,
+                           cudaStream_t s);
+template <typename Real>
+struct ApdFields {
+  Real *apd1, *apd2, *sapd, *dapd, *back, *front;
+  uint8_t *first;
+};
+template <typename Real>
+cudaError_t launch_space_apd(const yh_param_var &p, int count,
+                             const Real *uold, const Real *unew,
+                             const ApdFields<Real> &f,
+                             const uint8_t *stim_area, bool stimulate,
+                             cudaStream_t s);
 cudaError_t launch_pick_centre(const int *count, const yh_tip *vec, int cap,
                                yh_sym_state *sym, cudaStream_t s);
 

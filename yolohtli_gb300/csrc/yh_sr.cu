@@ -26,37 +26,99 @@ namespace yh {
 
 struct TipArgs {
   int nx, ny, r2;
+  int tox, toy;  // tipOffsetX/Y: the Newton search window
   double Uth;
+  double invdx, invdy;  // 1/(2 hx), 1/(2 hy): the tip gradient
   double dt;     // with sym: time = dt * sym->step (graph-stable)
   double ptime;  // without sym: the time stamp of the tips
 };
 
-__device__ __forceinline__ void tip_record(int i, int j, float s, float t,
-                                           float ptime, int *count,
-                                           yh_tip *vec, int cap) {
-  // tipRecordPlane (tipTracker.cu:215-236)
+// Index (i, j) clamped into the grid: the gradient stencil below reaches
+// i-1 at i = 0 and j+2 near the top, where the reference reads outside its
+// arrays; inside the grid the indices are the reference's.
+__device__ __forceinline__ int gidx(int nx, int ny, int i, int j) {
+  i = i < 0 ? 0 : (i >= nx ? nx - 1 : i);
+  j = j < 0 ? 0 : (j >= ny ? ny - 1 : j);
+  return i + nx * j;
+}
+
+// Gradient of g at the tip (i + s, j + t): central differences at the four
+// corners of the cell, blended bilinearly, with the reference's choice of
+// stencil at the grid edges (gradient, tipTracker.cu:519-566).
+template <typename Real>
+__device__ float2 tip_gradient(const TipArgs &a, int i, int j, double s,
+                               double t, const Real *__restrict__ g) {
+  const int nx = a.nx, ny = a.ny;
+  auto at = [&](int x, int y) { return (double)g[gidx(nx, ny, x, y)]; };
+  const bool xl = i < nx - 1, xl2 = i < nx - 2, yl = j < ny - 1, yl2 = j < ny - 2;
+  const double S = j > 0 ? at(i, j - 1) : at(i, j + 1);
+  const double Sx = (j > 0 && xl) ? at(i + 1, j - 1) : at(i - 1, j + 1);
+  const double Sy = at(i, j);
+  const double Sxy = xl ? at(i + 1, j) : at(i - 1, j);
+  const double N = yl ? at(i, j + 1) : at(i, j - 1);
+  const double Nx = (xl && yl) ? at(i + 1, j + 1) : at(i - 1, j - 1);
+  const double Ny = yl2 ? at(i, j + 2) : (j == ny - 2 ? at(i, j) : at(i, j - 1));
+  const double Nxy = (xl && yl2) ? at(i + 1, j + 2)
+                                 : (j == ny - 2 ? at(i - 1, j) : at(i - 1, j - 1));
+  const double W = at(i - 1, j);
+  const double Wx = at(i, j);
+  const double Wy = (i > 0 && yl) ? at(i - 1, j + 1) : at(i + 1, j - 1);
+  const double Wxy = yl ? at(i, j + 1) : at(i - 1, j);
+  const double E = xl ? at(i + 1, j) : at(i - 1, j);
+  const double Ex = xl2 ? at(i + 2, j) : (i == nx - 2 ? at(i, j) : at(i - 1, j));
+  const double Ey = (xl && yl) ? at(i + 1, j + 1) : at(i - 1, j - 1);
+  const double Exy = (xl2 && yl) ? at(i + 2, j + 1)
+                                 : (i == nx - 2 ? at(i, j - 1) : at(i - 1, j - 1));
+  const double gx1 = (E - W) * a.invdx, gy1 = (N - S) * a.invdy;
+  const double gx2 = (Ex - Wx) * a.invdx, gy2 = (Nx - Sx) * a.invdy;
+  const double gx3 = (Ey - Wy) * a.invdx, gy3 = (Ny - Sy) * a.invdy;
+  const double gx4 = (Exy - Wxy) * a.invdx, gy4 = (Nxy - Sxy) * a.invdy;
+  float2 r;
+  r.x = (float)((1.0 - s) * (1.0 - t) * gx1 + s * (1.0 - t) * gx2 +
+                t * (1.0 - s) * gx3 + s * t * gx4);
+  r.y = (float)((1.0 - s) * (1.0 - t) * gy1 + s * (1.0 - t) * gy2 +
+                t * (1.0 - s) * gy3 + s * t * gy4);
+  return r;
+}
+
+// tipRecordPlane (tipTracker.cu:210-241): a tip strictly inside the cell is
+// pushed (with the gradient of the present field when GRAD) and, with a
+// plot array, its cell marked.
+template <bool GRAD, typename Real>
+__device__ __forceinline__ void tip_record(const TipArgs &a, int i, int j,
+                                           float s, float t, float ptime,
+                                           const Real *present, int *count,
+                                           yh_tip *vec, int cap,
+                                           uint8_t *plot) {
   if ((s > 0.0f && s < 1.0f) && (t > 0.0f && t < 1.0f)) {
+    float2 g = make_float2(0.0f, 0.0f);
+    if (GRAD) g = tip_gradient(a, i, j, (double)s, (double)t, present);
+    yh_tip d;
+    d.x = (float)i + s;
+    d.y = (float)j + t;
+    d.vx = g.x;
+    d.vy = g.y;
+    d.t = ptime;
     const int slot = atomicAdd(count, 1);
-    if (slot < cap) {
-      yh_tip d;
-      d.x = (float)i + s;
-      d.y = (float)j + t;
-      d.vx = 0.0f;
-      d.vy = 0.0f;
-      d.t = ptime;
-      vec[slot] = d;
+    if (slot < cap) vec[slot] = d;
+    if (plot) {  // plot_field's linear index, marks outside the array dropped
+      const long long k = (long long)floorf(d.x) + (long long)a.nx * (long long)floorf(d.y);
+      if (k >= 0 && k < (long long)a.nx * a.ny) plot[k] = 1;
     }
   }
 }
 
 // Candidate tips of one cell; x = present corners, y = past corners in the
 // order (i,j), (i+1,j), (i+1,j+1), (i,j+1) (tipTracker.cu:140-174), in FP64.
-__device__ __forceinline__ void tip_cell(double Uth, int i, int j, double x1,
-                                         double x2, double x3, double x4,
-                                         double y1, double y2, double y3,
-                                         double y4, bool need_disc,
-                                         float ptime, int *count, yh_tip *vec,
-                                         int cap) {
+template <bool GRAD, typename Real>
+__device__ __forceinline__ void tip_cell(const TipArgs &a, int i, int j,
+                                         double x1, double x2, double x3,
+                                         double x4, double y1, double y2,
+                                         double y3, double y4, bool need_disc,
+                                         float ptime, const Real *present,
+                                         int *count, yh_tip *vec, int cap,
+                                         uint8_t *plot) {
+  const double Uth = a.Uth;
   const double x3y1 = x3 * y1, x4y1 = x4 * y1, x3y2 = x3 * y2, x4y2 = x4 * y2;
   const double x1y3 = x1 * y3, x2y3 = x2 * y3, x1y4 = x1 * y4, x2y4 = x2 * y4;
   const double x2y1 = x2 * y1, x1y2 = x1 * y2, x4y3 = x4 * y3, x3y4 = x3 * y4;
@@ -74,10 +136,59 @@ __device__ __forceinline__ void tip_cell(double Uth, int i, int j, double x1,
   const double py =
       Uth * ctn1 - x3y1 + x4y2 + x1y3 - x2y4 + 2.0 * (x2y1 - x1y2);
   if (need_disc && !(disc >= 0.0)) return;
-  tip_record(i, j, (float)((px + disc) / den1), (float)((py + disc) / den2),
-             ptime, count, vec, cap);
-  tip_record(i, j, (float)((px - disc) / den1), (float)((py - disc) / den2),
-             ptime, count, vec, cap);
+  tip_record<GRAD>(a, i, j, (float)((px + disc) / den1),
+                   (float)((py + disc) / den2), ptime, present, count, vec,
+                   cap, plot);
+  tip_record<GRAD>(a, i, j, (float)((px - disc) / den1),
+                   (float)((py - disc) / den2), ptime, present, count, vec,
+                   cap, plot);
+}
+
+__device__ __forceinline__ bool near(double x, double y, double tol) {
+  return x == y || (x <= y + tol && x >= y - tol);  // equals (helper_functions.cu:58-62)
+}
+
+// Newton's method for the crossing of the two bilinear isolines x = Uth and
+// y = Uth in one cell (spiralTipNewton_kernel, tipTracker.cu:287-333): four
+// iterations from the cell centre, clamped to the cell, accepted when both
+// interpolants hit Uth to 1e-15; the reference's expressions in FP64.
+template <bool GRAD, typename Real>
+__device__ __forceinline__ void tip_cell_newton(
+    const TipArgs &a, int i, int j, double px1, double px2, double px3,
+    double px4, double py1, double py2, double py3, double py4, float ptime,
+    const Real *present, int *count, yh_tip *vec, int cap, uint8_t *plot) {
+  const double Uth = a.Uth;
+  double s = 0.5, t = 0.5;
+  for (int k = 0; k < 4; ++k) {
+    const double r1 = px1 * (1.0 - s) * (1.0 - t) + px2 * s * (1.0 - t) +
+                      px3 * s * t + px4 * (1.0 - s) * t - Uth;
+    const double r2 = py1 * (1.0 - s) * (1.0 - t) + py2 * s * (1.0 - t) +
+                      py3 * s * t + py4 * (1.0 - s) * t - Uth;
+    const double J11 = -px1 * (1.0 - t) + px2 * (1.0 - t) + px3 * t - px4 * t;
+    const double J21 = -py1 * (1.0 - t) + py2 * (1.0 - t) + py3 * t - py4 * t;
+    const double J12 = -px1 * (1.0 - s) - px2 * s + px3 * s + px4 * (1.0 - s);
+    const double J22 = -py1 * (1.0 - s) - py2 * s + py3 * s + py4 * (1.0 - s);
+    const double detJ = J11 * J22 - J12 * J21;
+    if (!near(detJ, 0.0, 1e-14)) {
+      s -= (J22 * r1 - J12 * r2) / detJ;
+      t -= (-J21 * r1 + J11 * r2) / detJ;
+      s = fmin(fmax(s, 0.0), 1.0);
+      t = fmin(fmax(t, 0.0), 1.0);
+    } else {
+      s = -1.0;
+      t = -1.0;
+    }
+  }
+  const bool in = (s >= 0.0) && (s <= 1.0) && (t >= 0.0) && (t <= 1.0);
+  const double u1 = in ? px1 * (1 - s) * (1.0 - t) + px2 * s * (1.0 - t) +
+                             px3 * s * t + px4 * (1.0 - s) * t
+                       : 0.0;
+  const double u2 = in ? py1 * (1 - s) * (1.0 - t) + py2 * s * (1.0 - t) +
+                             py3 * s * t + py4 * (1.0 - s) * t
+                       : 0.0;
+  if (near(u1, Uth, 1e-15) && near(u2, Uth, 1e-15))
+    tip_record<GRAD>(a, i, j, (float)s, (float)t, ptime, present, count, vec,
+                     cap, plot);
 }
 
 // Block-wide argmin (256 threads, linear id t) of the tip nearest to the
@@ -132,17 +243,18 @@ __device__ void pick_centre_block(int t, const int *count, const yh_tip *vec,
   }
 }
 
-// HOLES: the disc around the grid centre, all cells, no disc>=0 test
-// (tipTracker.cu:47-122); otherwise i in [1,nx-3], j in [1,ny-3]
-// (tipTracker.cu:124-204). For FP32 fields a cell is skipped early when the
-// threshold lies outside the corner range of either level: a bilinear
-// interpolant on the unit cell stays within its corner values, so no root
-// of x = Uth, y = Uth can lie inside such a cell.
-template <typename Real, bool HOLES>
+// HOLES: the disc around the grid centre, all cells (tipTracker.cu:47-122,
+// :262-266); otherwise, closed form (ALG 1): i in [1,nx-3], j in [1,ny-3]
+// (tipTracker.cu:124-204), Newton (ALG 2): the 2 tipOffset window around
+// the grid centre (tipTracker.cu:339-341). For FP32 fields the closed form
+// skips a cell early when the threshold lies outside the corner range of
+// either level: a bilinear interpolant on the unit cell stays within its
+// corner values, so no root of x = Uth, y = Uth can lie inside such a cell.
+template <typename Real, bool HOLES, int ALG, bool GRAD>
 __global__ void __launch_bounds__(256)
     tip_kernel(const TipArgs a, const Real *__restrict__ past,
                const Real *__restrict__ present, int *count, yh_tip *vec,
-               int cap, yh_sym_state *sym, unsigned int *done) {
+               int cap, yh_sym_state *sym, unsigned int *done, uint8_t *plot) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = a.nx, ny = a.ny;
@@ -152,8 +264,11 @@ __global__ void __launch_bounds__(256)
   if (HOLES) {
     const int ic = i - nx / 2, jc = j - ny / 2;
     active = i < nx && j < ny && (ic * ic + jc * jc) < a.r2;
-  } else {
+  } else if (ALG == 1) {
     active = (i >= 1) && (i < nx - 2) && (j >= 1) && (j < ny - 2);
+  } else {
+    active = i < nx && j < ny && i >= nx / 2 - a.tox && i < nx / 2 + a.tox &&
+             j >= ny / 2 - a.toy && j < ny / 2 + a.toy;
   }
   if (active) {
     const int s0 = i + nx * j;
@@ -163,19 +278,24 @@ __global__ void __launch_bounds__(256)
     const Real x1 = present[s0], x2 = present[sx], x4 = present[sy],
                x3 = present[sxy];
     const Real y1 = past[s0], y2 = past[sx], y4 = past[sy], y3 = past[sxy];
-    bool cand = true;
-    if (sizeof(Real) == 4) {
-      const float th = (float)a.Uth, tol = 1e-5f;
-      const float xmn = fminf(fminf(x1, x2), fminf(x3, x4));
-      const float xmx = fmaxf(fmaxf(x1, x2), fmaxf(x3, x4));
-      const float ymn = fminf(fminf(y1, y2), fminf(y3, y4));
-      const float ymx = fmaxf(fmaxf(y1, y2), fmaxf(y3, y4));
-      cand = th >= xmn - tol && th <= xmx + tol && th >= ymn - tol &&
-             th <= ymx + tol;
+    if (ALG == 2) {
+      tip_cell_newton<GRAD>(a, i, j, x1, x2, x3, x4, y1, y2, y3, y4, ptime,
+                            present, count, vec, cap, plot);
+    } else {
+      bool cand = true;
+      if (sizeof(Real) == 4) {
+        const float th = (float)a.Uth, tol = 1e-5f;
+        const float xmn = fminf(fminf(x1, x2), fminf(x3, x4));
+        const float xmx = fmaxf(fmaxf(x1, x2), fmaxf(x3, x4));
+        const float ymn = fminf(fminf(y1, y2), fminf(y3, y4));
+        const float ymx = fmaxf(fmaxf(y1, y2), fmaxf(y3, y4));
+        cand = th >= xmn - tol && th <= xmx + tol && th >= ymn - tol &&
+               th <= ymx + tol;
+      }
+      if (cand)
+        tip_cell<GRAD>(a, i, j, x1, x2, x3, x4, y1, y2, y3, y4, !HOLES, ptime,
+                       present, count, vec, cap, plot);
     }
-    if (cand)
-      tip_cell(a.Uth, i, j, x1, x2, x3, x4, y1, y2, y3, y4, !HOLES, ptime,
-               count, vec, cap);
   }
   if (sym == nullptr) return;
   // Last block to finish chooses the disc centre.
@@ -201,29 +321,46 @@ __global__ void pick_centre_kernel(const int *count, const yh_tip *vec,
 
 // With sym_pick != nullptr the tips are stamped dt*sym->step (so a captured
 // graph stays valid as steps advance) and the last block picks the centre;
-// otherwise they are stamped `ptime`. `done` is a zeroed counter.
+// otherwise they are stamped `ptime`. `done` is a zeroed counter. The
+// algorithm (p.tipAlgorithm 1 closed form, 2 Newton) and the gradient
+// (p.tipGrad) follow p; plot (may be null) gets the tips' cells marked.
 template <typename Real>
 cudaError_t launch_tips(const yh_param_var &p, const Real *past,
                         const Real *present, bool holes, double ptime,
                         int *count, yh_tip *vec, int cap,
                         yh_sym_state *sym_pick, unsigned int *done,
-                        cudaStream_t s) {
+                        cudaStream_t s, uint8_t *plot) {
+  if (p.tipAlgorithm != 1 && p.tipAlgorithm != 2) return cudaErrorNotSupported;
   TipArgs a;
   a.nx = p.nx;
   a.ny = p.ny;
   a.r2 = p.tipOffsetX * p.tipOffsetY;
+  a.tox = p.tipOffsetX;
+  a.toy = p.tipOffsetY;
   a.Uth = p.Uth;
+  a.invdx = p.invdx;
+  a.invdy = p.invdy;
   a.dt = p.dt;
   a.ptime = ptime;
   const dim3 block(32, 8);
   const dim3 grid((p.nx + 31) / 32, (p.ny + 7) / 8);
-  if (holes)
-    tip_kernel<Real, true><<<grid, block, 0, s>>>(a, past, present, count,
-                                                  vec, cap, sym_pick, done);
-  else
-    tip_kernel<Real, false><<<grid, block, 0, s>>>(a, past, present, count,
-                                                   vec, cap, sym_pick, done);
-  return cudaGetLastError();
+  const bool newton = p.tipAlgorithm == 2, grad = p.tipGrad;
+#define YH_TIP(H, ALG, G)                                                   \
+  if (holes == H && newton == (ALG == 2) && grad == G) {                    \
+    tip_kernel<Real, H, ALG, G><<<grid, block, 0, s>>>(                     \
+        a, past, present, count, vec, cap, sym_pick, done, plot);           \
+    return cudaGetLastError();                                             \
+  }
+  YH_TIP(true, 1, false)
+  YH_TIP(true, 1, true)
+  YH_TIP(true, 2, false)
+  YH_TIP(true, 2, true)
+  YH_TIP(false, 1, false)
+  YH_TIP(false, 1, true)
+  YH_TIP(false, 2, false)
+  YH_TIP(false, 2, true)
+#undef YH_TIP
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_pick_centre(const int *count, const yh_tip *vec, int cap,
@@ -736,7 +873,8 @@ cudaError_t launch_bfecc_2d(const yh_param_var &p, int nf,
 #define YH_INST(Real)                                                         \
   template cudaError_t launch_tips<Real>(                                     \
       const yh_param_var &, const Real *, const Real *, bool, double, int *,  \
-      yh_tip *, int, yh_sym_state *, unsigned int *, cudaStream_t);           \
+      yh_tip *, int, yh_sym_state *, unsigned int *, cudaStream_t,            \
+      uint8_t *);                                                            \
   template cudaError_t launch_phase<Real>(                                    \
       const yh_param_var &, int, const Fld<Real> &, const Fld<Real> &,        \
       const Fld<Real> &, const Fld<Real> &, const Fld<Real> &,                \

@@ -61,6 +61,32 @@ def spiral_tip(p, past_u, present_u, tip_count, tip_vec, capacity,
         _p(tip_count), _p(tip_vec), capacity, _p(solid), _stream()))
 
 
+def filament_mark(p, past_u, present_u, mark):
+    """tipAlgorithm 3: sets mark (uint8, nx*ny) on the filament cells."""
+    return check("yh_filament_mark", load().yh_filament_mark(
+        C.byref(p), _p(past_u), _p(present_u), _p(mark), _stream()))
+
+
+def contour(p, field1, field2, stim_area, mode, time, count, vec, capacity,
+            plot=None):
+    """Contour points (modes 1-3) into vec (float32[3*capacity])."""
+    return check("yh_contour", load().yh_contour(
+        C.byref(p), _p(field1), _p(field2), _p(stim_area), int(mode),
+        C.c_float(time), _p(count), _p(vec), int(capacity), _p(plot),
+        _stream()))
+
+
+def space_apd(p, count, uold, unew, apd, stim_area=None, stimulate=False):
+    """One step of the space-APD tracker; apd: dict of device tensors
+    apd1, apd2, sapd, dapd, back, front (float32) and first (uint8)."""
+    f = A.ApdFields(*[_p(apd[k]) if apd.get(k) is not None else None
+                      for k in ("apd1", "apd2", "sapd", "dapd", "back",
+                                "front", "first")])
+    return check("yh_space_apd", load().yh_space_apd(
+        C.byref(p), int(count), _p(uold), _p(unew), f, _p(stim_area),
+        1 if stimulate else 0, _stream()))
+
+
 def pick_centre(tip_count, tip_vec, capacity, sym):
     lib = load()
     return check("yh_pick_centre", lib.yh_pick_centre(
