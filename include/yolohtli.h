@@ -501,6 +501,41 @@ int yh_batch_get_step(yh_batch *b, int *step);
 int yh_batch_get_launch_count(yh_batch *b, long long *n);
 
 /* ------------------------------------------------------------------ */
+/* Layer 5: adjoint (gradient of a probe loss with respect to D(x, y))   */
+/* ------------------------------------------------------------------ */
+/* No reference counterpart (the reference has constant D and no
+ * gradients). FK3V with a per-cell diffusion coefficient D (nx*ny floats,
+ * cm^2/ms): du_i = dt/h^2 sum over the 4 faces of (D_i + D_m)/2 (u_m - u_i),
+ * m the mirrored neighbour (no-flux edges as the reference's mirror
+ * ghosts), then the FK3V Euler update in exact arithmetic. The loss sums
+ * (u - target)^2 over a lattice of probes (every probe_spacing cells, at
+ * the cell centres of the lattice squares) on the states after every
+ * frame_steps steps. One run takes nsteps forward steps keeping a
+ * checkpoint every checkpoint_steps, then recomputes each segment and
+ * sweeps it backwards: memory is the checkpoints plus one segment. fp64
+ * runs the same in FP64 (for gradient checks). hx must equal hy. */
+typedef struct yh_adjoint yh_adjoint;
+int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
+                      int nsteps, int frame_steps, int probe_spacing,
+                      int checkpoint_steps, int fp64, void *stream,
+                      yh_adjoint **out);
+int yh_adjoint_destroy(yh_adjoint *h);
+/* Frames (nsteps / frame_steps) and probes (nx / spacing, ny / spacing). */
+int yh_adjoint_probes(yh_adjoint *h, int *frames, int *probes_x,
+                      int *probes_y);
+/* target: frames x probes_y x probes_x floats, host or device. */
+int yh_adjoint_set_target(yh_adjoint *h, const float *target);
+/* A forward run from (u0, v0, w0) with D that writes the probe values of
+ * every frame (the shape of a target) to `probes` (device). */
+int yh_adjoint_record(yh_adjoint *h, const float *D, const float *u0,
+                      const float *v0, const float *w0, float *probes);
+/* Loss (host) and, when grad_D is not NULL, dLoss/dD (device, nx*ny) from
+ * the initial state (u0, v0, w0) and D, all device arrays. */
+int yh_adjoint_run(yh_adjoint *h, const float *D, const float *u0,
+                   const float *v0, const float *w0, double *loss,
+                   float *grad_D);
+
+/* ------------------------------------------------------------------ */
 /* Layer 4: the reference's interchange files                           */
 /* ------------------------------------------------------------------ */
 /* Line for line the files the reference writes for its MATLAB

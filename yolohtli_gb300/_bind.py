@@ -75,6 +75,14 @@ SIGNATURES = {
     "yh_batch_set_schedule": (_i, [_v, C.c_longlong, _i]),
     "yh_batch_get_step": (_i, [_v, _P(_i)]),
     "yh_batch_get_launch_count": (_i, [_v, _P(C.c_longlong)]),
+    # adjoint
+    "yh_adjoint_create": (_i, [_P(A.ParamVar), _P(A.FKParams), _i, _i, _i, _i,
+                               _i, _v, _P(_v)]),
+    "yh_adjoint_destroy": (_i, [_v]),
+    "yh_adjoint_probes": (_i, [_v, _P(_i), _P(_i), _P(_i)]),
+    "yh_adjoint_set_target": (_i, [_v, _v]),
+    "yh_adjoint_record": (_i, [_v, _v, _v, _v, _v, _v]),
+    "yh_adjoint_run": (_i, [_v, _v, _v, _v, _v, _P(_d), _v]),
     # the reference's interchange files
     "yh_write_param_csv": (_i, [C.c_char_p, _P(A.ParamVar), C.c_char_p,
                                 C.c_char_p]),

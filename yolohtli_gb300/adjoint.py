@@ -1,0 +1,106 @@
+"""Gradients of a probe loss with respect to the diffusion map D(x, y)
+(yh_adjoint_* in include/yolohtli.h), and a torch.autograd.Function over
+them: `loss = ProbeLoss.apply(D, problem)` then `loss.backward()` fills
+D.grad with the adjoint's dLoss/dD."""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+from ._loader import load
+from .ops import check
+
+
+class Adjoint:
+    """One FK3V problem: grid and parameters p (hx == hy), the FK3V
+    parameters, nsteps steps, the loss on the states after every
+    frame_steps steps at a probe lattice every probe_spacing cells,
+    checkpoints every checkpoint_steps (default ~sqrt(nsteps))."""
+
+    def __init__(self, p, fk, nsteps, frame_steps, probe_spacing,
+                 checkpoint_steps=None, fp64=False, stream=None):
+        self.lib = load()
+        self.p = p.copy()
+        if checkpoint_steps is None:
+            checkpoint_steps = max(1, int(round(np.sqrt(nsteps))))
+        h = C.c_void_p()
+        check("yh_adjoint_create", self.lib.yh_adjoint_create(
+            C.byref(self.p), C.byref(fk), int(nsteps), int(frame_steps),
+            int(probe_spacing), int(checkpoint_steps), 1 if fp64 else 0,
+            C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.h = h
+        f, px, py = C.c_int(), C.c_int(), C.c_int()
+        check("yh_adjoint_probes", self.lib.yh_adjoint_probes(
+            h, C.byref(f), C.byref(px), C.byref(py)))
+        self.frames, self.probes_x, self.probes_y = f.value, px.value, py.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.yh_adjoint_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def target_shape(self):
+        return (self.frames, self.probes_y, self.probes_x)
+
+    def set_target(self, target):
+        """target: a device tensor or host array of target_shape floats."""
+        ptr = target.data_ptr() if hasattr(target, "data_ptr") else \
+            np.ascontiguousarray(target, dtype=np.float32).ctypes.data
+        check("yh_adjoint_set_target", self.lib.yh_adjoint_set_target(self.h, ptr))
+
+    def record(self, D, state0, out):
+        """Probe values of a forward run into `out` (device float32)."""
+        check("yh_adjoint_record", self.lib.yh_adjoint_record(
+            self.h, D.data_ptr(), *[x.data_ptr() for x in state0],
+            out.data_ptr()))
+
+    def run(self, D, state0, grad=None):
+        """Loss (float) and, with `grad` (device float32 like D), dLoss/dD."""
+        loss = C.c_double()
+        check("yh_adjoint_run", self.lib.yh_adjoint_run(
+            self.h, D.data_ptr(), *[x.data_ptr() for x in state0],
+            C.byref(loss), grad.data_ptr() if grad is not None else None))
+        return loss.value
+
+
+def _make_function():
+    import torch
+
+    class ProbeLoss(torch.autograd.Function):
+        """loss = ProbeLoss.apply(D, adjoint, state0): D a float32 CUDA
+        tensor of nx*ny, state0 (u0, v0, w0) float32 CUDA tensors."""
+
+        @staticmethod
+        def forward(ctx, D, adjoint, state0):
+            D = D.contiguous()
+            state0 = [x.contiguous() for x in state0]
+            torch.cuda.synchronize()
+            grad = torch.empty_like(D)
+            loss = adjoint.run(D, state0, grad)
+            ctx.save_for_backward(grad)
+            return torch.tensor(loss, dtype=torch.float64, device=D.device)
+
+        @staticmethod
+        def backward(ctx, g):
+            (grad,) = ctx.saved_tensors
+            return (g.to(grad.dtype) * grad, None, None)
+
+    return ProbeLoss
+
+
+_fn = None
+
+
+def probe_loss(D, adjoint, state0):
+    """The probe loss as a differentiable function of D."""
+    global _fn
+    if _fn is None:
+        _fn = _make_function()
+    return _fn.apply(D, adjoint, state0)

@@ -15,7 +15,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
-SOURCES = ["yh_rd.cu", "yh_rd_2s.cu", "yh_rd_tb.cu", "yh_io.cu", "yh_analysis.cu", "yh_rd_resident.cu", "yh_sr.cu", "yh_api.cu", "yh_noalloc.cu", "yh_batch.cu",
+SOURCES = ["yh_rd.cu", "yh_rd_2s.cu", "yh_rd_tb.cu", "yh_io.cu", "yh_analysis.cu", "yh_rd_resident.cu", "yh_sr.cu", "yh_api.cu", "yh_noalloc.cu", "yh_batch.cu", "yh_adjoint.cu",
            "yh_solver.cu", "yh_compat.cu"]
 
 

@@ -1,0 +1,582 @@
+// Adjoint of the FK3V explicit solver with a per-cell diffusion map
+// (include/yolohtli.h, layer 5): the gradient of a probe loss with respect
+// to D(x, y), for parameter estimation. No reference counterpart (the
+// reference has constant D and no gradients).
+//
+// Forward step (finite-volume form of div(D grad u), no-flux edges by the
+// reference's mirror ghosts, helper_functions.cu:69-79):
+//   r_i = dt D_i / h^2,  k_f = (r_i + r_m(f)) / 2 for face f of cell i
+//   towards its (mirrored) neighbour m(f),
+//   du_i = sum_f k_f (u_m(f) - u_i),
+// then the FK3V update with du (Fenton & Karma 1998, tc-scaled Euler):
+//   u' = u + tc du - dt tc J(u, v, w),  v' = v + dt tc g_v,  w' = w + dt tc g_w
+// in exact arithmetic (exp2 and division, no approximate MUFU forms), so the
+// reverse step differentiates exactly what the forward step computes.
+//
+// Loss: L = sum over frames f (the states after every `frame` steps) of
+// sum over probes p (cells (px*sp + sp/2, py*sp + sp/2)) of
+// (u_f,p - target_f,p)^2.
+//
+// Reverse step n (gather form, one kernel per step): from lambda^{n+1} and
+// the state x^n it forms lambda^n = (dF/dx^n)^T lambda^{n+1} + dL/dx^n and
+// adds (dF/dr)^T lambda^{n+1} to the gradient with respect to r. The
+// forward states of a segment are recomputed from a checkpoint (every
+// `ck` steps) before the segment's reverse sweep: memory is the
+// checkpoints plus one segment of states. The whole sequence (~3 nsteps
+// launches and the checkpoint copies) is captured once per handle as a
+// CUDA graph and replayed.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <utility>
+
+#include "yh_kernels.cuh"
+
+namespace yh {
+template <typename Real>
+StepCoeffs<Real> make_step_coeffs(const yh_param_var &p, int model,
+                                  const yh_fk_params *fk);
+int check_params(const yh_param_var *p, int model, const yh_fk_params *fk);
+}  // namespace yh
+
+using namespace yh;
+
+namespace {
+
+template <typename Real>
+struct AdjCoeffs {
+  int nx, ny;
+  Real tc, dt;
+  Real u_c, u_v, u_csi, k2;  // k2: -2k log2(e) of the sigmoid's 2^(k2 (u - u_csi))
+  Real s_td, s_tr, s_to, s_tsi, s_tvp, s_tv1m, s_tv2m, s_twp, s_twm;
+};
+
+template <typename Real>
+__device__ __forceinline__ Real ex2(Real x);
+template <>
+__device__ __forceinline__ float ex2<float>(float x) { return exp2f(x); }
+template <>
+__device__ __forceinline__ double ex2<double>(double x) { return exp2(x); }
+
+// The pointwise FK3V update and its partial derivatives.
+template <typename Real>
+struct FkLocal {
+  Real un, vn, wn;
+  Real dun_du, dun_dv, dun_dw;  // of un (du held fixed)
+  Real dvn_dv, dwn_dw;
+};
+
+template <typename Real>
+__device__ __forceinline__ FkLocal<Real> fk_local(const AdjCoeffs<Real> &a,
+                                                  Real u, Real v, Real w,
+                                                  Real du) {
+  FkLocal<Real> r;
+  const bool p = u >= a.u_c, q = u >= a.u_v;
+  const Real e = ex2<Real>(a.k2 * (u - a.u_csi));
+  const Real sig = Real(1) / (Real(1) + e);
+  // d sig / du = -ln2 k2 e / (1 + e)^2 = -ln2 k2 sig (1 - sig)
+  const Real dsig = -Real(0.69314718055994530942) * a.k2 * sig * (Real(1) - sig);
+  const Real J1 = p ? a.s_tr - v * (Real(1) - u) * (u - a.u_c) * a.s_td
+                    : u * a.s_to;
+  const Real dJ1_du = p ? -a.s_td * v * (Real(1) - Real(2) * u + a.u_c) : a.s_to;
+  const Real dJ1_dv = p ? -a.s_td * (Real(1) - u) * (u - a.u_c) : Real(0);
+  const Real Jd = J1 - w * sig * a.s_tsi;
+  r.un = u + a.tc * du - Jd;
+  r.dun_du = Real(1) - (dJ1_du - w * dsig * a.s_tsi);
+  r.dun_dv = -dJ1_dv;
+  r.dun_dw = sig * a.s_tsi;
+  const Real sv = q ? a.s_tv1m : a.s_tv2m;
+  r.vn = p ? v - v * a.s_tvp : v + (Real(1) - v) * sv;
+  r.dvn_dv = p ? Real(1) - a.s_tvp : Real(1) - sv;
+  r.wn = p ? w - w * a.s_twp : w + (Real(1) - w) * a.s_twm;
+  r.dwn_dw = p ? Real(1) - a.s_twp : Real(1) - a.s_twm;
+  return r;
+}
+
+// du of cell (i, j): the four faces towards the mirrored neighbours.
+template <typename Real>
+__device__ __forceinline__ Real diffusion(const AdjCoeffs<Real> &a,
+                                          const Real *__restrict__ u,
+                                          const Real *__restrict__ r, int i,
+                                          int j) {
+  const int nx = a.nx, ny = a.ny, c = i + nx * j;
+  const int m[4] = {mirror(i - 1, nx) + nx * j, mirror(i + 1, nx) + nx * j,
+                    i + nx * mirror(j - 1, ny), i + nx * mirror(j + 1, ny)};
+  const Real uc = u[c], rc = r[c];
+  Real du = Real(0);
+#pragma unroll
+  for (int f = 0; f < 4; ++f) du += Real(0.5) * (rc + r[m[f]]) * (u[m[f]] - uc);
+  return du;
+}
+
+template <typename Real>
+__global__ void adj_forward_kernel(const AdjCoeffs<Real> a,
+                                   const Real *__restrict__ r,
+                                   const Real *__restrict__ u,
+                                   const Real *__restrict__ v,
+                                   const Real *__restrict__ w, Real *__restrict__ uo,
+                                   Real *__restrict__ vo, Real *__restrict__ wo) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const int c = i + a.nx * j;
+  const FkLocal<Real> f = fk_local(a, u[c], v[c], w[c], diffusion(a, u, r, i, j));
+  uo[c] = f.un;
+  vo[c] = f.vn;
+  wo[c] = f.wn;
+}
+
+// Reverse step: lambda_in = lambda^{n+1} (lu, lv, lw), x^n = (u, v, w);
+// writes lambda^n (without the loss term) and adds to gr (the gradient
+// with respect to r).
+template <typename Real>
+__global__ void adj_reverse_kernel(const AdjCoeffs<Real> a,
+                                   const Real *__restrict__ r,
+                                   const Real *__restrict__ u,
+                                   const Real *__restrict__ v,
+                                   const Real *__restrict__ w,
+                                   const Real *__restrict__ lu,
+                                   const Real *__restrict__ lv,
+                                   const Real *__restrict__ lw,
+                                   Real *__restrict__ lu_o, Real *__restrict__ lv_o,
+                                   Real *__restrict__ lw_o, Real *__restrict__ gr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.nx, ny = a.ny;
+  if (i >= nx || j >= ny) return;
+  const int c = i + nx * j;
+  // pointwise part at c
+  const Real du = diffusion(a, u, r, i, j);
+  const FkLocal<Real> f = fk_local(a, u[c], v[c], w[c], du);
+  const Real lun = lu[c];
+  Real gu = lun * f.dun_du;
+  const Real gv = lun * f.dun_dv + lv[c] * f.dvn_dv;
+  const Real gw = lun * f.dun_dw + lw[c] * f.dwn_dw;
+  // diffusion part: mu_j = tc * lambda_u^{n+1}_j is the adjoint of du_j.
+  // du_j = sum_f (r_j + r_m(j,f)) / 2 (u_m(j,f) - u_j): cell c enters as
+  // j itself (-k_f per face, and r_j in every k_f), and as m(j, f) of the
+  // cells j whose face f points (through the mirror) at c.
+  const Real muc = a.tc * lun;
+  const Real uc = u[c], rc = r[c];
+  const int m[4] = {mirror(i - 1, nx) + nx * j, mirror(i + 1, nx) + nx * j,
+                    i + nx * mirror(j - 1, ny), i + nx * mirror(j + 1, ny)};
+  Real g = Real(0);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const Real k = Real(0.5) * (rc + r[m[q]]);
+    gu -= muc * k;
+    g += Real(0.5) * muc * (u[m[q]] - uc);
+  }
+  // neighbours j of c (the cells whose faces can point at c): the four
+  // physical neighbours in range; for each, the faces f with m(j, f) == c
+  const int di[4] = {-1, 1, 0, 0}, dj[4] = {0, 0, -1, 1};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int ii = i + di[q], jj = j + dj[q];
+    if (ii < 0 || ii >= nx || jj < 0 || jj >= ny) continue;
+    const int cj = ii + nx * jj;
+    const int mj[4] = {mirror(ii - 1, nx) + nx * jj, mirror(ii + 1, nx) + nx * jj,
+                       ii + nx * mirror(jj - 1, ny), ii + nx * mirror(jj + 1, ny)};
+    const Real muj = a.tc * lu[cj];
+    const Real uj = u[cj], rj = r[cj];
+#pragma unroll
+    for (int fq = 0; fq < 4; ++fq) {
+      if (mj[fq] != c) continue;
+      gu += muj * Real(0.5) * (rj + rc);  // d du_j / d u_c
+      g += muj * Real(0.5) * (uc - uj);   // d du_j / d r_c
+    }
+  }
+  lu_o[c] = gu;
+  lv_o[c] = gv;
+  lw_o[c] = gw;
+  gr[c] += g;
+}
+
+// Probe loss of one frame (one block of 256 threads, fixed-order sum) and,
+// with lu != null, its adjoint 2 (u - target) added at the probes.
+template <typename Real>
+__global__ void adj_probe_kernel(int nx, int sp, int npx, int npy,
+                                 const Real *__restrict__ u,
+                                 const float *__restrict__ target,
+                                 double *loss, Real *lu) {
+  __shared__ double s[256];
+  double acc = 0.0;
+  const int np = npx * npy;
+  for (int p = threadIdx.x; p < np; p += 256) {
+    const int px = p % npx, py = p / npx;
+    const int c = (px * sp + sp / 2) + nx * (py * sp + sp / 2);
+    const double d = (double)u[c] - (double)target[p];
+    acc += d * d;
+    if (lu) lu[c] += (Real)(2.0 * d);
+  }
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && loss) *loss += s[0];
+}
+
+template <typename Real>
+__global__ void adj_scale_kernel(int n, Real scale, const Real *__restrict__ x,
+                                 float *__restrict__ y) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) y[k] = (float)(scale * x[k]);
+}
+
+template <typename Real>
+__global__ void adj_to_r_kernel(int n, Real scale, const float *__restrict__ D,
+                                Real *__restrict__ r) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) r[k] = scale * (Real)D[k];
+}
+
+template <typename Real>
+__global__ void adj_widen_kernel(int n, const float *__restrict__ x,
+                                 Real *__restrict__ y) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) y[k] = (Real)x[k];
+}
+
+// The probe values of one frame.
+template <typename Real>
+__global__ void adj_gather_kernel(int nx, int sp, int npx, int npy,
+                                  const Real *__restrict__ u,
+                                  float *__restrict__ out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npx * npy) return;
+  const int px = p % npx, py = p / npx;
+  out[p] = (float)u[(px * sp + sp / 2) + nx * (py * sp + sp / 2)];
+}
+
+inline int st(cudaError_t e) {
+  if (e == cudaSuccess) return YH_OK;
+  if (e == cudaErrorMemoryAllocation) return YH_ENOMEM;
+  return YH_ECUDA;
+}
+
+}  // namespace
+
+struct yh_adjoint {
+  int fp64 = 0;
+  int nx = 0, ny = 0, n = 0;
+  int nsteps = 0, frame = 0, sp = 0, npx = 0, npy = 0, ck = 0;
+  double rscale = 0;  // r = rscale * D
+  cudaStream_t s = nullptr;
+  bool own_stream = false;
+  AdjCoeffs<float> af{};
+  AdjCoeffs<double> ad{};
+  void *ckpt = nullptr;   // checkpoints: (nsteps / ck + 1) states
+  void *seg = nullptr;    // one segment of states: ck + 1 states
+  void *lam = nullptr;    // two adjoint states (ping-pong)
+  void *r = nullptr;      // r = dt D / h^2
+  void *gr = nullptr;     // gradient with respect to r
+  float *target = nullptr;  // [frames][probes]
+  double *loss = nullptr;
+  int frames = 0;
+  // the whole forward (+ reverse) sequence on the handle's own buffers,
+  // captured once: [0] loss only, [1] loss and gradient
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+};
+
+namespace {
+
+template <typename Real>
+struct View {
+  Real *p;
+  int n;
+  Real *f(int state, int field) const { return p + ((size_t)state * 3 + field) * n; }
+};
+
+template <typename Real>
+const AdjCoeffs<Real> &coeffs(const yh_adjoint *h);
+template <>
+const AdjCoeffs<float> &coeffs<float>(const yh_adjoint *h) { return h->af; }
+template <>
+const AdjCoeffs<double> &coeffs<double>(const yh_adjoint *h) { return h->ad; }
+
+template <typename Real>
+cudaError_t fwd(const yh_adjoint *h, const Real *r, const Real *const *x,
+                Real *const *y) {
+  const dim3 b(32, 8), g((h->nx + 31) / 32, (h->ny + 7) / 8);
+  adj_forward_kernel<Real><<<g, b, 0, h->s>>>(coeffs<Real>(h), r, x[0], x[1],
+                                              x[2], y[0], y[1], y[2]);
+  return cudaGetLastError();
+}
+
+// The forward pass (checkpoints, loss) and, with grad, the reverse sweep,
+// on the handle's buffers only: r and checkpoint 0 hold the inputs. Its
+// launches are captured into a CUDA graph by run_t.
+template <typename Real>
+cudaError_t run_body(yh_adjoint *h, bool grad) {
+  const int n = h->n, T = h->nsteps, ck = h->ck;
+  const View<Real> C{(Real *)h->ckpt, n}, S{(Real *)h->seg, n}, L{(Real *)h->lam, n};
+  Real *r = (Real *)h->r, *gr = (Real *)h->gr;
+  cudaError_t e = cudaMemsetAsync(h->loss, 0, sizeof(double), h->s);
+  // forward: checkpoints every ck steps, the loss at every frame
+  {
+    Real *cur[3] = {S.f(0, 0), S.f(0, 1), S.f(0, 2)};
+    Real *nxt[3] = {S.f(1, 0), S.f(1, 1), S.f(1, 2)};
+    for (int q = 0; q < 3 && e == cudaSuccess; ++q)
+      e = cudaMemcpyAsync(cur[q], C.f(0, q), n * sizeof(Real),
+                          cudaMemcpyDeviceToDevice, h->s);
+    for (int t = 0; t < T && e == cudaSuccess; ++t) {
+      e = fwd<Real>(h, r, cur, nxt);
+      for (int q = 0; q < 3; ++q) std::swap(cur[q], nxt[q]);
+      const int step = t + 1;
+      if (e == cudaSuccess && step % h->frame == 0) {
+        adj_probe_kernel<Real><<<1, 256, 0, h->s>>>(
+            h->nx, h->sp, h->npx, h->npy, cur[0],
+            h->target + (size_t)(step / h->frame - 1) * h->npx * h->npy,
+            h->loss, nullptr);
+        e = cudaGetLastError();
+      }
+      if (e == cudaSuccess && step % ck == 0 && step < T)
+        for (int q = 0; q < 3 && e == cudaSuccess; ++q)
+          e = cudaMemcpyAsync(C.f(step / ck, q), cur[q], n * sizeof(Real),
+                              cudaMemcpyDeviceToDevice, h->s);
+    }
+  }
+  if (e != cudaSuccess || !grad) return e;
+  // reverse, one segment at a time from the last: lambda^T = dL/dx^T
+  e = cudaMemsetAsync(L.f(0, 0), 0, 3 * n * sizeof(Real), h->s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(gr, 0, n * sizeof(Real), h->s);
+  int li = 0;  // lambda^{t+1} lives in L state li
+  for (int s0 = ((T - 1) / ck) * ck; s0 >= 0 && e == cudaSuccess; s0 -= ck) {
+    const int s1 = std::min(s0 + ck, T);  // states s0 .. s1
+    for (int q = 0; q < 3 && e == cudaSuccess; ++q)
+      e = cudaMemcpyAsync(S.f(0, q), C.f(s0 / ck, q), n * sizeof(Real),
+                          cudaMemcpyDeviceToDevice, h->s);
+    for (int t = s0; t < s1 && e == cudaSuccess; ++t) {
+      Real *x[3] = {S.f(t - s0, 0), S.f(t - s0, 1), S.f(t - s0, 2)};
+      Real *y[3] = {S.f(t - s0 + 1, 0), S.f(t - s0 + 1, 1), S.f(t - s0 + 1, 2)};
+      e = fwd<Real>(h, r, x, y);
+    }
+    for (int t = s1; t > s0 && e == cudaSuccess; --t) {
+      // lambda^t += dL/dx^t, then lambda^{t-1} from lambda^t and x^{t-1}
+      if (t % h->frame == 0) {
+        adj_probe_kernel<Real><<<1, 256, 0, h->s>>>(
+            h->nx, h->sp, h->npx, h->npy, S.f(t - s0, 0),
+            h->target + (size_t)(t / h->frame - 1) * h->npx * h->npy, nullptr,
+            L.f(li, 0));
+        e = cudaGetLastError();
+        if (e != cudaSuccess) break;
+      }
+      const dim3 b(32, 8), g((h->nx + 31) / 32, (h->ny + 7) / 8);
+      adj_reverse_kernel<Real><<<g, b, 0, h->s>>>(
+          coeffs<Real>(h), r, S.f(t - 1 - s0, 0), S.f(t - 1 - s0, 1),
+          S.f(t - 1 - s0, 2), L.f(li, 0), L.f(li, 1), L.f(li, 2),
+          L.f(li ^ 1, 0), L.f(li ^ 1, 1), L.f(li ^ 1, 2), gr);
+      e = cudaGetLastError();
+      li ^= 1;
+    }
+  }
+  return e;
+}
+
+template <typename Real>
+int run_t(yh_adjoint *h, const float *D, const float *u0, const float *v0,
+          const float *w0, double *loss_out, float *grad) {
+  const int n = h->n;
+  const View<Real> C{(Real *)h->ckpt, n};
+  const int nb = (n + 255) / 256;
+  // the inputs into the handle's buffers (outside the graph: the caller's
+  // pointers may change from run to run)
+  adj_to_r_kernel<Real><<<nb, 256, 0, h->s>>>(n, (Real)h->rscale, D, (Real *)h->r);
+  const float *x0[3] = {u0, v0, w0};
+  for (int q = 0; q < 3; ++q)
+    adj_widen_kernel<Real><<<nb, 256, 0, h->s>>>(n, x0[q], C.f(0, q));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return st(e);
+  cudaGraphExec_t &ex = h->graph[grad ? 1 : 0];
+  if (!ex) {
+    cudaGraph_t g = nullptr;
+    e = cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return st(e);
+    const cudaError_t eb = run_body<Real>(h, grad != nullptr);
+    e = cudaStreamEndCapture(h->s, &g);
+    if (eb != cudaSuccess || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return st(eb != cudaSuccess ? eb : e);
+    }
+    e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      ex = nullptr;
+      return st(e);
+    }
+  }
+  e = cudaGraphLaunch(ex, h->s);
+  if (e == cudaSuccess && grad) {
+    // dL/dD = dL/dr * dt / h^2
+    adj_scale_kernel<Real><<<nb, 256, 0, h->s>>>(n, (Real)h->rscale,
+                                                 (const Real *)h->gr, grad);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && loss_out)
+    e = cudaMemcpyAsync(loss_out, h->loss, sizeof(double), cudaMemcpyDeviceToHost, h->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  return st(e);
+}
+
+// A forward run that gathers the probe values of every frame (a target).
+template <typename Real>
+int record_t(yh_adjoint *h, const float *D, const float *u0, const float *v0,
+             const float *w0, float *probes) {
+  const int n = h->n, T = h->nsteps, np = h->npx * h->npy;
+  const View<Real> S{(Real *)h->seg, n};
+  Real *r = (Real *)h->r;
+  const int nb = (n + 255) / 256;
+  adj_to_r_kernel<Real><<<nb, 256, 0, h->s>>>(n, (Real)h->rscale, D, r);
+  const float *x0[3] = {u0, v0, w0};
+  for (int q = 0; q < 3; ++q)
+    adj_widen_kernel<Real><<<nb, 256, 0, h->s>>>(n, x0[q], S.f(0, q));
+  cudaError_t e = cudaGetLastError();
+  Real *cur[3] = {S.f(0, 0), S.f(0, 1), S.f(0, 2)};
+  Real *nxt[3] = {S.f(1, 0), S.f(1, 1), S.f(1, 2)};
+  for (int t = 0; t < T && e == cudaSuccess; ++t) {
+    e = fwd<Real>(h, r, cur, nxt);
+    for (int q = 0; q < 3; ++q) std::swap(cur[q], nxt[q]);
+    if (e == cudaSuccess && (t + 1) % h->frame == 0) {
+      const int f = (t + 1) / h->frame - 1;
+      adj_gather_kernel<Real><<<(np + 255) / 256, 256, 0, h->s>>>(
+          h->nx, h->sp, h->npx, h->npy, cur[0], probes + (size_t)f * np);
+      e = cudaGetLastError();
+    }
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  return st(e);
+}
+
+}  // namespace
+
+extern "C" int yh_adjoint_destroy(yh_adjoint *h) {
+  if (!h) return YH_EINVAL;
+  if (h->s) cudaStreamSynchronize(h->s);
+  for (auto &g : h->graph)
+    if (g) cudaGraphExecDestroy(g);
+  cudaFree(h->ckpt);
+  cudaFree(h->seg);
+  cudaFree(h->lam);
+  cudaFree(h->r);
+  cudaFree(h->gr);
+  cudaFree(h->target);
+  cudaFree(h->loss);
+  if (h->own_stream && h->s) cudaStreamDestroy(h->s);
+  delete h;
+  return YH_OK;
+}
+
+extern "C" int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
+                                 int nsteps, int frame_steps, int probe_spacing,
+                                 int checkpoint_steps, int fp64, void *stream,
+                                 yh_adjoint **out) {
+  if (!out) return YH_EINVAL;
+  *out = nullptr;
+  int rc = check_params(p, YH_MODEL_FK3V, fk);
+  if (rc) return rc;
+  if (p->hx != p->hy || nsteps < 1 || frame_steps < 1 || probe_spacing < 1 ||
+      probe_spacing > p->nx || probe_spacing > p->ny || checkpoint_steps < 1)
+    return YH_EINVAL;
+  yh_adjoint *h = new (std::nothrow) yh_adjoint();
+  if (!h) return YH_ENOMEM;
+  h->fp64 = fp64 ? 1 : 0;
+  h->nx = p->nx;
+  h->ny = p->ny;
+  h->n = p->nx * p->ny;
+  h->nsteps = nsteps;
+  h->frame = frame_steps;
+  h->sp = probe_spacing;
+  h->npx = p->nx / probe_spacing;
+  h->npy = p->ny / probe_spacing;
+  h->ck = checkpoint_steps;
+  h->frames = nsteps / frame_steps;
+  h->rscale = p->dt / (p->hx * p->hx);
+  const StepCoeffs<double> sd = make_step_coeffs<double>(*p, YH_MODEL_FK3V, fk);
+  auto fill = [&](auto &a) {
+    using R = decltype(a.tc);
+    a.nx = p->nx;
+    a.ny = p->ny;
+    a.tc = (R)sd.tc;
+    a.dt = (R)sd.dt;
+    a.u_c = (R)sd.u_c;
+    a.u_v = (R)sd.u_v;
+    a.u_csi = (R)sd.u_csi;
+    a.k2 = (R)sd.k_exp2;
+    a.s_td = (R)sd.s_td;
+    a.s_tr = (R)sd.s_tr;
+    a.s_to = (R)sd.s_to;
+    a.s_tsi = (R)sd.s_tsi;
+    a.s_tvp = (R)sd.s_tvp;
+    a.s_tv1m = (R)sd.s_tv1m;
+    a.s_tv2m = (R)sd.s_tv2m;
+    a.s_twp = (R)sd.s_twp;
+    a.s_twm = (R)sd.s_twm;
+  };
+  fill(h->af);
+  fill(h->ad);
+  const size_t es = h->fp64 ? sizeof(double) : sizeof(float);
+  const size_t state = 3 * (size_t)h->n * es;
+  const size_t nck = (size_t)(nsteps - 1) / checkpoint_steps + 1;
+  cudaError_t e = cudaSuccess;
+  h->s = (cudaStream_t)stream;
+  if (!h->s) {
+    e = cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking);
+    h->own_stream = e == cudaSuccess;
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&h->ckpt, nck * state);
+  if (e == cudaSuccess) e = cudaMalloc(&h->seg, (size_t)(checkpoint_steps + 1) * state);
+  if (e == cudaSuccess) e = cudaMalloc(&h->lam, 2 * state);
+  if (e == cudaSuccess) e = cudaMalloc(&h->r, h->n * es);
+  if (e == cudaSuccess) e = cudaMalloc(&h->gr, h->n * es);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&h->target, (size_t)std::max(1, h->frames) * h->npx * h->npy * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&h->loss, sizeof(double));
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(h->target, 0,
+                        (size_t)std::max(1, h->frames) * h->npx * h->npy * sizeof(float), h->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  if (e != cudaSuccess) {
+    yh_adjoint_destroy(h);
+    return st(e);
+  }
+  *out = h;
+  return YH_OK;
+}
+
+extern "C" int yh_adjoint_set_target(yh_adjoint *h, const float *target) {
+  if (!h || !target) return YH_EINVAL;
+  cudaError_t e = cudaMemcpyAsync(h->target, target,
+                                  (size_t)h->frames * h->npx * h->npy * sizeof(float),
+                                  cudaMemcpyDefault, h->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  return st(e);
+}
+
+extern "C" int yh_adjoint_probes(yh_adjoint *h, int *frames, int *probes_x,
+                                 int *probes_y) {
+  if (!h) return YH_EINVAL;
+  if (frames) *frames = h->frames;
+  if (probes_x) *probes_x = h->npx;
+  if (probes_y) *probes_y = h->npy;
+  return YH_OK;
+}
+
+extern "C" int yh_adjoint_run(yh_adjoint *h, const float *D, const float *u0,
+                              const float *v0, const float *w0, double *loss,
+                              float *grad_D) {
+  if (!h || !D || !u0 || !v0 || !w0) return YH_EINVAL;
+  return h->fp64 ? run_t<double>(h, D, u0, v0, w0, loss, grad_D)
+                 : run_t<float>(h, D, u0, v0, w0, loss, grad_D);
+}
+
+extern "C" int yh_adjoint_record(yh_adjoint *h, const float *D, const float *u0,
+                                 const float *v0, const float *w0,
+                                 float *probes) {
+  if (!h || !D || !u0 || !v0 || !w0 || !probes) return YH_EINVAL;
+  return h->fp64 ? record_t<double>(h, D, u0, v0, w0, probes)
+                 : record_t<float>(h, D, u0, v0, w0, probes);
+}
