@@ -397,6 +397,127 @@ def run_batch(args):
         dist.destroy_process_group()
 
 
+def run_adjoint(args):
+    """The adjoint workload (fk_adjoint_512: 512^2 FK3V, D(x, y) of 8
+    Gaussian bumps in [5e-4, 1.5e-3], 10,000 steps, the loss on a 32 x 32
+    probe lattice every 20 steps, target from the true D, gradient at
+    1.1 D; the model's switches as tanh ramps of width 0.01, without which
+    the loss's derivative is not usable at this horizon): gradients per
+    second, the FP32 gradient against the FP64 one, and the FP64 gradient
+    against central differences of its loss."""
+    import torch
+    rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
+    torch.cuda.set_device(env_int("LOCAL_RANK", 0))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(
+            "cuda", env_int("LOCAL_RANK", 0)))
+    from yolohtli_gb300 import _abi as A
+    from yolohtli_gb300 import workloads as W
+    from yolohtli_gb300.adjoint import Adjoint
+    n, nsteps = 512, args.nsteps
+    frame, spacing = 20, 16
+    ck = max(1, int(round(nsteps ** 0.5)))
+    p = A.fk_tissue_params(n, n)
+    D_true, state0 = W.fk_adjoint_case(n, seed=0)
+
+    smooth = 0.01  # tanh switches: a derivative usable over 10,000 steps
+
+    def make(fp64, steps):
+        a = Adjoint(p, A.fk_defaults(), steps, frame, spacing,
+                    max(1, int(round(steps ** 0.5))), fp64=fp64, smooth=smooth)
+        st = [torch.tensor(x, device="cuda") for x in state0]
+        Dt = torch.tensor(D_true, device="cuda")
+        tgt = torch.empty(a.target_shape, dtype=torch.float32, device="cuda")
+        a.record(Dt, st, tgt)
+        a.set_target(tgt)
+        return a, st, Dt * 1.1
+
+    adj, st, D = make(False, nsteps)
+    g = torch.empty_like(D)
+    for _ in range(args.warmup):
+        adj.run(D, st, g)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(env_int("LOCAL_RANK", 0))
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        loss = adj.run(D, st, g)
+    sec = time.perf_counter() - t0
+    clk = clocks.stop()
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        adj.run(D, st)
+    fwd = time.perf_counter() - t1
+    sec = max_over_ranks(sec, dist, "cuda")
+    value = world * args.steps / sec
+    # end to end: D from the host, the gradient back, every gradient
+    Dh = D.cpu().pin_memory()
+    gh = torch.empty_like(Dh).pin_memory()
+    Dd = torch.empty_like(D)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    for _ in range(args.steps):
+        Dd.copy_(Dh, non_blocking=True)
+        adj.run(Dd, st, g)
+        gh.copy_(g)
+    e2e_s = max_over_ranks(time.perf_counter() - t2, dist, "cuda")
+    # accuracy, at the full size: the FP64 gradient against central
+    # differences of the FP64 loss (h = 1e-3 relative, 2 random directions),
+    # and the FP32 gradient against the FP64 one
+    b64, st64, D64 = make(True, nsteps)
+    g64 = torch.empty_like(D64)
+    b64.run(D64, st64, g64)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    b64.run(D64, st64, g64)
+    fp64_rate = 1.0 / (time.perf_counter() - t3)
+    rng = np.random.default_rng(3)
+    fd_err = 0.0
+    for _ in range(2):
+        d = torch.tensor(rng.standard_normal(n * n).astype(np.float32), device="cuda") * D64
+        Dp, Dm = D64 + 1e-3 * d, D64 - 1e-3 * d
+        step = (Dp.double() - Dm.double()) / 2
+        fd = b64.run(Dp, st64) - b64.run(Dm, st64)
+        ad = 2 * float((g64.double() * step).sum())
+        fd_err = max(fd_err, abs(fd - ad) / max(abs(ad), 1e-300))
+    rel = float((g.double() - g64.double()).norm() / g64.double().norm())
+    if rank == 0:
+        line = {
+            "metric": "adjoint gradients/s", "value": round(value, 3),
+            "unit": "gradients/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * sec / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "fk_adjoint_512", "grid": [n, n],
+                       "steps_per_gradient": nsteps, "frames": nsteps // frame,
+                       "probes": [n // spacing, n // spacing],
+                       "checkpoint_steps": ck, "D": "8 Gaussian bumps in [5e-4, 1.5e-3]",
+                       "switches": "FK3V's H(u - u_c), H(u - u_v) as tanh ramps of width %g" % smooth,
+                       "estimate": "1.1 x the true D",
+                       "parallelism": "replicas x%d" % world},
+            "loss": loss, "forward_ratio": round(sec / fwd, 3),
+            "fd_check": {"directions": 2, "h_rel": 1e-3,
+                         "max_rel_err": fd_err,
+                         "note": "directional derivatives of the FP64 "
+                                 "adjoint against central differences of "
+                                 "the FP64 loss, full size"},
+            "fp32_vs_fp64_gradient_rel_l2": rel,
+            "fp64_gradients_per_s": round(fp64_rate, 3),
+            "roofline": None, "cpu_baseline": None,
+            "e2e": {"value": round(world * args.steps / e2e_s, 3),
+                    "unit": "gradients/s", "h2d_bytes_per_step": 4 * n * n,
+                    "d2h_bytes_per_step": 4 * n * n},
+            "gpu_launches": None, "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -413,7 +534,7 @@ def main():
                     help="explicit steps per solve (default: the workload's, "
                          "20,000 for fk_holes_1024, 5,000 for batch256)")
     ap.add_argument("--workload", default="holes1024",
-                    choices=["holes1024", "batch256"],
+                    choices=["holes1024", "batch256", "adjoint512"],
                     help="holes1024: one 1024^2 grid with 300 holes (the "
                          "headline); batch256: 256 grids of 128^2..768^2 "
                          "through the batched solver")
@@ -424,6 +545,15 @@ def main():
     args = ap.parse_args()
 
     from yolohtli_gb300 import workloads as W
+    if args.workload == "adjoint512":
+        if args.nsteps is None:
+            args.nsteps = 10000
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the reference computes no gradients"}), flush=True)
+        else:
+            run_adjoint(args)
+        return
     if args.workload == "batch256":
         if args.nsteps is None:
             args.nsteps = 5000

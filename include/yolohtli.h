@@ -513,12 +513,17 @@ int yh_batch_get_launch_count(yh_batch *b, long long *n);
  * frame_steps steps. One run takes nsteps forward steps keeping a
  * checkpoint every checkpoint_steps, then recomputes each segment and
  * sweeps it backwards: memory is the checkpoints plus one segment. fp64
- * runs the same in FP64 (for gradient checks). hx must equal hy. */
+ * runs the same in FP64 (for gradient checks). hx must equal hy. smooth:
+ * 0 keeps FK3V's switches H(u - u_c), H(u - u_v) as steps (the model of
+ * the other engines; its derivative exists almost everywhere but grows with
+ * the horizon and leaves out the threshold-crossing times); smooth > 0
+ * replaces them by (1 + tanh(x / smooth)) / 2 in this solver's forward and
+ * reverse steps. */
 typedef struct yh_adjoint yh_adjoint;
 int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
                       int nsteps, int frame_steps, int probe_spacing,
-                      int checkpoint_steps, int fp64, void *stream,
-                      yh_adjoint **out);
+                      int checkpoint_steps, int fp64, double smooth,
+                      void *stream, yh_adjoint **out);
 int yh_adjoint_destroy(yh_adjoint *h);
 /* Frames (nsteps / frame_steps) and probes (nx / spacing, ny / spacing). */
 int yh_adjoint_probes(yh_adjoint *h, int *frames, int *probes_x,

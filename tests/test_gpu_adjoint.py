@@ -35,10 +35,11 @@ def start(n):
     return [u.ravel(), v.ravel(), w.ravel()]
 
 
-def problem(n, nsteps, frame, spacing, ck, fp64, seed=5):
+def problem(n, nsteps, frame, spacing, ck, fp64, seed=5, smooth=0.0):
     import torch
     p = A.fk_tissue_params(n, n)
-    adj = Adjoint(p, A.fk_defaults(), nsteps, frame, spacing, ck, fp64=fp64)
+    adj = Adjoint(p, A.fk_defaults(), nsteps, frame, spacing, ck, fp64=fp64,
+                  smooth=smooth)
     st = [dev(x) for x in start(n)]
     D_true = dev(d_map(n, seed))
     tgt = torch.empty(adj.target_shape, dtype=torch.float32, device="cuda")
@@ -67,6 +68,28 @@ def test_fp64_gradient_matches_central_differences():
         fd = (Lp - Lm)
         ad = 2 * float((g.double() * step).sum())
         assert abs(fd - ad) <= 1e-5 * abs(ad) + 1e-12 * L0, (k, fd, ad)
+
+
+@pytest.mark.parametrize("fp64", [True, False])
+def test_smoothed_switches_give_a_gradient_central_differences_confirm(fp64):
+    # with FK3V's switches as tanh ramps (width 0.01) the derivative stays
+    # bounded over long horizons and central differences with h = 1e-3
+    # (relative) agree with it; with steps they stop agreeing after a few
+    # hundred steps (the derivative leaves out the threshold crossings)
+    import torch
+    n, nsteps = 96, 1500
+    adj, st, D = problem(n, nsteps, 20, 8, 39, fp64=fp64, smooth=0.01)
+    g = torch.empty_like(D)
+    adj.run(D, st, g)
+    rng = np.random.default_rng(4)
+    for k in range(3):
+        d = dev(rng.standard_normal(n * n).astype(np.float32)) * D
+        Dp, Dm = D + 1e-3 * d, D - 1e-3 * d
+        step = (Dp.double() - Dm.double()) / 2
+        fd = adj.run(Dp, st) - adj.run(Dm, st)
+        ad = 2 * float((g.double() * step).sum())
+        tol = 1e-5 if fp64 else 1e-3
+        assert abs(fd - ad) <= tol * abs(ad), (k, fd, ad)
 
 
 def test_fp32_gradient_against_fp64():

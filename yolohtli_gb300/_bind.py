@@ -77,7 +77,7 @@ SIGNATURES = {
     "yh_batch_get_launch_count": (_i, [_v, _P(C.c_longlong)]),
     # adjoint
     "yh_adjoint_create": (_i, [_P(A.ParamVar), _P(A.FKParams), _i, _i, _i, _i,
-                               _i, _v, _P(_v)]),
+                               _i, _d, _v, _P(_v)]),
     "yh_adjoint_destroy": (_i, [_v]),
     "yh_adjoint_probes": (_i, [_v, _P(_i), _P(_i), _P(_i)]),
     "yh_adjoint_set_target": (_i, [_v, _v]),

@@ -11,14 +11,26 @@ from ._loader import load
 from .ops import check
 
 
+def _after_torch():
+    """The handle runs on its own stream: inputs that torch is still
+    writing on its current stream must be complete first."""
+    try:
+        import torch
+        if torch.cuda.is_available() and torch.cuda.is_initialized():
+            torch.cuda.current_stream().synchronize()
+    except ImportError:
+        pass
+
+
 class Adjoint:
     """One FK3V problem: grid and parameters p (hx == hy), the FK3V
     parameters, nsteps steps, the loss on the states after every
     frame_steps steps at a probe lattice every probe_spacing cells,
-    checkpoints every checkpoint_steps (default ~sqrt(nsteps))."""
+    checkpoints every checkpoint_steps (default ~sqrt(nsteps)); smooth > 0
+    replaces the model's switches by tanh ramps of that width."""
 
     def __init__(self, p, fk, nsteps, frame_steps, probe_spacing,
-                 checkpoint_steps=None, fp64=False, stream=None):
+                 checkpoint_steps=None, fp64=False, smooth=0.0, stream=None):
         self.lib = load()
         self.p = p.copy()
         if checkpoint_steps is None:
@@ -27,7 +39,7 @@ class Adjoint:
         check("yh_adjoint_create", self.lib.yh_adjoint_create(
             C.byref(self.p), C.byref(fk), int(nsteps), int(frame_steps),
             int(probe_spacing), int(checkpoint_steps), 1 if fp64 else 0,
-            C.c_void_p(stream) if stream else None, C.byref(h)))
+            float(smooth), C.c_void_p(stream) if stream else None, C.byref(h)))
         self.h = h
         f, px, py = C.c_int(), C.c_int(), C.c_int()
         check("yh_adjoint_probes", self.lib.yh_adjoint_probes(
@@ -53,10 +65,12 @@ class Adjoint:
         """target: a device tensor or host array of target_shape floats."""
         ptr = target.data_ptr() if hasattr(target, "data_ptr") else \
             np.ascontiguousarray(target, dtype=np.float32).ctypes.data
+        _after_torch()
         check("yh_adjoint_set_target", self.lib.yh_adjoint_set_target(self.h, ptr))
 
     def record(self, D, state0, out):
         """Probe values of a forward run into `out` (device float32)."""
+        _after_torch()
         check("yh_adjoint_record", self.lib.yh_adjoint_record(
             self.h, D.data_ptr(), *[x.data_ptr() for x in state0],
             out.data_ptr()))
@@ -64,6 +78,7 @@ class Adjoint:
     def run(self, D, state0, grad=None):
         """Loss (float) and, with `grad` (device float32 like D), dLoss/dD."""
         loss = C.c_double()
+        _after_torch()
         check("yh_adjoint_run", self.lib.yh_adjoint_run(
             self.h, D.data_ptr(), *[x.data_ptr() for x in state0],
             C.byref(loss), grad.data_ptr() if grad is not None else None))
@@ -81,7 +96,6 @@ def _make_function():
         def forward(ctx, D, adjoint, state0):
             D = D.contiguous()
             state0 = [x.contiguous() for x in state0]
-            torch.cuda.synchronize()
             grad = torch.empty_like(D)
             loss = adjoint.run(D, state0, grad)
             ctx.save_for_backward(grad)

@@ -11,7 +11,12 @@
 // then the FK3V update with du (Fenton & Karma 1998, tc-scaled Euler):
 //   u' = u + tc du - dt tc J(u, v, w),  v' = v + dt tc g_v,  w' = w + dt tc g_w
 // in exact arithmetic (exp2 and division, no approximate MUFU forms), so the
-// reverse step differentiates exactly what the forward step computes.
+// reverse step differentiates exactly what the forward step computes. The
+// model's switches H(u - u_c), H(u - u_v) are steps (smooth = 0) or, for a
+// loss that stays differentiable over long horizons, (1 + tanh(x/eps))/2:
+// with steps the derivative exists almost everywhere but leaves out the
+// threshold-crossing times that move the fronts, and it grows with the
+// horizon (the upstroke's local instability).
 //
 // Loss: L = sum over frames f (the states after every `frame` steps) of
 // sum over probes p (cells (px*sp + sp/2, py*sp + sp/2)) of
@@ -48,6 +53,7 @@ namespace {
 template <typename Real>
 struct AdjCoeffs {
   int nx, ny;
+  Real eps;  // width of the smoothed switches H(u - u_c), H(u - u_v); 0: steps
   Real tc, dt;
   Real u_c, u_v, u_csi, k2;  // k2: -2k log2(e) of the sigmoid's 2^(k2 (u - u_csi))
   Real s_td, s_tr, s_to, s_tsi, s_tvp, s_tv1m, s_tv2m, s_twp, s_twm;
@@ -60,38 +66,72 @@ __device__ __forceinline__ float ex2<float>(float x) { return exp2f(x); }
 template <>
 __device__ __forceinline__ double ex2<double>(double x) { return exp2(x); }
 
+template <typename Real>
+__device__ __forceinline__ Real th(Real x);
+template <>
+__device__ __forceinline__ float th<float>(float x) { return tanhf(x); }
+template <>
+__device__ __forceinline__ double th<double>(double x) { return tanh(x); }
+
+// The switch H(x) of the model (a step at 0) and its derivative: with a
+// smoothing width eps > 0, H = (1 + tanh(x / eps)) / 2.
+template <typename Real>
+__device__ __forceinline__ void heaviside(Real x, Real eps, Real &H, Real &dH) {
+  if (eps > Real(0)) {
+    const Real t = th<Real>(x / eps);
+    H = Real(0.5) * (Real(1) + t);
+    dH = Real(0.5) * (Real(1) - t * t) / eps;
+  } else {
+    H = x >= Real(0) ? Real(1) : Real(0);
+    dH = Real(0);
+  }
+}
+
 // The pointwise FK3V update and its partial derivatives.
 template <typename Real>
 struct FkLocal {
   Real un, vn, wn;
   Real dun_du, dun_dv, dun_dw;  // of un (du held fixed)
-  Real dvn_dv, dwn_dw;
+  Real dvn_du, dvn_dv, dwn_du, dwn_dw;
 };
 
+// J1 = H1 jp + (1 - H1) jn, v' = H1 vp + (1 - H1) vm, w' = H1 wp + (1 - H1) wm
+// with H1 = H(u - u_c) and the v time constant H2 s_tv1m + (1 - H2) s_tv2m,
+// H2 = H(u - u_v): the FK3V update (fk3v_update) when eps = 0.
 template <typename Real>
 __device__ __forceinline__ FkLocal<Real> fk_local(const AdjCoeffs<Real> &a,
                                                   Real u, Real v, Real w,
                                                   Real du) {
   FkLocal<Real> r;
-  const bool p = u >= a.u_c, q = u >= a.u_v;
+  Real H1, dH1, H2, dH2;
+  heaviside(u - a.u_c, a.eps, H1, dH1);
+  heaviside(u - a.u_v, a.eps, H2, dH2);
   const Real e = ex2<Real>(a.k2 * (u - a.u_csi));
   const Real sig = Real(1) / (Real(1) + e);
   // d sig / du = -ln2 k2 e / (1 + e)^2 = -ln2 k2 sig (1 - sig)
   const Real dsig = -Real(0.69314718055994530942) * a.k2 * sig * (Real(1) - sig);
-  const Real J1 = p ? a.s_tr - v * (Real(1) - u) * (u - a.u_c) * a.s_td
-                    : u * a.s_to;
-  const Real dJ1_du = p ? -a.s_td * v * (Real(1) - Real(2) * u + a.u_c) : a.s_to;
-  const Real dJ1_dv = p ? -a.s_td * (Real(1) - u) * (u - a.u_c) : Real(0);
+  const Real jp = a.s_tr - v * (Real(1) - u) * (u - a.u_c) * a.s_td;
+  const Real jn = u * a.s_to;
+  const Real djp_du = -a.s_td * v * (Real(1) - Real(2) * u + a.u_c);
+  const Real djp_dv = -a.s_td * (Real(1) - u) * (u - a.u_c);
+  const Real J1 = H1 * jp + (Real(1) - H1) * jn;
+  const Real dJ1_du = H1 * djp_du + (Real(1) - H1) * a.s_to + dH1 * (jp - jn);
+  const Real dJ1_dv = H1 * djp_dv;
   const Real Jd = J1 - w * sig * a.s_tsi;
   r.un = u + a.tc * du - Jd;
   r.dun_du = Real(1) - (dJ1_du - w * dsig * a.s_tsi);
   r.dun_dv = -dJ1_dv;
   r.dun_dw = sig * a.s_tsi;
-  const Real sv = q ? a.s_tv1m : a.s_tv2m;
-  r.vn = p ? v - v * a.s_tvp : v + (Real(1) - v) * sv;
-  r.dvn_dv = p ? Real(1) - a.s_tvp : Real(1) - sv;
-  r.wn = p ? w - w * a.s_twp : w + (Real(1) - w) * a.s_twm;
-  r.dwn_dw = p ? Real(1) - a.s_twp : Real(1) - a.s_twm;
+  const Real sv = H2 * a.s_tv1m + (Real(1) - H2) * a.s_tv2m;
+  const Real vp = v - v * a.s_tvp, vm = v + (Real(1) - v) * sv;
+  r.vn = H1 * vp + (Real(1) - H1) * vm;
+  r.dvn_dv = H1 * (Real(1) - a.s_tvp) + (Real(1) - H1) * (Real(1) - sv);
+  r.dvn_du = dH1 * (vp - vm) +
+             (Real(1) - H1) * (Real(1) - v) * dH2 * (a.s_tv1m - a.s_tv2m);
+  const Real wp = w - w * a.s_twp, wm = w + (Real(1) - w) * a.s_twm;
+  r.wn = H1 * wp + (Real(1) - H1) * wm;
+  r.dwn_dw = H1 * (Real(1) - a.s_twp) + (Real(1) - H1) * (Real(1) - a.s_twm);
+  r.dwn_du = dH1 * (wp - wm);
   return r;
 }
 
@@ -151,7 +191,7 @@ __global__ void adj_reverse_kernel(const AdjCoeffs<Real> a,
   const Real du = diffusion(a, u, r, i, j);
   const FkLocal<Real> f = fk_local(a, u[c], v[c], w[c], du);
   const Real lun = lu[c];
-  Real gu = lun * f.dun_du;
+  Real gu = lun * f.dun_du + lv[c] * f.dvn_du + lw[c] * f.dwn_du;
   const Real gv = lun * f.dun_dv + lv[c] * f.dvn_dv;
   const Real gw = lun * f.dun_dw + lw[c] * f.dwn_dw;
   // diffusion part: mu_j = tc * lambda_u^{n+1}_j is the adjoint of du_j.
@@ -472,14 +512,15 @@ extern "C" int yh_adjoint_destroy(yh_adjoint *h) {
 
 extern "C" int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
                                  int nsteps, int frame_steps, int probe_spacing,
-                                 int checkpoint_steps, int fp64, void *stream,
-                                 yh_adjoint **out) {
+                                 int checkpoint_steps, int fp64, double smooth,
+                                 void *stream, yh_adjoint **out) {
   if (!out) return YH_EINVAL;
   *out = nullptr;
   int rc = check_params(p, YH_MODEL_FK3V, fk);
   if (rc) return rc;
   if (p->hx != p->hy || nsteps < 1 || frame_steps < 1 || probe_spacing < 1 ||
-      probe_spacing > p->nx || probe_spacing > p->ny || checkpoint_steps < 1)
+      probe_spacing > p->nx || probe_spacing > p->ny || checkpoint_steps < 1 ||
+      !(smooth >= 0.0))
     return YH_EINVAL;
   yh_adjoint *h = new (std::nothrow) yh_adjoint();
   if (!h) return YH_ENOMEM;
@@ -500,6 +541,7 @@ extern "C" int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
     using R = decltype(a.tc);
     a.nx = p->nx;
     a.ny = p->ny;
+    a.eps = (R)smooth;
     a.tc = (R)sd.tc;
     a.dt = (R)sd.dt;
     a.u_c = (R)sd.u_c;

@@ -6,6 +6,9 @@ fk_spiral_256      256x256, 10,000 steps, S1 columns 0-9 at t=0, S2 lower-left
 fk_holes_1024      1024x1024, 20,000 steps, 300 circular holes (r ~ U[2,6]
                    cells), 12 S2 patches of 40x40 at uniform positions and
                    times ~ U[200,400] ms: fibrillation-like.
+fk_adjoint_case    512x512 parameter estimation: D(x, y) of 8 seeded Gaussian
+                   bumps in [5e-4, 1.5e-3] cm^2/ms, a plane wave from the
+                   left edge (the adjoint's workload).
 fk_batch_256       256 independent square grids, n ~ U{128, 160, ..., 768},
                    5,000 steps, D ~ U[5e-4, 1.5e-3] cm^2/ms, every FK time
                    constant scaled by exp(U[ln 0.8, ln 1.2]), 0-100 holes
@@ -159,3 +162,22 @@ def fk_batch_256(seed=0, count=256, nsteps=5000, sizes=range(128, 769, 32),
         inst.append(Workload("fk_batch_%d" % k, p, fk, A.YH_MODEL_FK3V,
                              u, v, w, solid, [s2], nsteps))
     return BatchWorkload("fk_batch_%d" % count, inst, nsteps)
+
+
+def fk_adjoint_case(n=512, seed=0, bumps=8):
+    """(D, (u0, v0, w0)): the diffusion map and initial state of the
+    adjoint workload."""
+    rng = np.random.default_rng(seed)
+    jj, ii = np.mgrid[0:n, 0:n] / n
+    z = np.zeros((n, n))
+    for _ in range(bumps):
+        cx, cy = rng.uniform(0, 1, 2)
+        s = rng.uniform(0.05, 0.2)
+        z += rng.uniform(-1, 1) * np.exp(-((ii - cx) ** 2 + (jj - cy) ** 2) / (2 * s * s))
+    z = (z - z.min()) / max(z.max() - z.min(), 1e-12)
+    D = (5e-4 + 1e-3 * z).astype(np.float32).ravel()
+    u = np.zeros((n, n), np.float32)
+    u[:, :6] = 1.0
+    v = np.ones((n, n), np.float32)
+    w = np.ones((n, n), np.float32)
+    return D, [u.ravel(), v.ravel(), w.ravel()]
