@@ -397,6 +397,226 @@ def run_batch(args):
         dist.destroy_process_group()
 
 
+def sr_start():
+    """The re-entry that seeds the symmetry-reduced workload (fk_sr_512:
+    FK3V BR fit on 512^2, S1 at 0 ms, S2 on the lower-left quadrant at
+    430 ms, 20,000 steps of 0.05 ms). Returns (p, fk, state, tips)."""
+    from yolohtli_gb300 import workloads as W
+    from yolohtli_gb300.solver import Monodomain
+    wl = W.fk_sr_512(seed=0)
+    n = wl.p.nx
+    q = wl.p.copy()
+    q.tipx = q.tipy = n / 2  # tips anywhere in the tissue
+    q.tipOffsetX = q.tipOffsetY = n // 2
+    m = Monodomain(q, wl.model, wl.fk)
+    m.set_state(*wl.state0())
+    m.run(wl.nsteps - 1, wl.stims)
+    m.run(1)
+    m.track_tips()
+    tips = m.get_tips()
+    st = m.get_state()
+    m.close()
+    return wl.p, wl.fk, st, tips
+
+
+def sr_params(p, tip, radius=160):
+    """SR parameters: dt halved as the reference does in SR mode
+    (main.cu:148), the tip disc centred on the spiral's tip."""
+    from yolohtli_gb300 import _abi as A
+    q = p.copy()
+    q.dt *= 0.5
+    A.param_derive(q)
+    q.tipx, q.tipy = tip
+    q.tipOffsetX = q.tipOffsetY = radius
+    return q
+
+
+def run_sr(args):
+    """The symmetry-reduced spiral: FK3V FP32 on 512^2, every step RD, tips,
+    slices, the 12 phase-condition integrals in FP64, the FP64 3x3 solve,
+    the comoving field and BFECC, all on the device. Template: the spiral at
+    1000 ms (frozen); tau_d in {0.25, 0.35, 0.45}. `value` is SR steps/s
+    at tau_d = 0.25; the template retaken every step (the reference's
+    behaviour) and the REF2V FP64 drop-in of the reference's own symbols,
+    driven in its own sequence (main.cu:894-954), are reported beside it."""
+    import torch
+    from yolohtli_gb300 import _abi as A
+    from yolohtli_gb300 import workloads as W
+    from yolohtli_gb300.compat import Compat, sr_driver
+    from yolohtli_gb300.solver import Monodomain
+    nsr, K = args.nsteps, args.steps
+    p, fk, st, tips = sr_start()
+    n = p.nx
+    if not len(tips):
+        raise RuntimeError("the SR start has no spiral tip")
+    q = sr_params(p, (float(tips[0, 0]), float(tips[0, 1])))
+    N = n * n
+
+    def timed(m, k):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = m.launch_count()
+        e0.record()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            m.sr_step(nsr)
+        m.synchronize()
+        e1.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        return wall, m.launch_count() - l0
+
+    rates, status, launches, clk = {}, {}, 0, None
+    for tau_d in (0.25, 0.35, 0.45):
+        f = A.FKParams.from_buffer_copy(fk)
+        f.tau_d = tau_d
+        m = Monodomain(q, A.YH_MODEL_FK3V, f)
+        m.set_state(*st)
+        m.sr_begin(A.YH_TEMPLATE_FROZEN, template=st)
+        for _ in range(args.warmup):
+            m.sr_step(nsr // 4)
+        m.synchronize()
+        if tau_d == 0.25:
+            clocks = ClockSampler(env_int("LOCAL_RANK", 0))
+            clocks.start()
+        wall, nl = timed(m, K)
+        if tau_d == 0.25:
+            clk = clocks.stop()
+            launches = nl
+        sym = m.get_sym()
+        rates[tau_d] = K * nsr / wall
+        status[tau_d] = dict(status=sym.status, c=[round(x, 6) for x in sym.c],
+                             ntips=sym.ntips)
+        m.close()
+    # the template retaken every step
+    m = Monodomain(q, A.YH_MODEL_FK3V, fk)
+    m.set_state(*st)
+    m.sr_begin(A.YH_TEMPLATE_CURRENT)
+    m.sr_step(nsr // 4)
+    m.synchronize()
+    wall, _ = timed(m, 1)
+    current = nsr / wall
+    # end to end: the state from pinned host memory each step, the state and
+    # the drift/rotation read back at its end
+    hst = [torch.from_numpy(np.ascontiguousarray(x, np.float32)).pin_memory()
+           for x in st]
+    m.sr_begin(A.YH_TEMPLATE_FROZEN, template=st)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        m.set_state(*[x.numpy() for x in hst])
+        m.sr_step(nsr)
+        m.get_state()
+        m.get_sym()
+    e2e = K * nsr / (time.perf_counter() - t0)
+    m.close()
+    # like for like with the reference: REF2V FP64 through the drop-in
+    r = A.param_defaults(n, n)
+    r.Lx = r.Ly = 3.0 * n / 256
+    r.hx = r.hy = r.Lx / (n - 1)
+    r = sr_params(r, (n / 2, n / 2))
+    u, v = W.ref2v_cross(n, n)
+    cp = Compat()
+    cp.set_params(r)
+    gin = [torch.tensor(np.asarray(x, np.float64), device="cuda") for x in (u, v)]
+    sr_driver(cp, r, gin, 5)
+    torch.cuda.synchronize()
+    k = 60
+    t0 = time.perf_counter()
+    sr_driver(cp, r, gin, k, count0=5)
+    torch.cuda.synchronize()
+    compat_rate = k / (time.perf_counter() - t0)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        m0 = O.SR(q, A.YH_MODEL_FK3V, fk, st, template_mode=A.YH_TEMPLATE_FROZEN,
+                  template=st)
+        t0 = time.perf_counter()
+        ks = 0
+        while time.perf_counter() - t0 < 10.0:
+            m0.step(5)
+            ks += 5
+        cpu = {"value": round(ks / (time.perf_counter() - t0), 3),
+               "unit": "SR steps/s", "cores": 1, "kind": "port",
+               "sample": "%d SR steps of the same 512^2 FK3V case in FP64 "
+                         "(oracle/oracle.c, one thread)" % ks}
+    v = rates[0.25]
+    line = {
+        "metric": "SR steps/s", "value": round(v, 2), "unit": "SR steps/s",
+        "n_gpus": 1, "steps": K, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * nsr / v, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 state, f64 integrals and solve", "data": "synthetic",
+        "config": {"workload": "fk_sr_512", "grid": [n, n], "model": "FK3V",
+                   "tau_d": 0.25, "sr_steps_per_step": nsr,
+                   "sr_steps_timed": K * nsr, "template": "frozen, the "
+                   "re-entry at 1000 ms (S2 at 430 ms: at 320 ms the "
+                   "tissue is still refractory)", "start_tips": len(tips),
+                   "disc_radius_cells": 160, "dt_ms": q.dt,
+                   "l2": "state 3 MB: L2-resident (SR steps are latency-bound)",
+                   "parallelism": "replicas x1"},
+        "gcell_steps_per_s": round(v * N / 1e9, 3),
+        "tau_d_sweep": {str(k): round(x, 2) for k, x in rates.items()},
+        "sym": {str(k): x for k, x in status.items()},
+        "current_template": {"value": round(current, 2), "unit": "SR steps/s"},
+        "compat_fp64_reference_sequence": {
+            "value": round(compat_rate, 2), "unit": "SR steps/s",
+            "model": "REF2V FP64",
+            "sequence": "main.cu:894-954 through the drop-in symbols from "
+                        "Python: 12 integral read-backs and a host solve "
+                        "per step, as the reference"},
+        "roofline": None, "cpu_baseline": cpu,
+        "e2e": {"value": round(e2e, 2), "unit": "SR steps/s",
+                "h2d_bytes_per_step": 3 * 4 * N,
+                "d2h_bytes_per_step": 3 * 4 * N + C.sizeof(A.SymState)},
+        "gpu_launches": int(launches), "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_sr_reference(args):
+    """The reference's own kernels in its symmetry-reduced sequence
+    (main.cu:894-954; REF2V FP64, 512^2), headless."""
+    try:
+        import torch
+        from oracle import oracle as O
+        from oracle import refgpu as R
+    except Exception as e:
+        print(json.dumps({"impl": "reference", "unavailable": str(e)}), flush=True)
+        return
+    if not torch.cuda.is_available() or not R.available():
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "no GPU or the reference kernels are not built"}), flush=True)
+        return
+    from yolohtli_gb300 import _abi as A
+    from yolohtli_gb300 import workloads as W
+    n = 512
+    r = A.param_defaults(n, n)
+    r.Lx = r.Ly = 3.0 * n / 256
+    r.hx = r.hy = r.Lx / (n - 1)
+    r = sr_params(r, (n / 2, n / 2))
+    u, v = W.ref2v_cross(n, n)
+    gin = [torch.tensor(np.asarray(x, np.float64), device="cuda") for x in (u, v)]
+    R.sr_driver(r, gin, 5, O.solve)
+    k = 60
+    t0 = time.perf_counter()
+    R.sr_driver(r, gin, k, O.solve, count0=5)
+    rate = k / (time.perf_counter() - t0)
+    print(json.dumps({
+        "impl": "reference", "metric": "SR steps/s", "value": round(rate, 2),
+        "unit": "SR steps/s", "n_gpus": args.gpus, "steps": 1, "warmup": 1,
+        "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "fk_sr_512", "grid": [n, n],
+                   "model": "REF2V FP64 (the reference's model; it has no FK3V)"},
+        "reference_gpu": {"value": round(rate, 2), "unit": "SR steps/s",
+                          "sequence": "main.cu:894-954 on the reference's "
+                                      "kernels: RD, tips, slices, 12 trapz "
+                                      "launches each read back, host solve, "
+                                      "Cxy, BFECC"},
+        "cpu_baseline": None,
+        "e2e": {"value": round(rate, 2), "unit": "SR steps/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
+
+
 def run_adjoint(args):
     """The adjoint workload (fk_adjoint_512: 512^2 FK3V, D(x, y) of 8
     Gaussian bumps in [5e-4, 1.5e-3], 10,000 steps, the loss on a 32 x 32
@@ -534,7 +754,7 @@ def main():
                     help="explicit steps per solve (default: the workload's, "
                          "20,000 for fk_holes_1024, 5,000 for batch256)")
     ap.add_argument("--workload", default="holes1024",
-                    choices=["holes1024", "batch256", "adjoint512"],
+                    choices=["holes1024", "batch256", "adjoint512", "sr512"],
                     help="holes1024: one 1024^2 grid with 300 holes (the "
                          "headline); batch256: 256 grids of 128^2..768^2 "
                          "through the batched solver")
@@ -545,6 +765,14 @@ def main():
     args = ap.parse_args()
 
     from yolohtli_gb300 import workloads as W
+    if args.workload == "sr512":
+        if args.nsteps is None:
+            args.nsteps = 8000  # x 5 steps = the 40,000 SR steps of the case
+        if args.impl == "reference":
+            run_sr_reference(args)
+        else:
+            run_sr(args)
+        return
     if args.workload == "adjoint512":
         if args.nsteps is None:
             args.nsteps = 10000

@@ -165,3 +165,39 @@ def sapd(count, uold, unew, apd1, apd2, sapd_, dapd, back, front, first,
                         _ptr(apd1), _ptr(apd2), _ptr(sapd_), _ptr(dapd),
                         _ptr(back), _ptr(front), _ptr(first), _ptr(stim_area),
                         1 if stimulate else 0))
+
+
+def sr_driver(p, gin, nsteps, solve, count0=0):
+    """The reference's symmetry-reduced steps (main.cu:894-954) on its own
+    kernels: RD, tips, slices, the 12 integrals (12 launches, each read
+    back), the host 3x3 solve (`solve(I, phi)`, the oracle's restatement
+    of solve_matrix), the comoving field, one BFECC launch and phi += dt c.
+    gin: FP64 (u, v) device tensors, advanced in place. Returns (c, phi)."""
+    import torch
+    n = p.nx * p.ny
+
+    def z(k):
+        return [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(k)]
+
+    gout, J, vt = z(2), z(2), z(2)
+    s, s0, adv = z(6), z(6), z(2)
+    uf, ub, ue = z(2), z(2), z(2)
+    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    vec = torch.zeros(5 * 500000, dtype=torch.float32, device="cuda")
+    plot = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    intgl = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    c, phi = [0.0, 0.0, 0.0], [0.0, 0.0, 0.0]
+    set_params(p)
+    for count in range(count0, count0 + nsteps):
+        rd(p, gout, gin, J, vt, reduce_sym=True)
+        cnt.zero_()
+        tip(p, gin[0], gout[0], plot, cnt, vec, p.dt * count)
+        for _ in range(2 if count == 0 else 1):
+            slice_(p, gin, s, s0, adv[0], adv[1], intgl, cnt, vec, count)
+            I = integrals(p, s, s0, vt, cnt, vec, count)
+            c = list(solve(I, phi))
+            cxy(p, adv[0], adv[1], c, phi)
+        bfecc(p, gin, gout, adv[0], adv[1], uf, ub, ue)
+        phi = [phi[k] + c[k] * p.dt for k in range(3)]
+    sync()
+    return c, phi

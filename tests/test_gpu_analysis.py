@@ -13,7 +13,7 @@ from yolohtli_gb300 import _abi as A
 from yolohtli_gb300 import ops
 
 from gpu_util import dev, host
-from test_gpu_compat import B2, Compat, Dim3, G2, StateVar, sv
+from yolohtli_gb300.compat import B2, Compat, Dim3, G2, StateVar, sv
 
 pytestmark = [pytest.mark.gpu,
               pytest.mark.skipif(not R.available(),

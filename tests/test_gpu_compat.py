@@ -19,86 +19,8 @@ pytestmark = [pytest.mark.gpu,
                                  reason="reference cubin not built (oracle/ref_build.sh)")]
 
 
-class Dim3(C.Structure):
-    _fields_ = [("x", C.c_uint), ("y", C.c_uint), ("z", C.c_uint)]
-
-
-class StateVar(C.Structure):
-    _fields_ = [("u", C.c_void_p), ("v", C.c_void_p)]
-
-
-class AdvVar(C.Structure):
-    _fields_ = [("x", C.c_void_p), ("y", C.c_void_p)]
-
-
-class SliceVar(C.Structure):
-    _fields_ = [(n, C.c_void_p) for n in ("ux", "uy", "ut", "vx", "vy", "vt")]
-
-
-class Real3(C.Structure):
-    _fields_ = [("x", C.c_double), ("y", C.c_double), ("t", C.c_double)]
-
-
-class Int2(C.Structure):
-    _fields_ = [("x", C.c_int), ("y", C.c_int)]
-
-
-SYMBOLS = {
-    "rd": "_Z25reactionDiffusion_wrapperm4dim3S_8stateVarS0_S0_S0_bPbbPdb4int2",
-    "tip": "_Z11tip_wrapperm4dim3S_8stateVarS0_S0_dibPbPiP7vec5dyn",
-    "slice": "_Z13slice_wrapperm4dim3S_8stateVar8sliceVarS1_bb6advVariPbPiP7vec5dyni",
-    "cxy": "_Z17Cxy_field_wrapperm4dim3S_6advVar5REAL3S1_Pb",
-    "bfecc": "_Z18advFDBFECC_wrapperm4dim3S_8stateVarS0_6advVarS0_S0_S0_Pb",
-    "solve": "_Z12solve_matrix5REAL3S_Pd",
-    "trapz": "_Z13trapz_wrapper4dim3S_8sliceVarS0_8stateVarPdS2_PiP7vec5dyni",
-}
-
-_v, _b, _z = C.c_void_p, C.c_bool, C.c_size_t
-
-
-class Compat:
-    """The seven symbols with their C++ signatures (hostPrototypes.h:22-42)."""
-
-    def __init__(self):
-        lib = load()
-        f = {k: getattr(lib, v) for k, v in SYMBOLS.items()}
-        f["rd"].argtypes = [_z, Dim3, Dim3, StateVar, StateVar, StateVar, StateVar,
-                            _b, _v, _b, _v, _b, Int2]
-        f["tip"].argtypes = [_z, Dim3, Dim3, StateVar, StateVar, StateVar,
-                             C.c_double, C.c_int, _b, _v, _v, _v]
-        f["slice"].argtypes = [_z, Dim3, Dim3, StateVar, SliceVar, SliceVar, _b, _b,
-                               AdvVar, C.c_int, _v, _v, _v, C.c_int]
-        f["cxy"].argtypes = [_z, Dim3, Dim3, AdvVar, Real3, Real3, _v]
-        f["bfecc"].argtypes = [_z, Dim3, Dim3, StateVar, StateVar, AdvVar, StateVar,
-                               StateVar, StateVar, _v]
-        f["solve"].argtypes = [Real3, Real3, C.POINTER(C.c_double)]
-        f["solve"].restype = Real3
-        f["trapz"].argtypes = [Dim3, Dim3, SliceVar, SliceVar, StateVar,
-                               C.POINTER(C.c_double), _v, _v, _v, C.c_int]
-        for k in f:
-            if k != "solve":
-                f[k].restype = None
-        self.f = f
-        self.lib = lib
-        lib.yh_compat_set_params.argtypes = [C.POINTER(A.ParamVar)]
-        lib.yh_compat_last_error.restype = C.c_int
-
-    def set_params(self, p):
-        assert self.lib.yh_compat_set_params(C.byref(p)) == 0
-
-    def err(self):
-        return self.lib.yh_compat_last_error()
-
-
-def sv(a, b):
-    return StateVar(a.data_ptr(), b.data_ptr())
-
-
-def slv(ts):
-    return SliceVar(*[t.data_ptr() for t in ts])
-
-
-G2, B2 = Dim3(1, 1, 1), Dim3(16, 16, 1)
+from yolohtli_gb300.compat import (  # noqa: E402,F401
+    B2, G2, AdvVar, Compat, Dim3, Int2, Real3, SliceVar, StateVar, slv, sv)
 
 
 def zeros(n, k, dtype=None):

@@ -2,10 +2,32 @@
 #pragma once
 
 #include <type_traits>
+#include <utility>
 
 #include "yh_common.cuh"
 
 namespace yh {
+
+// Launch with programmatic stream serialization: the kernel's blocks may be
+// scheduled while the previous kernel on the stream drains. Every kernel
+// launched this way calls grid_dep_wait() as its first statement, so it
+// still starts its work only after its predecessor has completed, and the
+// chain stays ordered.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block,
+                              size_t smem, cudaStream_t s, Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 template <typename Real>
 inline bool aligned16(const Fld<Real> &x, int model) {
@@ -109,6 +131,17 @@ cudaError_t launch_phase(const yh_param_var &p, int nf, const Fld<Real> &st,
                          const double *adv_rows, const double *adv_cols,
                          const uint8_t *solid, yh_sym_state *sym,
                          void *workspace, cudaStream_t s);
+// The phase launch of the FP32 symmetry-reduced step: upwinds by the FP32
+// comoving field adv_rows/adv_cols and, in its last block, rewrites that
+// field from the new c (the comoving launch folded in); with `advance`
+// also phi += dt*c, step += 1.
+cudaError_t launch_phase_comoving(const yh_param_var &p, int nf,
+                                  const Fld<float> &st, const Fld<float> &tan,
+                                  const Fld<float> &tx, const Fld<float> &ty,
+                                  const Fld<float> &tt, float *adv_rows,
+                                  float *adv_cols, const uint8_t *solid,
+                                  yh_sym_state *sym, void *workspace,
+                                  bool advance, cudaStream_t s);
 template <typename Real>
 cudaError_t launch_template(const yh_param_var &p, int nf,
                             const Fld<Real> &st, const Fld<Real> &tx,
@@ -138,9 +171,9 @@ cudaError_t launch_bfecc_2d(const yh_param_var &p, int nf,
 // I[3r+2]] . c = I[9+r]  (symmetryReduction.cu:390-396). Returns YH_OK, or
 // YH_ESINGULAR when a pivot is below 1e-13 of the largest entry (the
 // reference divides by unpivoted entries, symmetryReduction.cu:398-412).
-__host__ __device__ inline int solve3(const double I[12], double pt,
-                                      double c[3]) {
-  const double cs = cos(pt), sn = sin(pt);
+// solve3 with cos(pt), sin(pt) given.
+__host__ __device__ inline int solve3_cs(const double I[12], double cs,
+                                         double sn, double c[3]) {
   double A[3][4];
   double amax = 0.0;
   for (int r = 0; r < 3; ++r) {
@@ -176,6 +209,10 @@ __host__ __device__ inline int solve3(const double I[12], double pt,
   }
   for (int k = 0; k < 3; ++k) c[k] = x[k];
   return YH_OK;
+}
+__host__ __device__ inline int solve3(const double I[12], double pt,
+                                      double c[3]) {
+  return solve3_cs(I, cos(pt), sin(pt), c);
 }
 cudaError_t launch_sym_advance(const yh_param_var &p, yh_sym_state *sym,
                                cudaStream_t s);

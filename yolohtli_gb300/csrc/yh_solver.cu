@@ -632,7 +632,6 @@ static cudaError_t enqueue_sr_step(yh_solver *h, bool first) {
   const Fld<float> tx = h->frozen ? h->tx : none;
   const Fld<float> ty = h->frozen ? h->ty : none;
   const Fld<float> tt = h->frozen ? h->tt : none;
-  double *adv_rows = h->adv_d, *adv_cols = h->adv_d + h->p.ny;
   float *advf_rows = h->adv_f, *advf_cols = h->adv_f + h->p.ny;
   cudaError_t e = cudaMemsetAsync(h->tip_count, 0, sizeof(int), h->s);
   if (e == cudaSuccess)  // 1. RD with tangent: cur -> nxt
@@ -642,19 +641,18 @@ static cudaError_t enqueue_sr_step(yh_solver *h, bool first) {
     e = launch_tips<float>(h->p, h->nxt.f[0], h->cur.f[0], h->p.solidSwitch, 0.0,
                            h->tip_count, h->tips, kTipCapacity, h->sym,
                            h->tip_done, h->s);
-  const int reps = first ? 2 : 1;  // main.cu:910-926
-  for (int r = 0; r < reps && e == cudaSuccess; ++r) {
-    e = launch_phase<float>(h->p, h->nf, h->cur, h->tan, tx, ty, tt, adv_rows,
-                            adv_cols, h->solid, h->sym, h->ws, h->s);
-    if (e == cudaSuccess)
-      e = launch_comoving(h->p, h->sym, adv_rows, adv_cols, advf_rows,
-                          advf_cols, r == reps - 1, h->s);
-  }
+  // phase integrals + solve + comoving field, twice on the first step
+  // (main.cu:910-926)
+  const int reps = first ? 2 : 1;
+  for (int r = 0; r < reps && e == cudaSuccess; ++r)
+    e = launch_phase_comoving(h->p, h->nf, h->cur, h->tan, tx, ty, tt,
+                              advf_rows, advf_cols, h->solid, h->sym, h->ws,
+                              r == reps - 1, h->s);
   if (e == cudaSuccess)  // BFECC: nxt -> cur
     e = launch_bfecc<float>(h->p, h->nf, h->nxt, h->cur, advf_rows, advf_cols,
                             h->solid, h->uf, h->ue, h->s);
-  // RD, tips, (phase, comoving) x reps, 3 BFECC passes
-  if (e == cudaSuccess) h->launches += 2 + 2 * reps + 3;
+  // RD, tips, phase x reps, 3 BFECC passes
+  if (e == cudaSuccess) h->launches += 2 + reps + 3;
   return e;
 }
 

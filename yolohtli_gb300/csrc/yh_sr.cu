@@ -3,10 +3,11 @@
 //                  (spiralTip_kernel, tipTracker.cu:20-241) + the disc-centre
 //                  choice in the last block;
 //   phase_kernel   slices (symmetryReduction.cu:72-262) fused with the 12
-//                  phase integrals (integralTrapz.cu:17-184) in FP64 and the
-//                  FP64 3x3 solve (symmetryReduction.cu:329-420) in the last
+//                  phase integrals (integralTrapz.cu:17-184) and the FP64
+//                  3x3 solve (symmetryReduction.cu:329-420) in the last
 //                  block: one launch instead of 2 + 12 launches, 12 blocking
-//                  copies and a host solve;
+//                  copies and a host solve; in the symmetry-reduced step
+//                  the last block also writes the comoving field;
 //   comoving_kernel the comoving field (Cxy_field_kernel,
 //                  symmetryReduction.cu:20-62), which is separable: adv.x
 //                  depends on the row, adv.y on the column, so it is two
@@ -14,8 +15,11 @@
 //   bfecc_pass1/2/3 BFECC advection (advFDBFECC.cu:18-353) as three passes,
 //                  so no thread reads a neighbour written in the same launch.
 //
-// Reductions are deterministic: per-thread FP64 accumulators, warp shuffles,
-// per-block partials, and a fixed-order sum by the last block to finish.
+// Reductions are deterministic: per-thread accumulators (float-float pairs
+// for FP32 fields, doubles for FP64 fields), warp shuffles, per-block
+// partials, a fixed-order sum by the last block to finish, FP64 from the
+// 12 block-summed integrals on. The tip, phase and BFECC kernels are
+// launched with programmatic stream serialization.
 #include "yh_kernels.cuh"
 
 namespace yh {
@@ -246,62 +250,113 @@ __device__ void pick_centre_block(int t, const int *count, const yh_tip *vec,
 // HOLES: the disc around the grid centre, all cells (tipTracker.cu:47-122,
 // :262-266); otherwise, closed form (ALG 1): i in [1,nx-3], j in [1,ny-3]
 // (tipTracker.cu:124-204), Newton (ALG 2): the 2 tipOffset window around
-// the grid centre (tipTracker.cu:339-341). For FP32 fields the closed form
-// skips a cell early when the threshold lies outside the corner range of
-// either level: a bilinear interpolant on the unit cell stays within its
-// corner values, so no root of x = Uth, y = Uth can lie inside such a cell.
+// the grid centre (tipTracker.cu:339-341).
+template <bool HOLES, int ALG>
+__device__ __forceinline__ bool tip_active(const TipArgs &a, int i, int j) {
+  const int nx = a.nx, ny = a.ny;
+  if (HOLES) {
+    const int ic = i - nx / 2, jc = j - ny / 2;
+    return i < nx && j < ny && (ic * ic + jc * jc) < a.r2;
+  }
+  if (ALG == 1) return (i >= 1) && (i < nx - 2) && (j >= 1) && (j < ny - 2);
+  return i < nx && j < ny && i >= nx / 2 - a.tox && i < nx / 2 + a.tox &&
+         j >= ny / 2 - a.toy && j < ny / 2 + a.toy;
+}
+
+// Corners of cell (i, j): x = present, y = past, in the order (i,j),
+// (i+1,j), (i+1,j+1), (i,j+1) (tipTracker.cu:140-174), clamped at the edge.
+template <typename Real>
+__device__ __forceinline__ void tip_corners(const TipArgs &a, const Real *past,
+                                            const Real *present, int i, int j,
+                                            Real x[4], Real y[4]) {
+  const int nx = a.nx, ny = a.ny;
+  const int s0 = i + nx * j;
+  const int sx = (i < nx - 1) ? s0 + 1 : s0;
+  const int sy = (j < ny - 1) ? s0 + nx : s0;
+  const int sxy = ((j < ny - 1) && (i < nx - 1)) ? s0 + nx + 1 : s0;
+  x[0] = present[s0];
+  x[1] = present[sx];
+  x[2] = present[sxy];
+  x[3] = present[sy];
+  y[0] = past[s0];
+  y[1] = past[sx];
+  y[2] = past[sxy];
+  y[3] = past[sy];
+}
+
+constexpr int kTipRows = 4;  // FP32 closed form: cells per thread, 8 rows apart
+
+// FP32 closed form: a cell is a candidate when the threshold lies within
+// the corner range of both levels (a bilinear interpolant on the unit cell
+// stays within its corner values, so no root of x = Uth, y = Uth lies
+// inside any other cell). A block scans a 32x32 tile, gathers its
+// candidates in shared memory and runs the FP64 intersection on them with
+// full warps: GB300 issues FP64 at a small fraction of its FP32 rate and a
+// warp pays for an FP64 instruction whatever its active lanes, so a
+// candidate per warp would cost a whole warp's FP64 time each. Other
+// forms (FP64 levels, Newton) keep one thread per cell.
 template <typename Real, bool HOLES, int ALG, bool GRAD>
 __global__ void __launch_bounds__(256)
     tip_kernel(const TipArgs a, const Real *__restrict__ past,
                const Real *__restrict__ present, int *count, yh_tip *vec,
                int cap, yh_sym_state *sym, unsigned int *done, uint8_t *plot) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int nx = a.nx, ny = a.ny;
+  grid_dep_wait();
+  constexpr bool COMPACT = sizeof(Real) == 4 && ALG == 1;
+  const int i = blockIdx.x * 32 + threadIdx.x;
+  const int t = threadIdx.x + 32 * threadIdx.y;
   const float ptime =
       sym ? (float)(a.dt * (double)sym->step) : (float)a.ptime;
-  bool active;
-  if (HOLES) {
-    const int ic = i - nx / 2, jc = j - ny / 2;
-    active = i < nx && j < ny && (ic * ic + jc * jc) < a.r2;
-  } else if (ALG == 1) {
-    active = (i >= 1) && (i < nx - 2) && (j >= 1) && (j < ny - 2);
-  } else {
-    active = i < nx && j < ny && i >= nx / 2 - a.tox && i < nx / 2 + a.tox &&
-             j >= ny / 2 - a.toy && j < ny / 2 + a.toy;
-  }
-  if (active) {
-    const int s0 = i + nx * j;
-    const int sx = (i < nx - 1) ? s0 + 1 : s0;
-    const int sy = (j < ny - 1) ? s0 + nx : s0;
-    const int sxy = ((j < ny - 1) && (i < nx - 1)) ? s0 + nx + 1 : s0;
-    const Real x1 = present[s0], x2 = present[sx], x4 = present[sy],
-               x3 = present[sxy];
-    const Real y1 = past[s0], y2 = past[sx], y4 = past[sy], y3 = past[sxy];
-    if (ALG == 2) {
-      tip_cell_newton<GRAD>(a, i, j, x1, x2, x3, x4, y1, y2, y3, y4, ptime,
-                            present, count, vec, cap, plot);
-    } else {
-      bool cand = true;
-      if (sizeof(Real) == 4) {
-        const float th = (float)a.Uth, tol = 1e-5f;
-        const float xmn = fminf(fminf(x1, x2), fminf(x3, x4));
-        const float xmx = fmaxf(fmaxf(x1, x2), fmaxf(x3, x4));
-        const float ymn = fminf(fminf(y1, y2), fminf(y3, y4));
-        const float ymx = fmaxf(fmaxf(y1, y2), fmaxf(y3, y4));
-        cand = th >= xmn - tol && th <= xmx + tol && th >= ymn - tol &&
-               th <= ymx + tol;
+  if (COMPACT) {
+    __shared__ int s_n;
+    __shared__ short2 s_cell[256 * kTipRows];
+    if (t == 0) s_n = 0;
+    __syncthreads();
+    const float th = (float)a.Uth, tol = 1e-5f;
+#pragma unroll
+    for (int m = 0; m < kTipRows; ++m) {
+      const int j = blockIdx.y * 8 * kTipRows + threadIdx.y + 8 * m;
+      if (!tip_active<HOLES, ALG>(a, i, j)) continue;
+      Real x[4], y[4];
+      tip_corners(a, past, present, i, j, x, y);
+      const float xmn = fminf(fminf(x[0], x[1]), fminf(x[2], x[3]));
+      const float xmx = fmaxf(fmaxf(x[0], x[1]), fmaxf(x[2], x[3]));
+      const float ymn = fminf(fminf(y[0], y[1]), fminf(y[2], y[3]));
+      const float ymx = fmaxf(fmaxf(y[0], y[1]), fmaxf(y[2], y[3]));
+      if (th >= xmn - tol && th <= xmx + tol && th >= ymn - tol &&
+          th <= ymx + tol) {
+        const int k = atomicAdd(&s_n, 1);
+        s_cell[k] = make_short2((short)(threadIdx.x), (short)(threadIdx.y + 8 * m));
       }
-      if (cand)
-        tip_cell<GRAD>(a, i, j, x1, x2, x3, x4, y1, y2, y3, y4, !HOLES, ptime,
-                       present, count, vec, cap, plot);
+    }
+    __syncthreads();
+    const int n = s_n;
+    for (int k = t; k < n; k += 256) {
+      const int ci = blockIdx.x * 32 + s_cell[k].x;
+      const int cj = blockIdx.y * 8 * kTipRows + s_cell[k].y;
+      Real x[4], y[4];
+      tip_corners(a, past, present, ci, cj, x, y);
+      tip_cell<GRAD>(a, ci, cj, x[0], x[1], x[2], x[3], y[0], y[1], y[2],
+                     y[3], !HOLES, ptime, present, count, vec, cap, plot);
+    }
+  } else {
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    if (tip_active<HOLES, ALG>(a, i, j)) {
+      Real x[4], y[4];
+      tip_corners(a, past, present, i, j, x, y);
+      if (ALG == 2)
+        tip_cell_newton<GRAD>(a, i, j, x[0], x[1], x[2], x[3], y[0], y[1],
+                              y[2], y[3], ptime, present, count, vec, cap,
+                              plot);
+      else
+        tip_cell<GRAD>(a, i, j, x[0], x[1], x[2], x[3], y[0], y[1], y[2],
+                       y[3], !HOLES, ptime, present, count, vec, cap, plot);
     }
   }
   if (sym == nullptr) return;
   // Last block to finish chooses the disc centre.
   __shared__ bool s_last;
   __syncthreads();
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
+  if (t == 0) {
     __threadfence();
     const unsigned nb = gridDim.x * gridDim.y;
     s_last = atomicAdd(done, 1u) == nb - 1;
@@ -309,7 +364,6 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  const int t = threadIdx.x + blockDim.x * threadIdx.y;
   if (t == 0) *done = 0u;
   pick_centre_block(t, count, vec, cap, sym);
 }
@@ -342,15 +396,14 @@ cudaError_t launch_tips(const yh_param_var &p, const Real *past,
   a.invdy = p.invdy;
   a.dt = p.dt;
   a.ptime = ptime;
-  const dim3 block(32, 8);
-  const dim3 grid((p.nx + 31) / 32, (p.ny + 7) / 8);
   const bool newton = p.tipAlgorithm == 2, grad = p.tipGrad;
+  const int rows = (sizeof(Real) == 4 && !newton) ? 8 * kTipRows : 8;
+  const dim3 block(32, 8);
+  const dim3 grid((p.nx + 31) / 32, (p.ny + rows - 1) / rows);
 #define YH_TIP(H, ALG, G)                                                   \
-  if (holes == H && newton == (ALG == 2) && grad == G) {                    \
-    tip_kernel<Real, H, ALG, G><<<grid, block, 0, s>>>(                     \
-        a, past, present, count, vec, cap, sym_pick, done, plot);           \
-    return cudaGetLastError();                                             \
-  }
+  if (holes == H && newton == (ALG == 2) && grad == G)                      \
+    return launch_pdl(tip_kernel<Real, H, ALG, G>, grid, block, 0, s, a,     \
+                      past, present, count, vec, cap, sym_pick, done, plot);
   YH_TIP(true, 1, false)
   YH_TIP(true, 1, true)
   YH_TIP(true, 2, false)
@@ -380,15 +433,116 @@ struct PhaseArgs {
   double hxhy;
 };
 
-constexpr int kPhaseBX = 32, kPhaseBY = 8;
+// The comoving field computed by the last block of the phase launch from
+// the c it has just solved for (the work of comoving_kernel, in FP32, for
+// the FP32 BFECC), then phi += dt*c and step += 1 when `advance`.
+struct PhaseTail {
+  float *rows, *cols;  // null: no comoving field, no advance
+  float hx, hy;
+  double dt;
+  int advance;
+};
 
-// 2nd-order one-sided derivative, upwinded by the sign of adv
-// (convFB2ndOX/Y, symmetryReduction.cu:242-262).
+constexpr int kPhaseBX = 32, kPhaseBY = 8;
+constexpr int kPhaseRows = 2;  // cells per thread, 8 rows apart: 32x16 tiles
+
+// Phase-integral accumulators. FP32 fields: float-float pairs hi + lo kept
+// exact by Knuth's TwoSum (The Art of Computer Programming vol. 2, 4.2.2),
+// about 48 significant bits on the FP32 pipe. GB300 issues FP64 at a small
+// fraction of its FP32 rate; a per-cell FP64 sum and shuffle tree made this
+// launch FP64-bound. FP64 fields: plain doubles. Both store in 8 bytes.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  const float ap = __fsub_rn(s, bp);
+  e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+}
+
+struct AccF {
+  float hi, lo;
+  __device__ __forceinline__ void set(float v) {
+    hi = v;
+    lo = 0.f;
+  }
+  __device__ __forceinline__ void add(const AccF &b) {
+    float s, e;
+    two_sum(hi, b.hi, s, e);
+    e = __fadd_rn(e, __fadd_rn(lo, b.lo));
+    two_sum(s, e, hi, lo);
+  }
+  __device__ __forceinline__ void add(float v) {
+    AccF b;
+    b.set(v);
+    add(b);
+  }
+  __device__ __forceinline__ AccF down(int off, int width) const {
+    AccF r;
+    r.hi = __shfl_down_sync(0xffffffffu, hi, off, width);
+    r.lo = __shfl_down_sync(0xffffffffu, lo, off, width);
+    return r;
+  }
+  __device__ __forceinline__ double value() const {
+    return (double)hi + (double)lo;
+  }
+  __device__ __forceinline__ void store(double *p) const {
+    *reinterpret_cast<float2 *>(p) = make_float2(hi, lo);
+  }
+  __device__ __forceinline__ static AccF load(const double *p) {
+    const float2 v = __ldcg(reinterpret_cast<const float2 *>(p));
+    AccF r;
+    r.hi = v.x;
+    r.lo = v.y;
+    return r;
+  }
+};
+
+struct AccD {
+  double v;
+  __device__ __forceinline__ void set(double x) { v = x; }
+  __device__ __forceinline__ void add(const AccD &b) { v += b.v; }
+  __device__ __forceinline__ void add(double x) { v += x; }
+  __device__ __forceinline__ AccD down(int off, int width) const {
+    AccD r;
+    r.v = __shfl_down_sync(0xffffffffu, v, off, width);
+    return r;
+  }
+  __device__ __forceinline__ double value() const { return v; }
+  __device__ __forceinline__ void store(double *p) const { *p = v; }
+  __device__ __forceinline__ static AccD load(const double *p) {
+    AccD r;
+    r.v = __ldcg(p);
+    return r;
+  }
+};
+
+template <typename Real>
+struct AccOf {
+  using T = AccD;
+};
+template <>
+struct AccOf<float> {
+  using T = AccF;
+};
+
+// v > 0 from the bits, with no floating-point compare: an FP64 compare
+// issues on GB300's narrow FP64 pipe. Equal to v > 0 for every input,
+// NaN included.
+__device__ __forceinline__ bool adv_pos(double v) {
+  const long long b = __double_as_longlong(v);
+  return b > 0 && b <= 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool adv_pos(float v) {
+  const int b = __float_as_int(v);
+  return b > 0 && b <= 0x7f800000;
+}
+
+// 2nd-order one-sided derivative, upwinded by the sign of the comoving
+// field (convFB2ndOX/Y, symmetryReduction.cu:242-262).
 template <typename Real>
 __device__ __forceinline__ Real fb2(Real c, Real p1, Real p2, Real m1, Real m2,
-                                    double adv, Real inv) {
-  return adv > 0.0 ? (Real(-3) * c + Real(4) * p1 - p2) * inv
-                   : (Real(3) * c - Real(4) * m1 + m2) * inv;
+                                    bool pos, Real inv) {
+  return pos ? (Real(-3) * c + Real(4) * p1 - p2) * inv
+             : (Real(3) * c - Real(4) * m1 + m2) * inv;
 }
 // Negated 4th-order central derivative (convCentral2X/Y,
 // symmetryReduction.cu:224-240).
@@ -398,82 +552,108 @@ __device__ __forceinline__ Real c4(Real p1, Real p2, Real m1, Real m2,
   return (p2 - Real(8) * p1 + Real(8) * m1 - m2) * inv * Real(1.0 / 6.0);
 }
 
-// One block covers a 32x8 tile of the disc's bounding box, placed by the
-// current disc centre read from `sym` (so a captured graph follows the tip).
-template <int NF, typename Real, bool FROZEN, bool HOLES>
+// The 12 integrands of cell (i, j) when it lies in the disc: templates
+// (x, y, theta) against the slices (x, y, theta) and the tangent,
+// summed over the fields (integralTrapz.cu:17-184 with the slices of
+// symmetryReduction.cu:72-222).
+template <int NF, typename Real, bool FROZEN, bool HOLES, typename AdvT>
+__device__ __forceinline__ bool phase_cell(
+    const PhaseArgs<Real> &a, const Fld<Real> &st, const Fld<Real> &tan,
+    const Fld<Real> &tx, const Fld<Real> &ty, const Fld<Real> &tt,
+    const AdvT *adv_rows, const AdvT *adv_cols,
+    const uint8_t *__restrict__ solid, int i, int j, int cx, int cy,
+    Real s[12]) {
+  const int nx = a.nx, ny = a.ny;
+  if (i < 0 || i >= nx || j < 0 || j >= ny) return false;
+  const int ic = i - nx / 2 - cx, jc = j - ny / 2 - cy;
+  if (ic * ic + jc * jc >= a.r2) return false;
+  const int C = i + nx * j;
+  const bool tissue = !HOLES || solid[C] != 0;
+  const bool px = tissue && adv_pos(adv_rows[j]);
+  const bool py = tissue && adv_pos(adv_cols[i]);
+  const int row = nx * j;
+  const int iE = mirror(i + 1, nx), iW = mirror(i - 1, nx);
+  const int iEE = mirror(i + 2, nx), iWW = mirror(i - 2, nx);
+  const int jN = nx * mirror(j + 1, ny), jS = nx * mirror(j - 1, ny);
+  const int jNN = nx * mirror(j + 2, ny), jSS = nx * mirror(j - 2, ny);
+  const Real x = (Real)i, y = (Real)j;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) s[k] = Real(0);
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    const Real *__restrict__ g = st.f[f];
+    const Real c = g[C];
+    const Real e1 = g[row + iE], e2 = g[row + iEE];
+    const Real w1 = g[row + iW], w2 = g[row + iWW];
+    const Real n1 = g[i + jN], n2 = g[i + jNN];
+    const Real s1 = g[i + jS], s2 = g[i + jSS];
+    const Real dx = fb2(c, e1, e2, w1, w2, px, a.invdx);
+    const Real dy = fb2(c, n1, n2, s1, s2, py, a.invdy);
+    const Real dth = a.hx * x * dy - a.hy * y * dx;
+    Real Tx, Ty, Tt;
+    if (FROZEN) {
+      Tx = tx.f[f][C];
+      Ty = ty.f[f][C];
+      Tt = tt.f[f][C];
+    } else {
+      Tx = c4(e1, e2, w1, w2, a.invdx);
+      Ty = c4(n1, n2, s1, s2, a.invdy);
+      Tt = a.hx * x * Ty - a.hy * y * Tx;
+    }
+    const Real vt = tan.f[f][C];
+    const Real Tv[3] = {Tx, Ty, Tt};
+    const Real Cv[4] = {dx, dy, dth, vt};
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) s[q < 3 ? 3 * p + q : 9 + p] += Tv[p] * Cv[q];
+  }
+  return true;
+}
+
+// One block covers a 32x16 tile of the disc's bounding box, placed by the
+// current disc centre read from `sym` (so a captured graph follows the
+// tip). Per block: 12 partial sums (accumulator pairs); the last block to
+// finish sums them in a fixed order, solves in FP64 and, with a tail, writes
+// the comoving field.
+template <int NF, typename Real, bool FROZEN, bool HOLES, typename AdvT>
 __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
     phase_kernel(const PhaseArgs<Real> a, const Fld<Real> st,
                  const Fld<Real> tan, const Fld<Real> tx, const Fld<Real> ty,
-                 const Fld<Real> tt, const double *__restrict__ adv_rows,
-                 const double *__restrict__ adv_cols,
-                 const uint8_t *__restrict__ solid, yh_sym_state *sym,
-                 double *partials, unsigned int *done) {
+                 const Fld<Real> tt, const AdvT *adv_rows,
+                 const AdvT *adv_cols, const uint8_t *__restrict__ solid,
+                 yh_sym_state *sym, double *partials, unsigned int *done,
+                 const PhaseTail tail) {
+  // adv_rows/adv_cols are not __restrict__: the tail rewrites them
+  using Acc = typename AccOf<Real>::T;
+  grid_dep_wait();
   const int nx = a.nx, ny = a.ny;
   // integer centre as slice_kernel/trapz_kernel round it
   // (symmetryReduction.cu:98-104): float arithmetic, round-half-even.
   const int cx = __float2int_rn(sym->centre[0] - (float)(nx / 2));
   const int cy = __float2int_rn(sym->centre[1] - (float)(ny / 2));
   const int i = nx / 2 + cx - a.R + (int)(blockIdx.x * kPhaseBX + threadIdx.x);
-  const int j = ny / 2 + cy - a.R + (int)(blockIdx.y * kPhaseBY + threadIdx.y);
-  double acc[12];
+  const int j0 = ny / 2 + cy - a.R +
+                 (int)(blockIdx.y * kPhaseBY * kPhaseRows + threadIdx.y);
+  Acc acc[12];
 #pragma unroll
-  for (int k = 0; k < 12; ++k) acc[k] = 0.0;
-  if (i >= 0 && i < nx && j >= 0 && j < ny) {
-    const int ic = i - nx / 2 - cx, jc = j - ny / 2 - cy;
-    if (ic * ic + jc * jc < a.r2) {
-      const int C = i + nx * j;
-      const bool tissue = !HOLES || solid[C] != 0;
-      const double ax = tissue ? adv_rows[j] : 0.0;
-      const double ay = tissue ? adv_cols[i] : 0.0;
-      const int row = nx * j;
-      const int iE = mirror(i + 1, nx), iW = mirror(i - 1, nx);
-      const int iEE = mirror(i + 2, nx), iWW = mirror(i - 2, nx);
-      const int jN = nx * mirror(j + 1, ny), jS = nx * mirror(j - 1, ny);
-      const int jNN = nx * mirror(j + 2, ny), jSS = nx * mirror(j - 2, ny);
-      const Real x = (Real)i, y = (Real)j;
-      Real s[12];
+  for (int k = 0; k < 12; ++k) acc[k].set(Real(0));
 #pragma unroll
-      for (int k = 0; k < 12; ++k) s[k] = Real(0);
+  for (int m = 0; m < kPhaseRows; ++m) {
+    Real s[12];
+    if (phase_cell<NF, Real, FROZEN, HOLES, AdvT>(
+            a, st, tan, tx, ty, tt, adv_rows, adv_cols, solid, i,
+            j0 + m * kPhaseBY, cx, cy, s)) {
 #pragma unroll
-      for (int f = 0; f < NF; ++f) {
-        const Real *__restrict__ g = st.f[f];
-        const Real c = g[C];
-        const Real e1 = g[row + iE], e2 = g[row + iEE];
-        const Real w1 = g[row + iW], w2 = g[row + iWW];
-        const Real n1 = g[i + jN], n2 = g[i + jNN];
-        const Real s1 = g[i + jS], s2 = g[i + jSS];
-        const Real dx = fb2(c, e1, e2, w1, w2, ax, a.invdx);
-        const Real dy = fb2(c, n1, n2, s1, s2, ay, a.invdy);
-        const Real dth = a.hx * x * dy - a.hy * y * dx;
-        Real Tx, Ty, Tt;
-        if (FROZEN) {
-          Tx = tx.f[f][C];
-          Ty = ty.f[f][C];
-          Tt = tt.f[f][C];
-        } else {
-          Tx = c4(e1, e2, w1, w2, a.invdx);
-          Ty = c4(n1, n2, s1, s2, a.invdy);
-          Tt = a.hx * x * Ty - a.hy * y * Tx;
-        }
-        const Real vt = tan.f[f][C];
-        const Real Tv[3] = {Tx, Ty, Tt};
-        const Real Cv[4] = {dx, dy, dth, vt};
-#pragma unroll
-        for (int p = 0; p < 3; ++p)
-#pragma unroll
-          for (int q = 0; q < 4; ++q) s[q < 3 ? 3 * p + q : 9 + p] += Tv[p] * Cv[q];
-      }
-#pragma unroll
-      for (int k = 0; k < 12; ++k) acc[k] = (double)s[k];
+      for (int k = 0; k < 12; ++k) acc[k].add(s[k]);
     }
   }
   // warp tree
 #pragma unroll
   for (int k = 0; k < 12; ++k)
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-      acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
-  __shared__ double s_w[kPhaseBY][12];
+    for (int off = 16; off > 0; off >>= 1) acc[k].add(acc[k].down(off, 32));
+  __shared__ Acc s_w[kPhaseBY][12];
   __shared__ bool s_last;
   const int lane = threadIdx.x;  // blockDim.x == 32
   const int warp = threadIdx.y;
@@ -485,9 +665,9 @@ __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
   const unsigned nb = gridDim.x * gridDim.y;
   const unsigned bid = blockIdx.x + gridDim.x * blockIdx.y;
   if (t < 12) {
-    double v = 0.0;
-    for (int w = 0; w < kPhaseBY; ++w) v += s_w[w][t];
-    partials[(size_t)bid * 12 + t] = v;
+    Acc v = s_w[0][t];
+    for (int w = 1; w < kPhaseBY; ++w) v.add(s_w[w][t]);
+    v.store(&partials[(size_t)bid * 12 + t]);
   }
   __syncthreads();
   if (t == 0) {
@@ -497,36 +677,59 @@ __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  // Last block: fixed-order sum of the block partials, then the solve.
-  __shared__ double s_r[12][kPhaseBX * kPhaseBY / 12 + 1];
-  // 12 groups of 21 threads each sum a strided subset of blocks, in order.
-  constexpr int G = kPhaseBX * kPhaseBY / 12;  // 21
-  const int k = t / G, r = t % G;
-  if (k < 12) {
-    double v = 0.0;
-    for (unsigned b = r; b < nb; b += G)
-      v += ((volatile double *)partials)[(size_t)b * 12 + k];
-    s_r[k][r] = v;
+  // Last block: 12 groups of 16 lanes (warps 0-5), lane r sums the block
+  // partials r, r+16, ... in order, then a 16-lane tree.
+  __shared__ double s_I[12];
+  __shared__ double s_c[3], s_cs, s_sn;
+  if (t < 192) {
+    const int k = t >> 4, r = t & 15;
+    Acc v;
+    v.set(Real(0));
+    for (unsigned b = r; b < nb; b += 16)
+      v.add(Acc::load(&partials[(size_t)b * 12 + k]));
+#pragma unroll
+    for (int off = 8; off > 0; off >>= 1) v.add(v.down(off, 16));
+    if (r == 0) s_I[k] = a.hxhy * v.value();
   }
   __syncthreads();
   if (t == 0) {
     double I[12];
     for (int kk = 0; kk < 12; ++kk) {
-      double v = 0.0;
-      for (int rr = 0; rr < G; ++rr) v += s_r[kk][rr];
-      I[kk] = a.hxhy * v;
+      I[kk] = s_I[kk];
       sym->integrals[kk] = I[kk];
     }
+    // phi_adv = phi: one angle for the solve and the comoving field
+    double sn, cs;
+    sincos(sym->phi[2], &sn, &cs);
     double c[3];
-    const int st = solve3(I, sym->phi[2], c);
-    sym->status = st;
-    if (st == YH_OK)
+    const int stt = solve3_cs(I, cs, sn, c);
+    sym->status = stt;
+    if (stt == YH_OK)
       for (int kk = 0; kk < 3; ++kk) sym->c[kk] = c[kk];
     for (int kk = 0; kk < 3; ++kk) {
+      s_c[kk] = sym->c[kk];
       sym->c_adv[kk] = sym->c[kk];
       sym->phi_adv[kk] = sym->phi[kk];
     }
+    s_cs = cs;
+    s_sn = sn;
     *done = 0u;
+  }
+  if (tail.rows == nullptr) return;
+  __syncthreads();
+  // adv_x[j] = hy*y*ct - cx*cos(pt) + cy*sin(pt);
+  // adv_y[i] = -hx*x*ct - cx*sin(pt) - cy*cos(pt)   (symmetryReduction.cu:55-56)
+  const float fcx = (float)s_c[0], fcy = (float)s_c[1], fct = (float)s_c[2];
+  const float fcs = (float)s_cs, fsn = (float)s_sn;
+  const float r0 = fcy * fsn - fcx * fcs, c0 = -(fcx * fsn + fcy * fcs);
+  const float hyct = tail.hy * fct, hxct = tail.hx * fct;
+  for (int jj = t; jj < ny; jj += kPhaseBX * kPhaseBY)
+    tail.rows[jj] = hyct * (float)jj + r0;
+  for (int ii = t; ii < nx; ii += kPhaseBX * kPhaseBY)
+    tail.cols[ii] = c0 - hxct * (float)ii;
+  if (tail.advance && t == 0) {
+    for (int kk = 0; kk < 3; ++kk) sym->phi[kk] = sym->phi[kk] + s_c[kk] * tail.dt;
+    sym->step += 1;
   }
 }
 
@@ -537,25 +740,27 @@ static void phase_geometry(const yh_param_var &p, int *R, dim3 *grid) {
   // the box never needs to exceed twice the grid
   const int bx = 2 * r + 1 < 2 * p.nx ? 2 * r + 1 : 2 * p.nx;
   const int by = 2 * r + 1 < 2 * p.ny ? 2 * r + 1 : 2 * p.ny;
+  constexpr int TY = kPhaseBY * kPhaseRows;
   *R = r;
-  *grid = dim3((bx + kPhaseBX - 1) / kPhaseBX, (by + kPhaseBY - 1) / kPhaseBY);
+  *grid = dim3((bx + kPhaseBX - 1) / kPhaseBX, (by + TY - 1) / TY);
 }
 
 size_t phase_workspace_bytes(const yh_param_var &p) {
   int R;
   dim3 g;
   phase_geometry(p, &R, &g);
-  // counter (256 B slot) + 12 doubles per block
+  // counter (256 B slot) + 12 accumulators of 8 bytes per block
   return 256 + (size_t)g.x * g.y * 12 * sizeof(double);
 }
 
-template <typename Real>
-cudaError_t launch_phase(const yh_param_var &p, int nf, const Fld<Real> &st,
-                         const Fld<Real> &tan, const Fld<Real> &tx,
-                         const Fld<Real> &ty, const Fld<Real> &tt,
-                         const double *adv_rows, const double *adv_cols,
-                         const uint8_t *solid, yh_sym_state *sym,
-                         void *workspace, cudaStream_t s) {
+template <typename Real, typename AdvT>
+static cudaError_t phase_dispatch(const yh_param_var &p, int nf,
+                                  const Fld<Real> &st, const Fld<Real> &tan,
+                                  const Fld<Real> &tx, const Fld<Real> &ty,
+                                  const Fld<Real> &tt, const AdvT *adv_rows,
+                                  const AdvT *adv_cols, const uint8_t *solid,
+                                  yh_sym_state *sym, void *workspace,
+                                  const PhaseTail &tail, cudaStream_t s) {
   PhaseArgs<Real> a;
   a.nx = p.nx;
   a.ny = p.ny;
@@ -574,12 +779,10 @@ cudaError_t launch_phase(const yh_param_var &p, int nf, const Fld<Real> &st,
   const bool frozen = tx.f[0] != nullptr;
   const bool holes = p.solidSwitch && solid;
 #define YH_PH(NF, FZ, HO)                                                      \
-  if (nf == NF && frozen == FZ && holes == HO) {                               \
-    phase_kernel<NF, Real, FZ, HO><<<grid, block, 0, s>>>(                     \
-        a, st, tan, tx, ty, tt, adv_rows, adv_cols, solid, sym, partials,      \
-        done);                                                                 \
-    return cudaGetLastError();                                                 \
-  }
+  if (nf == NF && frozen == FZ && holes == HO)                                 \
+    return launch_pdl(phase_kernel<NF, Real, FZ, HO, AdvT>, grid, block, 0, s, \
+                      a, st, tan, tx, ty, tt, adv_rows, adv_cols, solid, sym,  \
+                      partials, done, tail);
   YH_PH(2, false, false)
   YH_PH(2, false, true)
   YH_PH(2, true, false)
@@ -590,6 +793,36 @@ cudaError_t launch_phase(const yh_param_var &p, int nf, const Fld<Real> &st,
   YH_PH(3, true, true)
 #undef YH_PH
   return cudaErrorInvalidValue;
+}
+
+template <typename Real>
+cudaError_t launch_phase(const yh_param_var &p, int nf, const Fld<Real> &st,
+                         const Fld<Real> &tan, const Fld<Real> &tx,
+                         const Fld<Real> &ty, const Fld<Real> &tt,
+                         const double *adv_rows, const double *adv_cols,
+                         const uint8_t *solid, yh_sym_state *sym,
+                         void *workspace, cudaStream_t s) {
+  PhaseTail none = {};
+  return phase_dispatch<Real, double>(p, nf, st, tan, tx, ty, tt, adv_rows,
+                                      adv_cols, solid, sym, workspace, none, s);
+}
+
+cudaError_t launch_phase_comoving(const yh_param_var &p, int nf,
+                                  const Fld<float> &st, const Fld<float> &tan,
+                                  const Fld<float> &tx, const Fld<float> &ty,
+                                  const Fld<float> &tt, float *adv_rows,
+                                  float *adv_cols, const uint8_t *solid,
+                                  yh_sym_state *sym, void *workspace,
+                                  bool advance, cudaStream_t s) {
+  PhaseTail tail;
+  tail.rows = adv_rows;
+  tail.cols = adv_cols;
+  tail.hx = (float)p.hx;
+  tail.hy = (float)p.hy;
+  tail.dt = p.dt;
+  tail.advance = advance ? 1 : 0;
+  return phase_dispatch<float, float>(p, nf, st, tan, tx, ty, tt, adv_rows,
+                                      adv_cols, solid, sym, workspace, tail, s);
 }
 
 // Template derivative fields over the whole grid (frozen template).
@@ -773,6 +1006,7 @@ __global__ void __launch_bounds__(256)
                const Real *__restrict__ adv_rows,
                const Real *__restrict__ adv_cols,
                const uint8_t *__restrict__ solid) {
+  grid_dep_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = a.nx, ny = a.ny;
@@ -816,13 +1050,15 @@ static cudaError_t bfecc_nf(const BfeccArgs<Real> &a, const Fld<Real> &in,
                             cudaStream_t s) {
   const dim3 block(32, 8);
   const dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8);
-  bfecc_pass<1, NF, Real, HOLES, ADV2D>
-      <<<grid, block, 0, s>>>(a, in, uf, ue, out, ar, ac, solid);
-  bfecc_pass<2, NF, Real, HOLES, ADV2D>
-      <<<grid, block, 0, s>>>(a, in, uf, ue, out, ar, ac, solid);
-  bfecc_pass<3, NF, Real, HOLES, ADV2D>
-      <<<grid, block, 0, s>>>(a, in, uf, ue, out, ar, ac, solid);
-  return cudaGetLastError();
+  cudaError_t e = launch_pdl(bfecc_pass<1, NF, Real, HOLES, ADV2D>, grid,
+                             block, 0, s, a, in, uf, ue, out, ar, ac, solid);
+  if (e == cudaSuccess)
+    e = launch_pdl(bfecc_pass<2, NF, Real, HOLES, ADV2D>, grid, block, 0, s,
+                   a, in, uf, ue, out, ar, ac, solid);
+  if (e == cudaSuccess)
+    e = launch_pdl(bfecc_pass<3, NF, Real, HOLES, ADV2D>, grid, block, 0, s,
+                   a, in, uf, ue, out, ar, ac, solid);
+  return e;
 }
 
 template <typename Real, bool ADV2D>

@@ -77,14 +77,26 @@ def stim(step, i0, j0, i1, j1, value=1.0):
     return s
 
 
-def fk_spiral_256(seed=0, n=256, nsteps=10000):
+def fk_spiral_256(seed=0, n=256, nsteps=10000, s2_ms=320.0):
+    """S1 on columns 0-9 at t = 0, S2 on the lower-left quadrant at s2_ms.
+    With the BR-fit parameters the S1 back leaves the tissue refractory to
+    about 400 ms; on 256^2 (6.4 cm) no S2 time leaves activity past 600 ms,
+    on 512^2 (12.8 cm) an S2 at 400-550 ms gives re-entry that lasts past
+    1000 ms (fk_sr_512)."""
     rng = np.random.default_rng(seed)
     p = A.fk_tissue_params(n, n)
     u, v, w = _ic(n, n, rng)
     dt = p.dt
-    s2 = stim(int(round(320.0 / dt)), 0, 0, n // 2, n // 2)
+    s2 = stim(int(round(s2_ms / dt)), 0, 0, n // 2, n // 2)
     return Workload("fk_spiral_%d" % n, p, A.fk_defaults(), A.YH_MODEL_FK3V,
                     u, v, w, None, [s2], nsteps)
+
+
+def fk_sr_512(seed=0):
+    """The start of the symmetry-reduced workload: fk_spiral_256's protocol
+    on 512^2 with S2 at 430 ms (inside the vulnerable window), run to
+    1000 ms, where two tips are in the tissue."""
+    return fk_spiral_256(seed=seed, n=512, nsteps=20000, s2_ms=430.0)
 
 
 def fk_holes_1024(seed=0, n=1024, nsteps=20000, nholes=300, npatch=12):
