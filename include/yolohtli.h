@@ -539,6 +539,16 @@ int yh_adjoint_record(yh_adjoint *h, const float *D, const float *u0,
 int yh_adjoint_run(yh_adjoint *h, const float *D, const float *u0,
                    const float *v0, const float *w0, double *loss,
                    float *grad_D);
+/* yh_adjoint_run that also returns dLoss/d(FK parameter) for each of the
+ * 13 fields of yh_fk_params in grad_fk (host): the sum over steps and
+ * cells of the adjoint state times the derivative of the pointwise update
+ * with respect to the parameter. With smooth = 0 the thresholds u_c, u_v
+ * enter only where they are not switches (u_c in the fast current). */
+int yh_adjoint_run_fk(yh_adjoint *h, const float *D, const float *u0,
+                      const float *v0, const float *w0, double *loss,
+                      float *grad_D, yh_fk_params *grad_fk);
+/* New FK parameters for the following runs (checked as at create). */
+int yh_adjoint_set_fk(yh_adjoint *h, const yh_fk_params *fk);
 
 /* ------------------------------------------------------------------ */
 /* Layer 4: the reference's interchange files                           */

@@ -6,4 +6,4 @@ here=$(cd "$(dirname "$0")" && pwd)
 mkdir -p "$here/_build"
 ${CC:-gcc} -O3 -fopenmp -ffp-contract=off -fPIC -shared -std=c11 \
   -Wall -Wno-unused-function \
-  "$here/yh_oracle.c" -o "$here/_build/liboracle.so" -lm
+  "$here/yh_oracle.c" "$here/yh_oracle_tlm.c" -o "$here/_build/liboracle.so" -lm

@@ -252,3 +252,19 @@ class SR:
         if getattr(self, "h", None):
             lib().orc_sr_destroy(C.c_void_p(self.h))
             self.h = None
+
+
+def adj_tlm(p, fk, dfk, eps, nsteps, frame, sp, D, dD, state0, target):
+    """FP64 tangent-linear model of the adjoint solver's forward map
+    (yh_oracle_tlm.c): (loss, directional derivative) along (dD, dfk)."""
+    f32 = [np.ascontiguousarray(x, np.float32) for x in
+           (D, dD, state0[0], state0[1], state0[2], target)]
+    L, dL = C.c_double(), C.c_double()
+    P = C.POINTER(C.c_float)
+    rc = lib().orc_adj_tlm(C.byref(p), C.byref(fk), C.byref(dfk),
+                           C.c_double(eps), int(nsteps), int(frame), int(sp),
+                           *[a.ctypes.data_as(P) for a in f32],
+                           C.byref(L), C.byref(dL))
+    if rc != 0:
+        raise MemoryError("orc_adj_tlm")
+    return L.value, dL.value

@@ -129,3 +129,103 @@ def test_autograd_function():
     loss = probe_loss(Dv, adj, st)
     (3.0 * loss).backward()
     assert torch.allclose(Dv.grad, 3.0 * g)
+
+
+def test_fk_parameter_gradient_matches_central_differences():
+    # all 13 FK3V parameters, FP64, smoothed switches (so u_c and u_v act
+    # through a differentiable ramp): the adjoint's dLoss/dtheta against
+    # central differences with a relative step of 1e-5
+    import torch
+    from yolohtli_gb300.adjoint import fk_array, fk_struct
+    n, nsteps = 48, 200
+    adj, st, D = problem(n, nsteps, 20, 6, 14, fp64=True, smooth=0.02)
+    g = torch.empty_like(D)
+    gfk = A.FKParams()
+    adj.run(D, st, g, gfk)
+    ad = fk_array(gfk)
+    base = fk_array(adj.fk)
+    assert np.all(np.isfinite(ad)) and np.abs(ad).max() > 0
+    fd = np.zeros(13)
+    for q in range(13):
+        h = 1e-5 * abs(base[q])
+        for sgn in (1, -1):
+            x = base.copy()
+            x[q] += sgn * h
+            adj.set_fk(fk_struct(x))
+            fd[q] += sgn * adj.run(D, st)
+        fd[q] /= 2 * h
+    adj.set_fk(fk_struct(base))
+    print("dL/dtheta adjoint", ad)
+    print("dL/dtheta central", fd)
+    for q in range(13):
+        assert abs(fd[q] - ad[q]) <= 1e-5 * abs(ad[q]) + 1e-9 * np.abs(ad).max(), \
+            (A.FK_NAMES[q], fd[q], ad[q])
+
+
+def test_fk_parameter_gradient_fp32_against_fp64_and_steps():
+    import torch
+    from yolohtli_gb300.adjoint import fk_array
+    n, nsteps = 64, 240
+    out = []
+    for fp64 in (True, False):
+        adj, st, D = problem(n, nsteps, 20, 8, 15, fp64=fp64)
+        g = torch.empty_like(D)
+        gfk = A.FKParams()
+        L = adj.run(D, st, g, gfk)
+        g0 = torch.empty_like(D)
+        assert adj.run(D, st, g0) == L      # the same forward pass
+        assert torch.equal(g, g0)           # and the same dLoss/dD
+        out.append(fk_array(gfk))
+    a64, a32 = out
+    err = np.abs(a32 - a64) / np.abs(a64).max()
+    print("FK gradient FP32 vs FP64 (relative to the largest):", err.max())
+    assert err.max() <= 1e-3
+
+
+def test_autograd_with_fk_parameters():
+    import torch
+    from yolohtli_gb300.adjoint import fk_array
+    n = 48
+    adj, st, D = problem(n, 120, 20, 6, 11, fp64=False)
+    g = torch.empty_like(D)
+    gfk = A.FKParams()
+    adj.run(D, st, g, gfk)
+    Dv = D.clone().requires_grad_(True)
+    fk = torch.tensor(fk_array(adj.fk), dtype=torch.float64, requires_grad=True)
+    loss = probe_loss(Dv, adj, st, fk)
+    (2.0 * loss).backward()
+    assert torch.allclose(Dv.grad, 2.0 * g)
+    assert np.allclose(fk.grad.numpy(), 2.0 * fk_array(gfk))
+    # a different fk switches the handle and changes the loss
+    fk2 = fk.detach().clone()
+    fk2[0] *= 1.2
+    assert float(probe_loss(D, adj, st, fk2)) != float(loss)
+
+
+@pytest.mark.parametrize("smooth", [0.0, 0.02])
+def test_gradients_match_the_fp64_tangent_linear_oracle(smooth):
+    # 64x64 downscale: the adjoint's <dL/dD, dD> + <dL/dtheta, dtheta> against
+    # the directional derivative of the oracle's tangent-linear model (dual
+    # numbers through the same discrete map, no shared derivation)
+    import torch
+    from oracle import oracle as O
+    from yolohtli_gb300.adjoint import fk_array, fk_struct
+    n, nsteps, frame, sp = 64, 240, 20, 8
+    adj, st, D = problem(n, nsteps, frame, sp, 15, fp64=True, smooth=smooth)
+    tgt = torch.empty(adj.target_shape, dtype=torch.float32, device="cuda")
+    adj.record(D / 1.1, st, tgt)  # a target: the run with D / 1.1
+    adj.set_target(tgt)
+    g = torch.empty_like(D)
+    gfk = A.FKParams()
+    L = adj.run(D, st, g, gfk)
+    rng = np.random.default_rng(8)
+    dD = (rng.standard_normal(n * n) * 1e-4).astype(np.float32)
+    dth = rng.standard_normal(13) * fk_array(adj.fk) * 0.05
+    Lo, dLo = O.adj_tlm(adj.p, adj.fk, fk_struct(dth), smooth, nsteps, frame, sp,
+                        host(D), dD, [host(x) for x in st], host(tgt))
+    ad = float(np.dot(host(g).astype(np.float64), dD.astype(np.float64))) + \
+        float(np.dot(fk_array(gfk), dth))
+    print("loss GPU %.12e oracle %.12e; dL adjoint %.10e tangent-linear %.10e"
+          % (L, Lo, ad, dLo))
+    assert abs(L - Lo) <= 1e-9 * abs(Lo)
+    assert abs(ad - dLo) <= 1e-6 * abs(dLo)

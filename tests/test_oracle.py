@@ -323,3 +323,35 @@ def test_oracle_bfecc_matches_reference_fixed_point(golden_gpu):
     out = O.bfecc(p, [g["bfecc_u0"], g["bfecc_v0"]], g["bfecc_c"], g["bfecc_phi"])
     assert rel(out[0], g["bfecc_u"]) < 1e-13
     assert rel(out[1], g["bfecc_v"]) < 1e-13
+
+
+def test_tangent_linear_model_matches_its_own_central_differences():
+    # the FP64 tangent-linear oracle of the adjoint solver's forward map:
+    # its directional derivative against central differences of its loss
+    from yolohtli_gb300.adjoint import fk_array, fk_struct
+    n, nsteps, frame, sp = 24, 80, 10, 4
+    p = A.fk_tissue_params(n, n)
+    rng = np.random.default_rng(3)
+    D = rng.uniform(5e-4, 1.5e-3, n * n).astype(np.float32)
+    u = np.zeros((n, n), np.float32)
+    u[:, :4] = 1.0
+    st = [u.ravel(), np.ones(n * n, np.float32), np.ones(n * n, np.float32)]
+    tgt = rng.uniform(0, 0.5, (nsteps // frame) * (n // sp) ** 2).astype(np.float32)
+    base = fk_array(A.fk_defaults())
+    dth = rng.standard_normal(13) * base * 0.1
+    dD = (rng.standard_normal(n * n) * 1e-4).astype(np.float32)
+    h = 1e-4
+    # D +- h dD is rounded to FP32: the direction is the step actually taken
+    Dp = (D + h * dD).astype(np.float32)
+    Dm = (D - h * dD).astype(np.float32)
+    dD = ((Dp.astype(np.float64) - Dm) / (2 * h)).astype(np.float32)
+    for eps in (0.0, 0.02):
+        L, dL = O.adj_tlm(p, fk_struct(base), fk_struct(dth), eps, nsteps, frame,
+                          sp, D, dD, st, tgt)
+        Lp, _ = O.adj_tlm(p, fk_struct(base + h * dth), fk_struct(0 * dth), eps,
+                          nsteps, frame, sp, Dp, 0 * dD, st, tgt)
+        Lm, _ = O.adj_tlm(p, fk_struct(base - h * dth), fk_struct(0 * dth), eps,
+                          nsteps, frame, sp, Dm, 0 * dD, st, tgt)
+        assert L > 0
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(fd - dL) <= 1e-5 * abs(dL), (eps, fd, dL)

@@ -83,6 +83,8 @@ SIGNATURES = {
     "yh_adjoint_set_target": (_i, [_v, _v]),
     "yh_adjoint_record": (_i, [_v, _v, _v, _v, _v, _v]),
     "yh_adjoint_run": (_i, [_v, _v, _v, _v, _v, _P(_d), _v]),
+    "yh_adjoint_run_fk": (_i, [_v, _v, _v, _v, _v, _P(_d), _v, _P(A.FKParams)]),
+    "yh_adjoint_set_fk": (_i, [_v, _P(A.FKParams)]),
     # the reference's interchange files
     "yh_write_param_csv": (_i, [C.c_char_p, _P(A.ParamVar), C.c_char_p,
                                 C.c_char_p]),

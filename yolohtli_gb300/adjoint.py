@@ -1,7 +1,8 @@
-"""Gradients of a probe loss with respect to the diffusion map D(x, y)
-(yh_adjoint_* in include/yolohtli.h), and a torch.autograd.Function over
-them: `loss = ProbeLoss.apply(D, problem)` then `loss.backward()` fills
-D.grad with the adjoint's dLoss/dD."""
+"""Gradients of a probe loss with respect to the diffusion map D(x, y) and
+the 13 FK3V parameters (yh_adjoint_* in include/yolohtli.h), and a
+torch.autograd.Function over them: `loss = probe_loss(D, adjoint, state0,
+fk)` then `loss.backward()` fills D.grad (and fk.grad, a float64 tensor of
+the 13 parameters in yh_fk_params order) with the adjoint's gradients."""
 import ctypes as C
 
 import numpy as np
@@ -41,6 +42,7 @@ class Adjoint:
             int(probe_spacing), int(checkpoint_steps), 1 if fp64 else 0,
             float(smooth), C.c_void_p(stream) if stream else None, C.byref(h)))
         self.h = h
+        self.fk = A.FKParams.from_buffer_copy(fk)
         f, px, py = C.c_int(), C.c_int(), C.c_int()
         check("yh_adjoint_probes", self.lib.yh_adjoint_probes(
             h, C.byref(f), C.byref(px), C.byref(py)))
@@ -75,36 +77,71 @@ class Adjoint:
             self.h, D.data_ptr(), *[x.data_ptr() for x in state0],
             out.data_ptr()))
 
-    def run(self, D, state0, grad=None):
-        """Loss (float) and, with `grad` (device float32 like D), dLoss/dD."""
+    def set_fk(self, fk):
+        """New FK3V parameters (an A.FKParams) for the following runs."""
+        check("yh_adjoint_set_fk", self.lib.yh_adjoint_set_fk(self.h, C.byref(fk)))
+        self.fk = A.FKParams.from_buffer_copy(fk)
+
+    def run(self, D, state0, grad=None, grad_fk=None):
+        """Loss (float) and, with `grad` (device float32 like D), dLoss/dD;
+        with grad_fk (an A.FKParams) also dLoss/d(each FK parameter)."""
         loss = C.c_double()
         _after_torch()
-        check("yh_adjoint_run", self.lib.yh_adjoint_run(
-            self.h, D.data_ptr(), *[x.data_ptr() for x in state0],
-            C.byref(loss), grad.data_ptr() if grad is not None else None))
+        g = grad.data_ptr() if grad is not None else None
+        x = [D.data_ptr()] + [t.data_ptr() for t in state0]
+        if grad_fk is not None:
+            check("yh_adjoint_run_fk", self.lib.yh_adjoint_run_fk(
+                self.h, *x, C.byref(loss), g, C.byref(grad_fk)))
+        else:
+            check("yh_adjoint_run", self.lib.yh_adjoint_run(
+                self.h, *x, C.byref(loss), g))
         return loss.value
+
+
+def fk_array(fk):
+    """The 13 FK3V parameters of an A.FKParams as a float64 array."""
+    return np.array([getattr(fk, n) for n in A.FK_NAMES], np.float64)
+
+
+def fk_struct(x):
+    """An A.FKParams from 13 values in yh_fk_params order."""
+    f = A.FKParams()
+    for n, v in zip(A.FK_NAMES, np.asarray(x, np.float64).tolist()):
+        setattr(f, n, v)
+    return f
 
 
 def _make_function():
     import torch
 
     class ProbeLoss(torch.autograd.Function):
-        """loss = ProbeLoss.apply(D, adjoint, state0): D a float32 CUDA
-        tensor of nx*ny, state0 (u0, v0, w0) float32 CUDA tensors."""
+        """loss = ProbeLoss.apply(D, fk, adjoint, state0): D a float32 CUDA
+        tensor of nx*ny, fk None or a float64 tensor of the 13 FK3V
+        parameters (the handle is switched to them when they differ),
+        state0 (u0, v0, w0) float32 CUDA tensors."""
 
         @staticmethod
-        def forward(ctx, D, adjoint, state0):
+        def forward(ctx, D, fk, adjoint, state0):
             D = D.contiguous()
             state0 = [x.contiguous() for x in state0]
             grad = torch.empty_like(D)
-            loss = adjoint.run(D, state0, grad)
+            gfk = None
+            if fk is not None:
+                want = fk.detach().cpu().double().numpy()
+                if not np.array_equal(want, fk_array(adjoint.fk)):
+                    adjoint.set_fk(fk_struct(want))
+                gfk = A.FKParams()
+            loss = adjoint.run(D, state0, grad, gfk)
             ctx.save_for_backward(grad)
+            ctx.gfk = None if gfk is None else torch.tensor(
+                fk_array(gfk), dtype=fk.dtype, device=fk.device)
             return torch.tensor(loss, dtype=torch.float64, device=D.device)
 
         @staticmethod
         def backward(ctx, g):
             (grad,) = ctx.saved_tensors
-            return (g.to(grad.dtype) * grad, None, None)
+            gfk = None if ctx.gfk is None else g.to(ctx.gfk.dtype).to(ctx.gfk.device) * ctx.gfk
+            return (g.to(grad.dtype) * grad, gfk, None, None)
 
     return ProbeLoss
 
@@ -112,9 +149,10 @@ def _make_function():
 _fn = None
 
 
-def probe_loss(D, adjoint, state0):
-    """The probe loss as a differentiable function of D."""
+def probe_loss(D, adjoint, state0, fk=None):
+    """The probe loss as a differentiable function of D (and, when given,
+    of the FK3V parameters fk: a float64 tensor of 13)."""
     global _fn
     if _fn is None:
         _fn = _make_function()
-    return _fn.apply(D, adjoint, state0)
+    return _fn.apply(D, fk, adjoint, state0)

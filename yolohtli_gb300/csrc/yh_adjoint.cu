@@ -135,6 +135,49 @@ __device__ __forceinline__ FkLocal<Real> fk_local(const AdjCoeffs<Real> &a,
   return r;
 }
 
+// The raw FK3V parameters of the update, in the order of yh_fk_params:
+// the nine rates s_X = tc dt / tau_X (tau_d, tau_r, tau_si, tau_0,
+// tau_v_plus, tau_v1_minus, tau_v2_minus, tau_w_plus, tau_w_minus), then
+// u_c, u_v, u_csi and k2 = -2k / ln 2. kNumFk of them.
+constexpr int kNumFk = 13;
+
+// g[q] = lu dun/dp_q + lv dvn/dp_q + lw dwn/dp_q for the raw parameters p_q
+// at one cell: (lu, lv, lw) is the adjoint of (un, vn, wn).
+template <typename Real>
+__device__ __forceinline__ void fk_param_terms(const AdjCoeffs<Real> &a,
+                                               Real u, Real v, Real w,
+                                               Real lu, Real lv, Real lw,
+                                               Real g[kNumFk]) {
+  Real H1, dH1, H2, dH2;
+  heaviside(u - a.u_c, a.eps, H1, dH1);
+  heaviside(u - a.u_v, a.eps, H2, dH2);
+  const Real e = ex2<Real>(a.k2 * (u - a.u_csi));
+  const Real sig = Real(1) / (Real(1) + e);
+  const Real ln2 = Real(0.69314718055994530942);
+  const Real ss = sig * (Real(1) - sig);
+  const Real q = v * (Real(1) - u) * (u - a.u_c);  // jp = s_tr - q s_td
+  const Real jp = a.s_tr - q * a.s_td;
+  const Real jn = u * a.s_to;
+  const Real sv = H2 * a.s_tv1m + (Real(1) - H2) * a.s_tv2m;
+  const Real vp = v - v * a.s_tvp, vm = v + (Real(1) - v) * sv;
+  const Real wp = w - w * a.s_twp, wm = w + (Real(1) - w) * a.s_twm;
+  const Real L1 = Real(1) - H1;
+  g[0] = lu * H1 * q;                          // s_td
+  g[1] = -lu * H1;                             // s_tr
+  g[2] = lu * w * sig;                         // s_tsi
+  g[3] = -lu * L1 * u;                         // s_to
+  g[4] = -lv * H1 * v;                         // s_tvp
+  g[5] = lv * L1 * (Real(1) - v) * H2;         // s_tv1m
+  g[6] = lv * L1 * (Real(1) - v) * (Real(1) - H2);  // s_tv2m
+  g[7] = -lw * H1 * w;                         // s_twp
+  g[8] = lw * L1 * (Real(1) - w);              // s_twm
+  g[9] = lu * (dH1 * (jp - jn) - H1 * v * (Real(1) - u) * a.s_td) -
+         lv * dH1 * (vp - vm) - lw * dH1 * (wp - wm);  // u_c
+  g[10] = -lv * L1 * (Real(1) - v) * dH2 * (a.s_tv1m - a.s_tv2m);  // u_v
+  g[11] = lu * w * a.s_tsi * ln2 * a.k2 * ss;       // u_csi
+  g[12] = -lu * w * a.s_tsi * ln2 * (u - a.u_csi) * ss;  // k2
+}
+
 // du of cell (i, j): the four faces towards the mirrored neighbours.
 template <typename Real>
 __device__ __forceinline__ Real diffusion(const AdjCoeffs<Real> &a,
@@ -171,20 +214,47 @@ __global__ void adj_forward_kernel(const AdjCoeffs<Real> a,
 // Reverse step: lambda_in = lambda^{n+1} (lu, lv, lw), x^n = (u, v, w);
 // writes lambda^n (without the loss term) and adds to gr (the gradient
 // with respect to r).
-template <typename Real>
-__global__ void adj_reverse_kernel(const AdjCoeffs<Real> a,
-                                   const Real *__restrict__ r,
-                                   const Real *__restrict__ u,
-                                   const Real *__restrict__ v,
-                                   const Real *__restrict__ w,
-                                   const Real *__restrict__ lu,
-                                   const Real *__restrict__ lv,
-                                   const Real *__restrict__ lw,
-                                   Real *__restrict__ lu_o, Real *__restrict__ lv_o,
-                                   Real *__restrict__ lw_o, Real *__restrict__ gr) {
+// With PARAMS the block also adds its cells' fk_param_terms to its own
+// accumulators gp[block][0..12] (FP64; one slot per block, so the sum over
+// steps keeps a fixed order).
+template <typename Real, bool PARAMS>
+__global__ void __launch_bounds__(256)
+    adj_reverse_kernel(const AdjCoeffs<Real> a, const Real *__restrict__ r,
+                       const Real *__restrict__ u, const Real *__restrict__ v,
+                       const Real *__restrict__ w, const Real *__restrict__ lu,
+                       const Real *__restrict__ lv, const Real *__restrict__ lw,
+                       Real *__restrict__ lu_o, Real *__restrict__ lv_o,
+                       Real *__restrict__ lw_o, Real *__restrict__ gr,
+                       double *__restrict__ gp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = a.nx, ny = a.ny;
+  if (PARAMS) {
+    Real g[kNumFk];
+    if (i < nx && j < ny) {
+      const int c = i + nx * j;
+      fk_param_terms(a, u[c], v[c], w[c], lu[c], lv[c], lw[c], g);
+    } else {
+#pragma unroll
+      for (int k = 0; k < kNumFk; ++k) g[k] = Real(0);
+    }
+#pragma unroll
+    for (int k = 0; k < kNumFk; ++k)
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1)
+        g[k] += __shfl_down_sync(0xffffffffu, g[k], off);
+    __shared__ Real s_g[8][kNumFk];  // blockDim (32, 8)
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < kNumFk; ++k) s_g[threadIdx.y][k] = g[k];
+    __syncthreads();
+    const int t = threadIdx.x + 32 * threadIdx.y;
+    if (t < kNumFk) {
+      Real sum = s_g[0][t];
+      for (int q = 1; q < 8; ++q) sum += s_g[q][t];
+      gp[(size_t)(blockIdx.x + gridDim.x * blockIdx.y) * 16 + t] += (double)sum;
+    }
+  }
   if (i >= nx || j >= ny) return;
   const int c = i + nx * j;
   // pointwise part at c
@@ -292,6 +362,16 @@ __global__ void adj_gather_kernel(int nx, int sp, int npx, int npy,
   out[p] = (float)u[(px * sp + sp / 2) + nx * (py * sp + sp / 2)];
 }
 
+// Sum of the per-block parameter accumulators, in block order.
+__global__ void adj_param_reduce_kernel(int nb, const double *__restrict__ gp,
+                                        double *__restrict__ out) {
+  const int k = threadIdx.x;
+  if (k >= kNumFk) return;
+  double s = 0.0;
+  for (int b = 0; b < nb; ++b) s += gp[(size_t)b * 16 + k];
+  out[k] = s;
+}
+
 inline int st(cudaError_t e) {
   if (e == cudaSuccess) return YH_OK;
   if (e == cudaErrorMemoryAllocation) return YH_ENOMEM;
@@ -316,10 +396,18 @@ struct yh_adjoint {
   void *gr = nullptr;     // gradient with respect to r
   float *target = nullptr;  // [frames][probes]
   double *loss = nullptr;
+  double *gp = nullptr;   // per-block FK-parameter accumulators (16 each)
+  double *gfk = nullptr;  // their sum: dL/d(raw FK parameters)
+  int nrev = 0;           // blocks of the reverse launch
   int frames = 0;
   // the whole forward (+ reverse) sequence on the handle's own buffers,
-  // captured once: [0] loss only, [1] loss and gradient
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  // captured once: [0] loss only, [1] loss and dL/dD, [2] also the FK
+  // parameters
+  cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+  yh_fk_params fk{};
+  yh_param_var pv{};
+  double smooth = 0;
+  double tcdt = 0;  // s_X = tcdt / tau_X
 };
 
 namespace {
@@ -351,7 +439,7 @@ cudaError_t fwd(const yh_adjoint *h, const Real *r, const Real *const *x,
 // on the handle's buffers only: r and checkpoint 0 hold the inputs. Its
 // launches are captured into a CUDA graph by run_t.
 template <typename Real>
-cudaError_t run_body(yh_adjoint *h, bool grad) {
+cudaError_t run_body(yh_adjoint *h, bool grad, bool params) {
   const int n = h->n, T = h->nsteps, ck = h->ck;
   const View<Real> C{(Real *)h->ckpt, n}, S{(Real *)h->seg, n}, L{(Real *)h->lam, n};
   Real *r = (Real *)h->r, *gr = (Real *)h->gr;
@@ -384,6 +472,8 @@ cudaError_t run_body(yh_adjoint *h, bool grad) {
   // reverse, one segment at a time from the last: lambda^T = dL/dx^T
   e = cudaMemsetAsync(L.f(0, 0), 0, 3 * n * sizeof(Real), h->s);
   if (e == cudaSuccess) e = cudaMemsetAsync(gr, 0, n * sizeof(Real), h->s);
+  if (e == cudaSuccess && params)
+    e = cudaMemsetAsync(h->gp, 0, (size_t)h->nrev * 16 * sizeof(double), h->s);
   int li = 0;  // lambda^{t+1} lives in L state li
   for (int s0 = ((T - 1) / ck) * ck; s0 >= 0 && e == cudaSuccess; s0 -= ck) {
     const int s1 = std::min(s0 + ck, T);  // states s0 .. s1
@@ -406,20 +496,30 @@ cudaError_t run_body(yh_adjoint *h, bool grad) {
         if (e != cudaSuccess) break;
       }
       const dim3 b(32, 8), g((h->nx + 31) / 32, (h->ny + 7) / 8);
-      adj_reverse_kernel<Real><<<g, b, 0, h->s>>>(
-          coeffs<Real>(h), r, S.f(t - 1 - s0, 0), S.f(t - 1 - s0, 1),
-          S.f(t - 1 - s0, 2), L.f(li, 0), L.f(li, 1), L.f(li, 2),
-          L.f(li ^ 1, 0), L.f(li ^ 1, 1), L.f(li ^ 1, 2), gr);
+      if (params)
+        adj_reverse_kernel<Real, true><<<g, b, 0, h->s>>>(
+            coeffs<Real>(h), r, S.f(t - 1 - s0, 0), S.f(t - 1 - s0, 1),
+            S.f(t - 1 - s0, 2), L.f(li, 0), L.f(li, 1), L.f(li, 2),
+            L.f(li ^ 1, 0), L.f(li ^ 1, 1), L.f(li ^ 1, 2), gr, h->gp);
+      else
+        adj_reverse_kernel<Real, false><<<g, b, 0, h->s>>>(
+            coeffs<Real>(h), r, S.f(t - 1 - s0, 0), S.f(t - 1 - s0, 1),
+            S.f(t - 1 - s0, 2), L.f(li, 0), L.f(li, 1), L.f(li, 2),
+            L.f(li ^ 1, 0), L.f(li ^ 1, 1), L.f(li ^ 1, 2), gr, nullptr);
       e = cudaGetLastError();
       li ^= 1;
     }
+  }
+  if (e == cudaSuccess && params) {
+    adj_param_reduce_kernel<<<1, 32, 0, h->s>>>(h->nrev, h->gp, h->gfk);
+    e = cudaGetLastError();
   }
   return e;
 }
 
 template <typename Real>
 int run_t(yh_adjoint *h, const float *D, const float *u0, const float *v0,
-          const float *w0, double *loss_out, float *grad) {
+          const float *w0, double *loss_out, float *grad, double *graw) {
   const int n = h->n;
   const View<Real> C{(Real *)h->ckpt, n};
   const int nb = (n + 255) / 256;
@@ -431,12 +531,13 @@ int run_t(yh_adjoint *h, const float *D, const float *u0, const float *v0,
     adj_widen_kernel<Real><<<nb, 256, 0, h->s>>>(n, x0[q], C.f(0, q));
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return st(e);
-  cudaGraphExec_t &ex = h->graph[grad ? 1 : 0];
+  const bool want_grad = grad != nullptr || graw != nullptr;
+  cudaGraphExec_t &ex = h->graph[graw ? 2 : (want_grad ? 1 : 0)];
   if (!ex) {
     cudaGraph_t g = nullptr;
     e = cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return st(e);
-    const cudaError_t eb = run_body<Real>(h, grad != nullptr);
+    const cudaError_t eb = run_body<Real>(h, want_grad, graw != nullptr);
     e = cudaStreamEndCapture(h->s, &g);
     if (eb != cudaSuccess || e != cudaSuccess) {
       if (g) cudaGraphDestroy(g);
@@ -458,6 +559,9 @@ int run_t(yh_adjoint *h, const float *D, const float *u0, const float *v0,
   }
   if (e == cudaSuccess && loss_out)
     e = cudaMemcpyAsync(loss_out, h->loss, sizeof(double), cudaMemcpyDeviceToHost, h->s);
+  if (e == cudaSuccess && graw)
+    e = cudaMemcpyAsync(graw, h->gfk, kNumFk * sizeof(double),
+                        cudaMemcpyDeviceToHost, h->s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
   return st(e);
 }
@@ -491,6 +595,36 @@ int record_t(yh_adjoint *h, const float *D, const float *u0, const float *v0,
   return st(e);
 }
 
+// The step coefficients of the handle from its parameters and fk.
+void set_coeffs(yh_adjoint *h, const yh_fk_params *fk) {
+  h->fk = *fk;
+  const StepCoeffs<double> sd =
+      make_step_coeffs<double>(h->pv, YH_MODEL_FK3V, fk);
+  auto fill = [&](auto &a) {
+    using R = decltype(a.tc);
+    a.nx = h->nx;
+    a.ny = h->ny;
+    a.eps = (R)h->smooth;
+    a.tc = (R)sd.tc;
+    a.dt = (R)sd.dt;
+    a.u_c = (R)sd.u_c;
+    a.u_v = (R)sd.u_v;
+    a.u_csi = (R)sd.u_csi;
+    a.k2 = (R)sd.k_exp2;
+    a.s_td = (R)sd.s_td;
+    a.s_tr = (R)sd.s_tr;
+    a.s_to = (R)sd.s_to;
+    a.s_tsi = (R)sd.s_tsi;
+    a.s_tvp = (R)sd.s_tvp;
+    a.s_tv1m = (R)sd.s_tv1m;
+    a.s_tv2m = (R)sd.s_tv2m;
+    a.s_twp = (R)sd.s_twp;
+    a.s_twm = (R)sd.s_twm;
+  };
+  fill(h->af);
+  fill(h->ad);
+}
+
 }  // namespace
 
 extern "C" int yh_adjoint_destroy(yh_adjoint *h) {
@@ -505,6 +639,8 @@ extern "C" int yh_adjoint_destroy(yh_adjoint *h) {
   cudaFree(h->gr);
   cudaFree(h->target);
   cudaFree(h->loss);
+  cudaFree(h->gp);
+  cudaFree(h->gfk);
   if (h->own_stream && h->s) cudaStreamDestroy(h->s);
   delete h;
   return YH_OK;
@@ -525,6 +661,7 @@ extern "C" int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
   yh_adjoint *h = new (std::nothrow) yh_adjoint();
   if (!h) return YH_ENOMEM;
   h->fp64 = fp64 ? 1 : 0;
+  h->smooth = smooth;
   h->nx = p->nx;
   h->ny = p->ny;
   h->n = p->nx * p->ny;
@@ -536,30 +673,10 @@ extern "C" int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
   h->ck = checkpoint_steps;
   h->frames = nsteps / frame_steps;
   h->rscale = p->dt / (p->hx * p->hx);
-  const StepCoeffs<double> sd = make_step_coeffs<double>(*p, YH_MODEL_FK3V, fk);
-  auto fill = [&](auto &a) {
-    using R = decltype(a.tc);
-    a.nx = p->nx;
-    a.ny = p->ny;
-    a.eps = (R)smooth;
-    a.tc = (R)sd.tc;
-    a.dt = (R)sd.dt;
-    a.u_c = (R)sd.u_c;
-    a.u_v = (R)sd.u_v;
-    a.u_csi = (R)sd.u_csi;
-    a.k2 = (R)sd.k_exp2;
-    a.s_td = (R)sd.s_td;
-    a.s_tr = (R)sd.s_tr;
-    a.s_to = (R)sd.s_to;
-    a.s_tsi = (R)sd.s_tsi;
-    a.s_tvp = (R)sd.s_tvp;
-    a.s_tv1m = (R)sd.s_tv1m;
-    a.s_tv2m = (R)sd.s_tv2m;
-    a.s_twp = (R)sd.s_twp;
-    a.s_twm = (R)sd.s_twm;
-  };
-  fill(h->af);
-  fill(h->ad);
+  h->tcdt = p->tc * p->dt;
+  h->nrev = ((p->nx + 31) / 32) * ((p->ny + 7) / 8);
+  h->pv = *p;
+  set_coeffs(h, fk);
   const size_t es = h->fp64 ? sizeof(double) : sizeof(float);
   const size_t state = 3 * (size_t)h->n * es;
   const size_t nck = (size_t)(nsteps - 1) / checkpoint_steps + 1;
@@ -577,6 +694,8 @@ extern "C" int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
   if (e == cudaSuccess)
     e = cudaMalloc(&h->target, (size_t)std::max(1, h->frames) * h->npx * h->npy * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&h->loss, sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&h->gp, (size_t)h->nrev * 16 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&h->gfk, 16 * sizeof(double));
   if (e == cudaSuccess)
     e = cudaMemsetAsync(h->target, 0,
                         (size_t)std::max(1, h->frames) * h->npx * h->npy * sizeof(float), h->s);
@@ -611,8 +730,57 @@ extern "C" int yh_adjoint_run(yh_adjoint *h, const float *D, const float *u0,
                               const float *v0, const float *w0, double *loss,
                               float *grad_D) {
   if (!h || !D || !u0 || !v0 || !w0) return YH_EINVAL;
-  return h->fp64 ? run_t<double>(h, D, u0, v0, w0, loss, grad_D)
-                 : run_t<float>(h, D, u0, v0, w0, loss, grad_D);
+  return h->fp64 ? run_t<double>(h, D, u0, v0, w0, loss, grad_D, nullptr)
+                 : run_t<float>(h, D, u0, v0, w0, loss, grad_D, nullptr);
+}
+
+extern "C" int yh_adjoint_run_fk(yh_adjoint *h, const float *D,
+                                 const float *u0, const float *v0,
+                                 const float *w0, double *loss, float *grad_D,
+                                 yh_fk_params *grad_fk) {
+  if (!h || !D || !u0 || !v0 || !w0 || !grad_fk) return YH_EINVAL;
+  double g[16];
+  const int rc = h->fp64 ? run_t<double>(h, D, u0, v0, w0, loss, grad_D, g)
+                         : run_t<float>(h, D, u0, v0, w0, loss, grad_D, g);
+  if (rc) return rc;
+  // chain rule from the raw parameters: s_X = tc dt / tau_X, so
+  // ds_X/dtau_X = -s_X / tau_X; k2 = -2k / ln 2
+  const yh_fk_params &f = h->fk;
+  const double tau[9] = {f.tau_d, f.tau_r, f.tau_si, f.tau_0, f.tau_v_plus,
+                         f.tau_v1_minus, f.tau_v2_minus, f.tau_w_plus,
+                         f.tau_w_minus};
+  double out[9];
+  for (int q = 0; q < 9; ++q) out[q] = -g[q] * h->tcdt / (tau[q] * tau[q]);
+  grad_fk->tau_d = out[0];
+  grad_fk->tau_r = out[1];
+  grad_fk->tau_si = out[2];
+  grad_fk->tau_0 = out[3];
+  grad_fk->tau_v_plus = out[4];
+  grad_fk->tau_v1_minus = out[5];
+  grad_fk->tau_v2_minus = out[6];
+  grad_fk->tau_w_plus = out[7];
+  grad_fk->tau_w_minus = out[8];
+  grad_fk->u_c = g[9];
+  grad_fk->u_v = g[10];
+  grad_fk->u_csi = g[11];
+  grad_fk->k = g[12] * (-2.0 / log(2.0));
+  return YH_OK;
+}
+
+extern "C" int yh_adjoint_set_fk(yh_adjoint *h, const yh_fk_params *fk) {
+  if (!h || !fk) return YH_EINVAL;
+  const int rc = check_params(&h->pv, YH_MODEL_FK3V, fk);
+  if (rc) return rc;
+  cudaError_t e = cudaStreamSynchronize(h->s);
+  if (e != cudaSuccess) return st(e);
+  set_coeffs(h, fk);
+  // the captured graphs hold the old coefficients as kernel arguments
+  for (auto &g : h->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  return YH_OK;
 }
 
 extern "C" int yh_adjoint_record(yh_adjoint *h, const float *D, const float *u0,
