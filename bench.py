@@ -622,9 +622,12 @@ def run_adjoint(args):
     Gaussian bumps in [5e-4, 1.5e-3], 10,000 steps, the loss on a 32 x 32
     probe lattice every 20 steps, target from the true D, gradient at
     1.1 D; the model's switches as tanh ramps of width 0.01, without which
-    the loss's derivative is not usable at this horizon): gradients per
-    second, the FP32 gradient against the FP64 one, and the FP64 gradient
-    against central differences of its loss."""
+    the loss's derivative is not usable at this horizon). A gradient is the
+    full one: dLoss/dD and dLoss/d(13 FK parameters). Reported: gradients
+    per second with sqrt(N) checkpoints (the headline), with every state
+    kept, and for 16 instances in one batched handle; the FP32 gradient
+    against the FP64 one; the FP64 gradient against central differences of
+    the FP64 loss along 20 random directions of (D, FK parameters)."""
     import torch
     rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
     torch.cuda.set_device(env_int("LOCAL_RANK", 0))
@@ -635,76 +638,105 @@ def run_adjoint(args):
             "cuda", env_int("LOCAL_RANK", 0)))
     from yolohtli_gb300 import _abi as A
     from yolohtli_gb300 import workloads as W
-    from yolohtli_gb300.adjoint import Adjoint
+    from yolohtli_gb300.adjoint import Adjoint, fk_array, fk_struct
     n, nsteps = 512, args.nsteps
     frame, spacing = 20, 16
     ck = max(1, int(round(nsteps ** 0.5)))
     p = A.fk_tissue_params(n, n)
     D_true, state0 = W.fk_adjoint_case(n, seed=0)
-
     smooth = 0.01  # tanh switches: a derivative usable over 10,000 steps
+    fk0 = A.fk_defaults()
 
-    def make(fp64, steps):
-        a = Adjoint(p, A.fk_defaults(), steps, frame, spacing,
-                    max(1, int(round(steps ** 0.5))), fp64=fp64, smooth=smooth)
-        st = [torch.tensor(x, device="cuda") for x in state0]
-        Dt = torch.tensor(D_true, device="cuda")
+    def make(fp64, steps, ckpt, batch=1):
+        a = Adjoint(p, fk0, steps, frame, spacing, ckpt, fp64=fp64,
+                    smooth=smooth, batch=batch)
+        st = [torch.tensor(x, device="cuda").repeat(batch) for x in state0]
+        Dt = torch.tensor(D_true, device="cuda").repeat(batch)
         tgt = torch.empty(a.target_shape, dtype=torch.float32, device="cuda")
         a.record(Dt, st, tgt)
         a.set_target(tgt)
         return a, st, Dt * 1.1
 
-    adj, st, D = make(False, nsteps)
-    g = torch.empty_like(D)
+    def timed(a, st, D, k, grad=True):
+        g = torch.empty_like(D) if grad else None
+        gfk = (A.FKParams * a.batch)() if grad else None
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            loss = a.run(D, st, g, gfk)
+        return time.perf_counter() - t0, loss, g, gfk
+
+    adj, st, D = make(False, nsteps, ck)
     for _ in range(args.warmup):
-        adj.run(D, st, g)
-    torch.cuda.synchronize()
+        timed(adj, st, D, 1)
     if dist:
         dist.barrier()
     clocks = ClockSampler(env_int("LOCAL_RANK", 0))
     clocks.start()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        loss = adj.run(D, st, g)
-    sec = time.perf_counter() - t0
+    sec, loss, g, gfk = timed(adj, st, D, args.steps)
     clk = clocks.stop()
-    t1 = time.perf_counter()
-    for _ in range(args.steps):
-        adj.run(D, st)
-    fwd = time.perf_counter() - t1
+    fwd, _, _, _ = timed(adj, st, D, args.steps, grad=False)
     sec = max_over_ranks(sec, dist, "cuda")
     value = world * args.steps / sec
-    # end to end: D from the host, the gradient back, every gradient
+    # end to end: D from the host, both gradients back, every gradient
     Dh = D.cpu().pin_memory()
     gh = torch.empty_like(Dh).pin_memory()
     Dd = torch.empty_like(D)
+    gfk_h = A.FKParams()
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     for _ in range(args.steps):
         Dd.copy_(Dh, non_blocking=True)
-        adj.run(Dd, st, g)
+        adj.run(Dd, st, g, gfk_h)
         gh.copy_(g)
     e2e_s = max_over_ranks(time.perf_counter() - t2, dist, "cuda")
-    # accuracy, at the full size: the FP64 gradient against central
-    # differences of the FP64 loss (h = 1e-3 relative, 2 random directions),
-    # and the FP32 gradient against the FP64 one
-    b64, st64, D64 = make(True, nsteps)
+    # every state kept (31 GB at this size): no recompute
+    del adj
+    torch.cuda.empty_cache()
+    a1, st1, D1 = make(False, nsteps, 1)
+    timed(a1, st1, D1, 1)
+    s1, _, _, _ = timed(a1, st1, D1, args.steps)
+    f1, _, _, _ = timed(a1, st1, D1, args.steps, grad=False)
+    del a1
+    torch.cuda.empty_cache()
+    # 16 instances, one handle
+    B = 16
+    ab, stb, Db = make(False, nsteps, ck, batch=B)
+    timed(ab, stb, Db, 1)
+    sb, _, _, _ = timed(ab, stb, Db, max(1, args.steps // 2))
+    batch_rate = B * max(1, args.steps // 2) / sb
+    del ab
+    torch.cuda.empty_cache()
+    # accuracy at the full size: the FP64 gradients against central
+    # differences of the FP64 loss (h = 1e-3 relative) along 20 random
+    # directions of (D, FK parameters); the FP32 gradients against FP64
+    b64, st64, D64 = make(True, nsteps, ck)
     g64 = torch.empty_like(D64)
-    b64.run(D64, st64, g64)
-    torch.cuda.synchronize()
+    f64 = A.FKParams()
     t3 = time.perf_counter()
-    b64.run(D64, st64, g64)
+    b64.run(D64, st64, g64, f64)
     fp64_rate = 1.0 / (time.perf_counter() - t3)
+    th0 = fk_array(fk0)
     rng = np.random.default_rng(3)
-    fd_err = 0.0
-    for _ in range(2):
+    ndir = 20
+    fd_err = {1e-3: 0.0, 1e-5: 0.0}
+    for _ in range(ndir):
         d = torch.tensor(rng.standard_normal(n * n).astype(np.float32), device="cuda") * D64
-        Dp, Dm = D64 + 1e-3 * d, D64 - 1e-3 * d
-        step = (Dp.double() - Dm.double()) / 2
-        fd = b64.run(Dp, st64) - b64.run(Dm, st64)
-        ad = 2 * float((g64.double() * step).sum())
-        fd_err = max(fd_err, abs(fd - ad) / max(abs(ad), 1e-300))
+        dth = rng.standard_normal(13) * th0
+        for hrel in fd_err:
+            Dp, Dm = D64 + hrel * d, D64 - hrel * d
+            step = (Dp.double() - Dm.double()) / 2
+            b64.set_fk(fk_struct(th0 + hrel * dth))
+            Lp = b64.run(Dp, st64)
+            b64.set_fk(fk_struct(th0 - hrel * dth))
+            Lm = b64.run(Dm, st64)
+            ad = 2 * (float((g64.double() * step).sum()) +
+                      hrel * float(np.dot(fk_array(f64), dth)))
+            fd_err[hrel] = max(fd_err[hrel], abs((Lp - Lm) - ad) / max(abs(ad), 1e-300))
+    b64.set_fk(fk0)
     rel = float((g.double() - g64.double()).norm() / g64.double().norm())
+    rel_fk = float(np.abs(fk_array(gfk[0]) - fk_array(f64)).max() /
+                   np.abs(fk_array(f64)).max())
     if rank == 0:
         line = {
             "metric": "adjoint gradients/s", "value": round(value, 3),
@@ -715,22 +747,38 @@ def run_adjoint(args):
             "config": {"workload": "fk_adjoint_512", "grid": [n, n],
                        "steps_per_gradient": nsteps, "frames": nsteps // frame,
                        "probes": [n // spacing, n // spacing],
-                       "checkpoint_steps": ck, "D": "8 Gaussian bumps in [5e-4, 1.5e-3]",
+                       "checkpoint_steps": ck,
+                       "gradient": "dLoss/dD (512^2) and dLoss/d(13 FK parameters)",
+                       "D": "8 Gaussian bumps in [5e-4, 1.5e-3]",
                        "switches": "FK3V's H(u - u_c), H(u - u_v) as tanh ramps of width %g" % smooth,
                        "estimate": "1.1 x the true D",
                        "parallelism": "replicas x%d" % world},
-            "loss": loss, "forward_ratio": round(sec / fwd, 3),
-            "fd_check": {"directions": 2, "h_rel": 1e-3,
-                         "max_rel_err": fd_err,
+            "loss": float(loss), "forward_ratio": round(sec / fwd, 3),
+            "store_all_states": {"value": round(args.steps / s1, 3),
+                                 "unit": "gradients/s",
+                                 "forward_ratio": round(s1 / f1, 3),
+                                 "memory_gb": round(3 * 4 * n * n * nsteps / 1e9, 1)},
+            "batched_16": {"value": round(batch_rate, 3),
+                           "unit": "instance gradients/s",
+                           "checkpoint_steps": ck,
+                           "note": "16 instances in one handle, one launch per step"},
+            "fd_check": {"directions": ndir,
+                         "max_rel_err": {"h_rel 1e-3": fd_err[1e-3],
+                                         "h_rel 1e-5": fd_err[1e-5]},
                          "note": "directional derivatives of the FP64 "
-                                 "adjoint against central differences of "
-                                 "the FP64 loss, full size"},
+                                 "adjoint along random directions of D "
+                                 "(relative) and all 13 FK parameters "
+                                 "(relative) against central differences of "
+                                 "the FP64 loss, full size; the error "
+                                 "falling as h^2 is the differences' "
+                                 "truncation"},
             "fp32_vs_fp64_gradient_rel_l2": rel,
+            "fp32_vs_fp64_fk_gradient_rel_max": rel_fk,
             "fp64_gradients_per_s": round(fp64_rate, 3),
             "roofline": None, "cpu_baseline": None,
             "e2e": {"value": round(world * args.steps / e2e_s, 3),
                     "unit": "gradients/s", "h2d_bytes_per_step": 4 * n * n,
-                    "d2h_bytes_per_step": 4 * n * n},
+                    "d2h_bytes_per_step": 4 * n * n + 13 * 8},
             "gpu_launches": None, "clocks": clk,
         }
         print(json.dumps(line), flush=True)

@@ -501,7 +501,7 @@ int yh_batch_get_step(yh_batch *b, int *step);
 int yh_batch_get_launch_count(yh_batch *b, long long *n);
 
 /* ------------------------------------------------------------------ */
-/* Layer 5: adjoint (gradient of a probe loss with respect to D(x, y))   */
+/* Layer 5: adjoint (gradients of a probe loss: D(x, y), FK parameters) */
 /* ------------------------------------------------------------------ */
 /* No reference counterpart (the reference has constant D and no
  * gradients). FK3V with a per-cell diffusion coefficient D (nx*ny floats,
@@ -524,6 +524,18 @@ int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
                       int nsteps, int frame_steps, int probe_spacing,
                       int checkpoint_steps, int fp64, double smooth,
                       void *stream, yh_adjoint **out);
+/* `batch` independent instances (1-4096) with the same grid, steps, probes
+ * and FK parameters and their own D, initial state and target, advanced by
+ * one launch per step. Every per-instance array below is then the
+ * instances' arrays one after another (D, u0, v0, w0, grad_D: batch x nx*ny;
+ * target, probes: batch x frames x probes; loss: batch doubles; grad_fk:
+ * batch structs). checkpoint_steps = 1 keeps every state (no recompute:
+ * 3 nx ny nsteps batch values). yh_adjoint_create is batch 1. */
+int yh_adjoint_create_batch(const yh_param_var *p, const yh_fk_params *fk,
+                            int batch, int nsteps, int frame_steps,
+                            int probe_spacing, int checkpoint_steps, int fp64,
+                            double smooth, void *stream, yh_adjoint **out);
+int yh_adjoint_batch(yh_adjoint *h, int *batch);
 int yh_adjoint_destroy(yh_adjoint *h);
 /* Frames (nsteps / frame_steps) and probes (nx / spacing, ny / spacing). */
 int yh_adjoint_probes(yh_adjoint *h, int *frames, int *probes_x,

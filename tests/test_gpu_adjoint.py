@@ -109,7 +109,7 @@ def test_checkpoint_interval_leaves_the_gradient_unchanged():
     import torch
     n, nsteps = 64, 200
     outs = []
-    for ck in (7, 64, 200):
+    for ck in (7, 64, 200, 1):  # 1: every state kept, no recompute
         adj, st, D = problem(n, nsteps, 25, 8, ck, fp64=False)
         g = torch.empty_like(D)
         L = adj.run(D, st, g)
@@ -229,3 +229,46 @@ def test_gradients_match_the_fp64_tangent_linear_oracle(smooth):
           % (L, Lo, ad, dLo))
     assert abs(L - Lo) <= 1e-9 * abs(Lo)
     assert abs(ad - dLo) <= 1e-6 * abs(dLo)
+
+
+@pytest.mark.parametrize("ck", [9, 1])
+def test_batched_instances_equal_single_handles(ck):
+    # three instances (own D, initial state, target) in one handle: each
+    # instance's loss, dLoss/dD and dLoss/dtheta equal to the bit those of a
+    # handle of its own
+    import torch
+    n, nsteps, frame, sp, B = 40, 90, 15, 5, 3
+    p = A.fk_tissue_params(n, n)
+    fk = A.fk_defaults()
+    Ds, sts, tgts, trues = [], [], [], []
+    for b in range(B):
+        D_true = dev(d_map(n, 20 + b))
+        trues.append(D_true)
+        st = [dev(x) for x in start(n)]
+        st[0] = st[0].roll(3 * b)  # a different start per instance
+        one = Adjoint(p, fk, nsteps, frame, sp, ck)
+        t = torch.empty(one.target_shape, dtype=torch.float32, device="cuda")
+        one.record(D_true, st, t)
+        Ds.append(D_true * (1.05 + 0.05 * b))
+        sts.append(st)
+        tgts.append(t)
+    bat = Adjoint(p, fk, nsteps, frame, sp, ck, batch=B)
+    tb = torch.empty(bat.target_shape, dtype=torch.float32, device="cuda")
+    bat.record(torch.cat(trues), [torch.cat([s[q] for s in sts]) for q in range(3)], tb)
+    for b in range(B):  # the batched forward records the same targets
+        assert torch.equal(tb[b], tgts[b])
+    bat.set_target(tb)
+    Dcat = torch.cat(Ds)
+    gb = torch.empty_like(Dcat)
+    gfk = (A.FKParams * B)()
+    Lb = bat.run(Dcat, [torch.cat([s[q] for s in sts]) for q in range(3)], gb, gfk)
+    from yolohtli_gb300.adjoint import fk_array
+    for b in range(B):
+        one = Adjoint(p, fk, nsteps, frame, sp, ck)
+        one.set_target(tgts[b])
+        g = torch.empty_like(Ds[b])
+        f1 = A.FKParams()
+        L1 = one.run(Ds[b], sts[b], g, f1)
+        assert L1 == Lb[b]
+        assert torch.equal(g, gb[b * n * n:(b + 1) * n * n])
+        assert np.array_equal(fk_array(f1), fk_array(gfk[b]))

@@ -78,6 +78,9 @@ SIGNATURES = {
     # adjoint
     "yh_adjoint_create": (_i, [_P(A.ParamVar), _P(A.FKParams), _i, _i, _i, _i,
                                _i, _d, _v, _P(_v)]),
+    "yh_adjoint_create_batch": (_i, [_P(A.ParamVar), _P(A.FKParams), _i, _i, _i,
+                                     _i, _i, _i, C.c_double, _v, _P(_v)]),
+    "yh_adjoint_batch": (_i, [_v, _P(_i)]),
     "yh_adjoint_destroy": (_i, [_v]),
     "yh_adjoint_probes": (_i, [_v, _P(_i), _P(_i), _P(_i)]),
     "yh_adjoint_set_target": (_i, [_v, _v]),

@@ -27,20 +27,26 @@ class Adjoint:
     """One FK3V problem: grid and parameters p (hx == hy), the FK3V
     parameters, nsteps steps, the loss on the states after every
     frame_steps steps at a probe lattice every probe_spacing cells,
-    checkpoints every checkpoint_steps (default ~sqrt(nsteps)); smooth > 0
-    replaces the model's switches by tanh ramps of that width."""
+    checkpoints every checkpoint_steps (default ~sqrt(nsteps); 1 keeps
+    every state); smooth > 0 replaces the model's switches by tanh ramps of
+    that width. batch > 1: that many instances with their own D, initial
+    state and target, one launch per step for all (every per-instance
+    tensor is then batch arrays one after another)."""
 
     def __init__(self, p, fk, nsteps, frame_steps, probe_spacing,
-                 checkpoint_steps=None, fp64=False, smooth=0.0, stream=None):
+                 checkpoint_steps=None, fp64=False, smooth=0.0, stream=None,
+                 batch=1):
         self.lib = load()
         self.p = p.copy()
+        self.batch = int(batch)
         if checkpoint_steps is None:
             checkpoint_steps = max(1, int(round(np.sqrt(nsteps))))
         h = C.c_void_p()
-        check("yh_adjoint_create", self.lib.yh_adjoint_create(
-            C.byref(self.p), C.byref(fk), int(nsteps), int(frame_steps),
-            int(probe_spacing), int(checkpoint_steps), 1 if fp64 else 0,
-            float(smooth), C.c_void_p(stream) if stream else None, C.byref(h)))
+        check("yh_adjoint_create_batch", self.lib.yh_adjoint_create_batch(
+            C.byref(self.p), C.byref(fk), self.batch, int(nsteps),
+            int(frame_steps), int(probe_spacing), int(checkpoint_steps),
+            1 if fp64 else 0, float(smooth),
+            C.c_void_p(stream) if stream else None, C.byref(h)))
         self.h = h
         self.fk = A.FKParams.from_buffer_copy(fk)
         f, px, py = C.c_int(), C.c_int(), C.c_int()
@@ -61,7 +67,8 @@ class Adjoint:
 
     @property
     def target_shape(self):
-        return (self.frames, self.probes_y, self.probes_x)
+        one = (self.frames, self.probes_y, self.probes_x)
+        return one if self.batch == 1 else (self.batch,) + one
 
     def set_target(self, target):
         """target: a device tensor or host array of target_shape floats."""
@@ -83,19 +90,21 @@ class Adjoint:
         self.fk = A.FKParams.from_buffer_copy(fk)
 
     def run(self, D, state0, grad=None, grad_fk=None):
-        """Loss (float) and, with `grad` (device float32 like D), dLoss/dD;
-        with grad_fk (an A.FKParams) also dLoss/d(each FK parameter)."""
-        loss = C.c_double()
+        """Loss and, with `grad` (device float32 like D), dLoss/dD; with
+        grad_fk also dLoss/d(each FK parameter): an A.FKParams (batch 1) or
+        an array of `batch` of them. The loss is a float (batch 1) or an
+        array of one per instance."""
+        loss = (C.c_double * self.batch)()
         _after_torch()
         g = grad.data_ptr() if grad is not None else None
         x = [D.data_ptr()] + [t.data_ptr() for t in state0]
         if grad_fk is not None:
+            ref = C.byref(grad_fk) if isinstance(grad_fk, A.FKParams) else grad_fk
             check("yh_adjoint_run_fk", self.lib.yh_adjoint_run_fk(
-                self.h, *x, C.byref(loss), g, C.byref(grad_fk)))
+                self.h, *x, loss, g, ref))
         else:
-            check("yh_adjoint_run", self.lib.yh_adjoint_run(
-                self.h, *x, C.byref(loss), g))
-        return loss.value
+            check("yh_adjoint_run", self.lib.yh_adjoint_run(self.h, *x, loss, g))
+        return loss[0] if self.batch == 1 else np.array(loss[:])
 
 
 def fk_array(fk):

@@ -201,9 +201,18 @@ __global__ void adj_forward_kernel(const AdjCoeffs<Real> a,
                                    const Real *__restrict__ v,
                                    const Real *__restrict__ w, Real *__restrict__ uo,
                                    Real *__restrict__ vo, Real *__restrict__ wo) {
+  grid_dep_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= a.nx || j >= a.ny) return;
+  const size_t off = (size_t)blockIdx.z * a.nx * a.ny;  // instance
+  r += off;
+  u += off;
+  v += off;
+  w += off;
+  uo += off;
+  vo += off;
+  wo += off;
   const int c = i + a.nx * j;
   const FkLocal<Real> f = fk_local(a, u[c], v[c], w[c], diffusion(a, u, r, i, j));
   uo[c] = f.un;
@@ -226,33 +235,55 @@ __global__ void __launch_bounds__(256)
                        Real *__restrict__ lu_o, Real *__restrict__ lv_o,
                        Real *__restrict__ lw_o, Real *__restrict__ gr,
                        double *__restrict__ gp) {
+  grid_dep_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = a.nx, ny = a.ny;
+  {
+    const size_t off = (size_t)blockIdx.z * nx * ny;  // instance
+    r += off;
+    u += off;
+    v += off;
+    w += off;
+    lu += off;
+    lv += off;
+    lw += off;
+    lu_o += off;
+    lv_o += off;
+    lw_o += off;
+    gr += off;
+  }
   if (PARAMS) {
-    Real g[kNumFk];
-    if (i < nx && j < ny) {
-      const int c = i + nx * j;
-      fk_param_terms(a, u[c], v[c], w[c], lu[c], lv[c], lw[c], g);
-    } else {
+    // the block's 256 x 13 terms through shared memory, transposed: warp
+    // q (0-7) sums rows q and q + 8 (8 values a lane, then a shuffle tree),
+    // far fewer instructions than 13 shuffle trees in every warp
+    __shared__ Real s_g[kNumFk][256];  // blockDim (32, 8)
+    const int t = threadIdx.x + 32 * threadIdx.y;
+    {
+      Real g[kNumFk];
+      if (i < nx && j < ny) {
+        const int c = i + nx * j;
+        fk_param_terms(a, u[c], v[c], w[c], lu[c], lv[c], lw[c], g);
+      } else {
 #pragma unroll
-      for (int k = 0; k < kNumFk; ++k) g[k] = Real(0);
+        for (int k = 0; k < kNumFk; ++k) g[k] = Real(0);
+      }
+#pragma unroll
+      for (int k = 0; k < kNumFk; ++k) s_g[k][t] = g[k];
     }
+    __syncthreads();
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const size_t blk =
+        blockIdx.x + gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
 #pragma unroll
-    for (int k = 0; k < kNumFk; ++k)
+    for (int q = warp; q < kNumFk; q += 8) {
+      Real sum = Real(0);
+#pragma unroll
+      for (int m = 0; m < 8; ++m) sum += s_g[q][lane + 32 * m];
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1)
-        g[k] += __shfl_down_sync(0xffffffffu, g[k], off);
-    __shared__ Real s_g[8][kNumFk];  // blockDim (32, 8)
-    if (threadIdx.x == 0)
-#pragma unroll
-      for (int k = 0; k < kNumFk; ++k) s_g[threadIdx.y][k] = g[k];
-    __syncthreads();
-    const int t = threadIdx.x + 32 * threadIdx.y;
-    if (t < kNumFk) {
-      Real sum = s_g[0][t];
-      for (int q = 1; q < 8; ++q) sum += s_g[q][t];
-      gp[(size_t)(blockIdx.x + gridDim.x * blockIdx.y) * 16 + t] += (double)sum;
+        sum += __shfl_down_sync(0xffffffffu, sum, off);
+      if (lane == 0) gp[blk * 16 + q] += (double)sum;
     }
   }
   if (i >= nx || j >= ny) return;
@@ -304,13 +335,20 @@ __global__ void __launch_bounds__(256)
   gr[c] += g;
 }
 
-// Probe loss of one frame (one block of 256 threads, fixed-order sum) and,
-// with lu != null, its adjoint 2 (u - target) added at the probes.
+// Probe loss of one frame (one block of 256 threads per instance,
+// fixed-order sum) and, with lu != null, its adjoint 2 (u - target) added at
+// the probes. u, lu: instance stride n; target: instance stride tstride;
+// loss: one per instance.
 template <typename Real>
-__global__ void adj_probe_kernel(int nx, int sp, int npx, int npy,
-                                 const Real *__restrict__ u,
+__global__ void adj_probe_kernel(int nx, int sp, int npx, int npy, int n,
+                                 size_t tstride, const Real *__restrict__ u,
                                  const float *__restrict__ target,
                                  double *loss, Real *lu) {
+  grid_dep_wait();
+  u += (size_t)blockIdx.x * n;
+  target += (size_t)blockIdx.x * tstride;
+  if (lu) lu += (size_t)blockIdx.x * n;
+  if (loss) loss += blockIdx.x;
   __shared__ double s[256];
   double acc = 0.0;
   const int np = npx * npy;
@@ -351,12 +389,15 @@ __global__ void adj_widen_kernel(int n, const float *__restrict__ x,
   if (k < n) y[k] = (Real)x[k];
 }
 
-// The probe values of one frame.
+// The probe values of one frame (instance blockIdx.y: u stride n, out
+// stride ostride).
 template <typename Real>
-__global__ void adj_gather_kernel(int nx, int sp, int npx, int npy,
-                                  const Real *__restrict__ u,
+__global__ void adj_gather_kernel(int nx, int sp, int npx, int npy, int n,
+                                  size_t ostride, const Real *__restrict__ u,
                                   float *__restrict__ out) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  u += (size_t)blockIdx.y * n;
+  out += (size_t)blockIdx.y * ostride;
   if (p >= npx * npy) return;
   const int px = p % npx, py = p / npx;
   out[p] = (float)u[(px * sp + sp / 2) + nx * (py * sp + sp / 2)];
@@ -366,6 +407,8 @@ __global__ void adj_gather_kernel(int nx, int sp, int npx, int npy,
 __global__ void adj_param_reduce_kernel(int nb, const double *__restrict__ gp,
                                         double *__restrict__ out) {
   const int k = threadIdx.x;
+  gp += (size_t)blockIdx.x * nb * 16;  // instance
+  out += (size_t)blockIdx.x * 16;
   if (k >= kNumFk) return;
   double s = 0.0;
   for (int b = 0; b < nb; ++b) s += gp[(size_t)b * 16 + k];
@@ -383,22 +426,24 @@ inline int st(cudaError_t e) {
 struct yh_adjoint {
   int fp64 = 0;
   int nx = 0, ny = 0, n = 0;
+  int batch = 1;  // instances: same grid, steps and FK parameters
   int nsteps = 0, frame = 0, sp = 0, npx = 0, npy = 0, ck = 0;
   double rscale = 0;  // r = rscale * D
   cudaStream_t s = nullptr;
   bool own_stream = false;
   AdjCoeffs<float> af{};
   AdjCoeffs<double> ad{};
-  void *ckpt = nullptr;   // checkpoints: (nsteps / ck + 1) states
+  // Every state is [field][instance][cell].
+  void *ckpt = nullptr;   // checkpoints: (nsteps - 1) / ck + 1 states
   void *seg = nullptr;    // one segment of states: ck + 1 states
   void *lam = nullptr;    // two adjoint states (ping-pong)
-  void *r = nullptr;      // r = dt D / h^2
+  void *r = nullptr;      // r = dt D / h^2, [instance][cell]
   void *gr = nullptr;     // gradient with respect to r
-  float *target = nullptr;  // [frames][probes]
-  double *loss = nullptr;
+  float *target = nullptr;  // [instance][frame][probe]
+  double *loss = nullptr;   // [instance]
   double *gp = nullptr;   // per-block FK-parameter accumulators (16 each)
-  double *gfk = nullptr;  // their sum: dL/d(raw FK parameters)
-  int nrev = 0;           // blocks of the reverse launch
+  double *gfk = nullptr;  // their sums: dL/d(raw FK parameters), 16 each
+  int nrev = 0;           // blocks of the reverse launch per instance
   int frames = 0;
   // the whole forward (+ reverse) sequence on the handle's own buffers,
   // captured once: [0] loss only, [1] loss and dL/dD, [2] also the FK
@@ -412,10 +457,11 @@ struct yh_adjoint {
 
 namespace {
 
+// States of all instances: f(state, field) is the base of batch * n cells.
 template <typename Real>
 struct View {
   Real *p;
-  int n;
+  size_t n;  // cells of one field over all instances
   Real *f(int state, int field) const { return p + ((size_t)state * 3 + field) * n; }
 };
 
@@ -429,25 +475,64 @@ const AdjCoeffs<double> &coeffs<double>(const yh_adjoint *h) { return h->ad; }
 template <typename Real>
 cudaError_t fwd(const yh_adjoint *h, const Real *r, const Real *const *x,
                 Real *const *y) {
-  const dim3 b(32, 8), g((h->nx + 31) / 32, (h->ny + 7) / 8);
-  adj_forward_kernel<Real><<<g, b, 0, h->s>>>(coeffs<Real>(h), r, x[0], x[1],
-                                              x[2], y[0], y[1], y[2]);
-  return cudaGetLastError();
+  const dim3 b(32, 8), g((h->nx + 31) / 32, (h->ny + 7) / 8, h->batch);
+  return launch_pdl(adj_forward_kernel<Real>, g, b, 0, h->s, coeffs<Real>(h),
+                    r, x[0], x[1], x[2], y[0], y[1], y[2]);
+}
+
+// Loss of frame f (1-based step / frame) from u, and with lu its adjoint.
+template <typename Real>
+cudaError_t probe(const yh_adjoint *h, int f, const Real *u, double *loss,
+                  Real *lu) {
+  const size_t np = (size_t)h->npx * h->npy;
+  return launch_pdl(adj_probe_kernel<Real>, dim3(h->batch), dim3(256), 0,
+                    h->s, h->nx, h->sp, h->npx, h->npy, h->n,
+                    (size_t)h->frames * np, (const Real *)u,
+                    (const float *)(h->target + (size_t)(f - 1) * np), loss,
+                    lu);
+}
+
+template <typename Real, bool PARAMS>
+cudaError_t rev(const yh_adjoint *h, const Real *r, const Real *const *x,
+                const Real *const *lin, Real *const *lout, Real *gr) {
+  const dim3 b(32, 8), g((h->nx + 31) / 32, (h->ny + 7) / 8, h->batch);
+  return launch_pdl(adj_reverse_kernel<Real, PARAMS>, g, b, 0, h->s,
+                    coeffs<Real>(h), r, (const Real *)x[0], (const Real *)x[1],
+                    (const Real *)x[2], (const Real *)lin[0],
+                    (const Real *)lin[1], (const Real *)lin[2], lout[0],
+                    lout[1], lout[2], gr, PARAMS ? h->gp : (double *)nullptr);
 }
 
 // The forward pass (checkpoints, loss) and, with grad, the reverse sweep,
 // on the handle's buffers only: r and checkpoint 0 hold the inputs. Its
-// launches are captured into a CUDA graph by run_t.
+// launches are captured into a CUDA graph by run_t. With ck == 1 every
+// state is kept (no recompute): the checkpoints are states 0 .. T-1 and
+// the forward pass writes them in place.
 template <typename Real>
 cudaError_t run_body(yh_adjoint *h, bool grad, bool params) {
-  const int n = h->n, T = h->nsteps, ck = h->ck;
+  const size_t n = (size_t)h->n * h->batch;
+  const int T = h->nsteps, ck = h->ck;
+  const bool all = ck == 1;
   const View<Real> C{(Real *)h->ckpt, n}, S{(Real *)h->seg, n}, L{(Real *)h->lam, n};
   Real *r = (Real *)h->r, *gr = (Real *)h->gr;
-  cudaError_t e = cudaMemsetAsync(h->loss, 0, sizeof(double), h->s);
+  auto st3 = [](const View<Real> &V, int k, Real **out) {
+    for (int q = 0; q < 3; ++q) out[q] = V.f(k, q);
+  };
+  cudaError_t e = cudaMemsetAsync(h->loss, 0, h->batch * sizeof(double), h->s);
   // forward: checkpoints every ck steps, the loss at every frame
-  {
-    Real *cur[3] = {S.f(0, 0), S.f(0, 1), S.f(0, 2)};
-    Real *nxt[3] = {S.f(1, 0), S.f(1, 1), S.f(1, 2)};
+  if (all) {
+    for (int t = 0; t < T && e == cudaSuccess; ++t) {
+      Real *x[3], *y[3];
+      st3(C, t, x);
+      if (t + 1 < T) st3(C, t + 1, y); else st3(S, 0, y);
+      e = fwd<Real>(h, r, x, y);
+      if (e == cudaSuccess && (t + 1) % h->frame == 0)
+        e = probe<Real>(h, (t + 1) / h->frame, y[0], h->loss, nullptr);
+    }
+  } else {
+    Real *cur[3], *nxt[3];
+    st3(S, 0, cur);
+    st3(S, 1, nxt);
     for (int q = 0; q < 3 && e == cudaSuccess; ++q)
       e = cudaMemcpyAsync(cur[q], C.f(0, q), n * sizeof(Real),
                           cudaMemcpyDeviceToDevice, h->s);
@@ -455,13 +540,8 @@ cudaError_t run_body(yh_adjoint *h, bool grad, bool params) {
       e = fwd<Real>(h, r, cur, nxt);
       for (int q = 0; q < 3; ++q) std::swap(cur[q], nxt[q]);
       const int step = t + 1;
-      if (e == cudaSuccess && step % h->frame == 0) {
-        adj_probe_kernel<Real><<<1, 256, 0, h->s>>>(
-            h->nx, h->sp, h->npx, h->npy, cur[0],
-            h->target + (size_t)(step / h->frame - 1) * h->npx * h->npy,
-            h->loss, nullptr);
-        e = cudaGetLastError();
-      }
+      if (e == cudaSuccess && step % h->frame == 0)
+        e = probe<Real>(h, step / h->frame, cur[0], h->loss, nullptr);
       if (e == cudaSuccess && step % ck == 0 && step < T)
         for (int q = 0; q < 3 && e == cudaSuccess; ++q)
           e = cudaMemcpyAsync(C.f(step / ck, q), cur[q], n * sizeof(Real),
@@ -473,63 +553,77 @@ cudaError_t run_body(yh_adjoint *h, bool grad, bool params) {
   e = cudaMemsetAsync(L.f(0, 0), 0, 3 * n * sizeof(Real), h->s);
   if (e == cudaSuccess) e = cudaMemsetAsync(gr, 0, n * sizeof(Real), h->s);
   if (e == cudaSuccess && params)
-    e = cudaMemsetAsync(h->gp, 0, (size_t)h->nrev * 16 * sizeof(double), h->s);
+    e = cudaMemsetAsync(h->gp, 0, (size_t)h->batch * h->nrev * 16 * sizeof(double),
+                        h->s);
   int li = 0;  // lambda^{t+1} lives in L state li
-  for (int s0 = ((T - 1) / ck) * ck; s0 >= 0 && e == cudaSuccess; s0 -= ck) {
-    const int s1 = std::min(s0 + ck, T);  // states s0 .. s1
-    for (int q = 0; q < 3 && e == cudaSuccess; ++q)
-      e = cudaMemcpyAsync(S.f(0, q), C.f(s0 / ck, q), n * sizeof(Real),
-                          cudaMemcpyDeviceToDevice, h->s);
-    for (int t = s0; t < s1 && e == cudaSuccess; ++t) {
-      Real *x[3] = {S.f(t - s0, 0), S.f(t - s0, 1), S.f(t - s0, 2)};
-      Real *y[3] = {S.f(t - s0 + 1, 0), S.f(t - s0 + 1, 1), S.f(t - s0 + 1, 2)};
-      e = fwd<Real>(h, r, x, y);
+  // one reverse step: lambda^t += dL/dx^t (u^t = ut), then lambda^{t-1}
+  // from lambda^t and x^{t-1}
+  auto back = [&](int t, const Real *ut, Real *const *xp) {
+    cudaError_t er = cudaSuccess;
+    if (t % h->frame == 0) er = probe<Real>(h, t / h->frame, ut, nullptr, L.f(li, 0));
+    Real *lin[3], *lout[3];
+    st3(L, li, lin);
+    st3(L, li ^ 1, lout);
+    if (er == cudaSuccess)
+      er = params ? rev<Real, true>(h, r, xp, lin, lout, gr)
+                  : rev<Real, false>(h, r, xp, lin, lout, gr);
+    li ^= 1;
+    return er;
+  };
+  if (all) {
+    for (int t = T; t > 0 && e == cudaSuccess; --t) {
+      Real *xp[3];
+      st3(C, t - 1, xp);
+      e = back(t, t == T ? S.f(0, 0) : C.f(t, 0), xp);
     }
-    for (int t = s1; t > s0 && e == cudaSuccess; --t) {
-      // lambda^t += dL/dx^t, then lambda^{t-1} from lambda^t and x^{t-1}
-      if (t % h->frame == 0) {
-        adj_probe_kernel<Real><<<1, 256, 0, h->s>>>(
-            h->nx, h->sp, h->npx, h->npy, S.f(t - s0, 0),
-            h->target + (size_t)(t / h->frame - 1) * h->npx * h->npy, nullptr,
-            L.f(li, 0));
-        e = cudaGetLastError();
-        if (e != cudaSuccess) break;
+  } else {
+    for (int s0 = ((T - 1) / ck) * ck; s0 >= 0 && e == cudaSuccess; s0 -= ck) {
+      const int s1 = std::min(s0 + ck, T);  // states s0 .. s1
+      for (int q = 0; q < 3 && e == cudaSuccess; ++q)
+        e = cudaMemcpyAsync(S.f(0, q), C.f(s0 / ck, q), n * sizeof(Real),
+                            cudaMemcpyDeviceToDevice, h->s);
+      for (int t = s0; t < s1 && e == cudaSuccess; ++t) {
+        Real *x[3], *y[3];
+        st3(S, t - s0, x);
+        st3(S, t - s0 + 1, y);
+        e = fwd<Real>(h, r, x, y);
       }
-      const dim3 b(32, 8), g((h->nx + 31) / 32, (h->ny + 7) / 8);
-      if (params)
-        adj_reverse_kernel<Real, true><<<g, b, 0, h->s>>>(
-            coeffs<Real>(h), r, S.f(t - 1 - s0, 0), S.f(t - 1 - s0, 1),
-            S.f(t - 1 - s0, 2), L.f(li, 0), L.f(li, 1), L.f(li, 2),
-            L.f(li ^ 1, 0), L.f(li ^ 1, 1), L.f(li ^ 1, 2), gr, h->gp);
-      else
-        adj_reverse_kernel<Real, false><<<g, b, 0, h->s>>>(
-            coeffs<Real>(h), r, S.f(t - 1 - s0, 0), S.f(t - 1 - s0, 1),
-            S.f(t - 1 - s0, 2), L.f(li, 0), L.f(li, 1), L.f(li, 2),
-            L.f(li ^ 1, 0), L.f(li ^ 1, 1), L.f(li ^ 1, 2), gr, nullptr);
-      e = cudaGetLastError();
-      li ^= 1;
+      for (int t = s1; t > s0 && e == cudaSuccess; --t) {
+        Real *xp[3];
+        st3(S, t - 1 - s0, xp);
+        e = back(t, S.f(t - s0, 0), xp);
+      }
     }
   }
   if (e == cudaSuccess && params) {
-    adj_param_reduce_kernel<<<1, 32, 0, h->s>>>(h->nrev, h->gp, h->gfk);
+    adj_param_reduce_kernel<<<h->batch, 32, 0, h->s>>>(h->nrev, h->gp, h->gfk);
     e = cudaGetLastError();
   }
   return e;
 }
 
+// The inputs (D, u0, v0, w0: batch * n floats each) into r and state 0 of
+// the checkpoints.
+template <typename Real>
+cudaError_t load_inputs(yh_adjoint *h, const float *D, const float *u0,
+                        const float *v0, const float *w0, Real *state0) {
+  const size_t n = (size_t)h->n * h->batch;
+  const int nb = (int)((n + 255) / 256);
+  adj_to_r_kernel<Real><<<nb, 256, 0, h->s>>>((int)n, (Real)h->rscale, D, (Real *)h->r);
+  const float *x0[3] = {u0, v0, w0};
+  for (int q = 0; q < 3; ++q)
+    adj_widen_kernel<Real><<<nb, 256, 0, h->s>>>((int)n, x0[q], state0 + q * n);
+  return cudaGetLastError();
+}
+
 template <typename Real>
 int run_t(yh_adjoint *h, const float *D, const float *u0, const float *v0,
           const float *w0, double *loss_out, float *grad, double *graw) {
-  const int n = h->n;
-  const View<Real> C{(Real *)h->ckpt, n};
-  const int nb = (n + 255) / 256;
+  const size_t n = (size_t)h->n * h->batch;
+  const int nb = (int)((n + 255) / 256);
   // the inputs into the handle's buffers (outside the graph: the caller's
   // pointers may change from run to run)
-  adj_to_r_kernel<Real><<<nb, 256, 0, h->s>>>(n, (Real)h->rscale, D, (Real *)h->r);
-  const float *x0[3] = {u0, v0, w0};
-  for (int q = 0; q < 3; ++q)
-    adj_widen_kernel<Real><<<nb, 256, 0, h->s>>>(n, x0[q], C.f(0, q));
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = load_inputs<Real>(h, D, u0, v0, w0, (Real *)h->ckpt);
   if (e != cudaSuccess) return st(e);
   const bool want_grad = grad != nullptr || graw != nullptr;
   cudaGraphExec_t &ex = h->graph[graw ? 2 : (want_grad ? 1 : 0)];
@@ -553,14 +647,15 @@ int run_t(yh_adjoint *h, const float *D, const float *u0, const float *v0,
   e = cudaGraphLaunch(ex, h->s);
   if (e == cudaSuccess && grad) {
     // dL/dD = dL/dr * dt / h^2
-    adj_scale_kernel<Real><<<nb, 256, 0, h->s>>>(n, (Real)h->rscale,
+    adj_scale_kernel<Real><<<nb, 256, 0, h->s>>>((int)n, (Real)h->rscale,
                                                  (const Real *)h->gr, grad);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && loss_out)
-    e = cudaMemcpyAsync(loss_out, h->loss, sizeof(double), cudaMemcpyDeviceToHost, h->s);
+    e = cudaMemcpyAsync(loss_out, h->loss, h->batch * sizeof(double),
+                        cudaMemcpyDeviceToHost, h->s);
   if (e == cudaSuccess && graw)
-    e = cudaMemcpyAsync(graw, h->gfk, kNumFk * sizeof(double),
+    e = cudaMemcpyAsync(graw, h->gfk, (size_t)h->batch * 16 * sizeof(double),
                         cudaMemcpyDeviceToHost, h->s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
   return st(e);
@@ -570,15 +665,11 @@ int run_t(yh_adjoint *h, const float *D, const float *u0, const float *v0,
 template <typename Real>
 int record_t(yh_adjoint *h, const float *D, const float *u0, const float *v0,
              const float *w0, float *probes) {
-  const int n = h->n, T = h->nsteps, np = h->npx * h->npy;
+  const size_t n = (size_t)h->n * h->batch;
+  const int T = h->nsteps, np = h->npx * h->npy;
   const View<Real> S{(Real *)h->seg, n};
   Real *r = (Real *)h->r;
-  const int nb = (n + 255) / 256;
-  adj_to_r_kernel<Real><<<nb, 256, 0, h->s>>>(n, (Real)h->rscale, D, r);
-  const float *x0[3] = {u0, v0, w0};
-  for (int q = 0; q < 3; ++q)
-    adj_widen_kernel<Real><<<nb, 256, 0, h->s>>>(n, x0[q], S.f(0, q));
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = load_inputs<Real>(h, D, u0, v0, w0, S.f(0, 0));
   Real *cur[3] = {S.f(0, 0), S.f(0, 1), S.f(0, 2)};
   Real *nxt[3] = {S.f(1, 0), S.f(1, 1), S.f(1, 2)};
   for (int t = 0; t < T && e == cudaSuccess; ++t) {
@@ -586,8 +677,9 @@ int record_t(yh_adjoint *h, const float *D, const float *u0, const float *v0,
     for (int q = 0; q < 3; ++q) std::swap(cur[q], nxt[q]);
     if (e == cudaSuccess && (t + 1) % h->frame == 0) {
       const int f = (t + 1) / h->frame - 1;
-      adj_gather_kernel<Real><<<(np + 255) / 256, 256, 0, h->s>>>(
-          h->nx, h->sp, h->npx, h->npy, cur[0], probes + (size_t)f * np);
+      adj_gather_kernel<Real><<<dim3((np + 255) / 256, h->batch), 256, 0, h->s>>>(
+          h->nx, h->sp, h->npx, h->npy, h->n, (size_t)h->frames * np, cur[0],
+          probes + (size_t)f * np);
       e = cudaGetLastError();
     }
   }
@@ -646,17 +738,19 @@ extern "C" int yh_adjoint_destroy(yh_adjoint *h) {
   return YH_OK;
 }
 
-extern "C" int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
-                                 int nsteps, int frame_steps, int probe_spacing,
-                                 int checkpoint_steps, int fp64, double smooth,
-                                 void *stream, yh_adjoint **out) {
+extern "C" int yh_adjoint_create_batch(const yh_param_var *p,
+                                       const yh_fk_params *fk, int batch,
+                                       int nsteps, int frame_steps,
+                                       int probe_spacing, int checkpoint_steps,
+                                       int fp64, double smooth, void *stream,
+                                       yh_adjoint **out) {
   if (!out) return YH_EINVAL;
   *out = nullptr;
   int rc = check_params(p, YH_MODEL_FK3V, fk);
   if (rc) return rc;
-  if (p->hx != p->hy || nsteps < 1 || frame_steps < 1 || probe_spacing < 1 ||
-      probe_spacing > p->nx || probe_spacing > p->ny || checkpoint_steps < 1 ||
-      !(smooth >= 0.0))
+  if (p->hx != p->hy || batch < 1 || batch > 4096 || nsteps < 1 ||
+      frame_steps < 1 || probe_spacing < 1 || probe_spacing > p->nx ||
+      probe_spacing > p->ny || checkpoint_steps < 1 || !(smooth >= 0.0))
     return YH_EINVAL;
   yh_adjoint *h = new (std::nothrow) yh_adjoint();
   if (!h) return YH_ENOMEM;
@@ -665,6 +759,7 @@ extern "C" int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
   h->nx = p->nx;
   h->ny = p->ny;
   h->n = p->nx * p->ny;
+  h->batch = batch;
   h->nsteps = nsteps;
   h->frame = frame_steps;
   h->sp = probe_spacing;
@@ -678,8 +773,11 @@ extern "C" int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
   h->pv = *p;
   set_coeffs(h, fk);
   const size_t es = h->fp64 ? sizeof(double) : sizeof(float);
-  const size_t state = 3 * (size_t)h->n * es;
+  const size_t cells = (size_t)h->n * batch;
+  const size_t state = 3 * cells * es;
   const size_t nck = (size_t)(nsteps - 1) / checkpoint_steps + 1;
+  const size_t nseg = checkpoint_steps == 1 ? 1 : (size_t)checkpoint_steps + 1;
+  const size_t tgt = (size_t)std::max(1, h->frames) * h->npx * h->npy * batch;
   cudaError_t e = cudaSuccess;
   h->s = (cudaStream_t)stream;
   if (!h->s) {
@@ -687,18 +785,16 @@ extern "C" int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
     h->own_stream = e == cudaSuccess;
   }
   if (e == cudaSuccess) e = cudaMalloc(&h->ckpt, nck * state);
-  if (e == cudaSuccess) e = cudaMalloc(&h->seg, (size_t)(checkpoint_steps + 1) * state);
+  if (e == cudaSuccess) e = cudaMalloc(&h->seg, std::max<size_t>(nseg, 2) * state);
   if (e == cudaSuccess) e = cudaMalloc(&h->lam, 2 * state);
-  if (e == cudaSuccess) e = cudaMalloc(&h->r, h->n * es);
-  if (e == cudaSuccess) e = cudaMalloc(&h->gr, h->n * es);
+  if (e == cudaSuccess) e = cudaMalloc(&h->r, cells * es);
+  if (e == cudaSuccess) e = cudaMalloc(&h->gr, cells * es);
+  if (e == cudaSuccess) e = cudaMalloc(&h->target, tgt * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&h->loss, batch * sizeof(double));
   if (e == cudaSuccess)
-    e = cudaMalloc(&h->target, (size_t)std::max(1, h->frames) * h->npx * h->npy * sizeof(float));
-  if (e == cudaSuccess) e = cudaMalloc(&h->loss, sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&h->gp, (size_t)h->nrev * 16 * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&h->gfk, 16 * sizeof(double));
-  if (e == cudaSuccess)
-    e = cudaMemsetAsync(h->target, 0,
-                        (size_t)std::max(1, h->frames) * h->npx * h->npy * sizeof(float), h->s);
+    e = cudaMalloc(&h->gp, (size_t)batch * h->nrev * 16 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&h->gfk, (size_t)batch * 16 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->target, 0, tgt * sizeof(float), h->s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
   if (e != cudaSuccess) {
     yh_adjoint_destroy(h);
@@ -708,11 +804,20 @@ extern "C" int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
   return YH_OK;
 }
 
+extern "C" int yh_adjoint_create(const yh_param_var *p, const yh_fk_params *fk,
+                                 int nsteps, int frame_steps, int probe_spacing,
+                                 int checkpoint_steps, int fp64, double smooth,
+                                 void *stream, yh_adjoint **out) {
+  return yh_adjoint_create_batch(p, fk, 1, nsteps, frame_steps, probe_spacing,
+                                 checkpoint_steps, fp64, smooth, stream, out);
+}
+
 extern "C" int yh_adjoint_set_target(yh_adjoint *h, const float *target) {
   if (!h || !target) return YH_EINVAL;
-  cudaError_t e = cudaMemcpyAsync(h->target, target,
-                                  (size_t)h->frames * h->npx * h->npy * sizeof(float),
-                                  cudaMemcpyDefault, h->s);
+  cudaError_t e = cudaMemcpyAsync(
+      h->target, target,
+      (size_t)h->batch * h->frames * h->npx * h->npy * sizeof(float),
+      cudaMemcpyDefault, h->s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
   return st(e);
 }
@@ -723,6 +828,12 @@ extern "C" int yh_adjoint_probes(yh_adjoint *h, int *frames, int *probes_x,
   if (frames) *frames = h->frames;
   if (probes_x) *probes_x = h->npx;
   if (probes_y) *probes_y = h->npy;
+  return YH_OK;
+}
+
+extern "C" int yh_adjoint_batch(yh_adjoint *h, int *batch) {
+  if (!h || !batch) return YH_EINVAL;
+  *batch = h->batch;
   return YH_OK;
 }
 
@@ -739,31 +850,40 @@ extern "C" int yh_adjoint_run_fk(yh_adjoint *h, const float *D,
                                  const float *w0, double *loss, float *grad_D,
                                  yh_fk_params *grad_fk) {
   if (!h || !D || !u0 || !v0 || !w0 || !grad_fk) return YH_EINVAL;
-  double g[16];
+  double *g = new (std::nothrow) double[(size_t)h->batch * 16];
+  if (!g) return YH_ENOMEM;
   const int rc = h->fp64 ? run_t<double>(h, D, u0, v0, w0, loss, grad_D, g)
                          : run_t<float>(h, D, u0, v0, w0, loss, grad_D, g);
-  if (rc) return rc;
+  if (rc) {
+    delete[] g;
+    return rc;
+  }
   // chain rule from the raw parameters: s_X = tc dt / tau_X, so
   // ds_X/dtau_X = -s_X / tau_X; k2 = -2k / ln 2
   const yh_fk_params &f = h->fk;
   const double tau[9] = {f.tau_d, f.tau_r, f.tau_si, f.tau_0, f.tau_v_plus,
                          f.tau_v1_minus, f.tau_v2_minus, f.tau_w_plus,
                          f.tau_w_minus};
-  double out[9];
-  for (int q = 0; q < 9; ++q) out[q] = -g[q] * h->tcdt / (tau[q] * tau[q]);
-  grad_fk->tau_d = out[0];
-  grad_fk->tau_r = out[1];
-  grad_fk->tau_si = out[2];
-  grad_fk->tau_0 = out[3];
-  grad_fk->tau_v_plus = out[4];
-  grad_fk->tau_v1_minus = out[5];
-  grad_fk->tau_v2_minus = out[6];
-  grad_fk->tau_w_plus = out[7];
-  grad_fk->tau_w_minus = out[8];
-  grad_fk->u_c = g[9];
-  grad_fk->u_v = g[10];
-  grad_fk->u_csi = g[11];
-  grad_fk->k = g[12] * (-2.0 / log(2.0));
+  for (int b = 0; b < h->batch; ++b) {
+    const double *gb = g + (size_t)b * 16;
+    double o[9];
+    for (int q = 0; q < 9; ++q) o[q] = -gb[q] * h->tcdt / (tau[q] * tau[q]);
+    yh_fk_params &d = grad_fk[b];
+    d.tau_d = o[0];
+    d.tau_r = o[1];
+    d.tau_si = o[2];
+    d.tau_0 = o[3];
+    d.tau_v_plus = o[4];
+    d.tau_v1_minus = o[5];
+    d.tau_v2_minus = o[6];
+    d.tau_w_plus = o[7];
+    d.tau_w_minus = o[8];
+    d.u_c = gb[9];
+    d.u_v = gb[10];
+    d.u_csi = gb[11];
+    d.k = gb[12] * (-2.0 / log(2.0));
+  }
+  delete[] g;
   return YH_OK;
 }
 
