@@ -431,6 +431,20 @@ def sr_params(p, tip, radius=160):
     return q
 
 
+def sr_roofline(rate, cells):
+    """The SR step against HBM: 84 algorithmic bytes per cell-step (RD 24,
+    BFECC 24, the integral pass's state reads 12, the frozen template's
+    derivative fields 24) x cells x SR steps/s."""
+    peak, kind = measured_peaks()
+    achieved = 84.0 * cells * rate / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+            "peak_kind": kind, "alg_bytes_per_cell_step": 84,
+            "kernel": "the SR step (6 kernels and a memset)",
+            "note": "latency-bound: five dependent launches of 0.1-0.26 M "
+                    "cells per step; see profiles/sr_step_fk3v_512.md"}
+
+
 def run_sr(args):
     """The symmetry-reduced spiral: FK3V FP32 on 512^2, every step RD, tips,
     slices, the 12 phase-condition integrals in FP64, the FP64 3x3 solve,
@@ -452,21 +466,24 @@ def run_sr(args):
     q = sr_params(p, (float(tips[0, 0]), float(tips[0, 1])))
     N = n * n
 
-    def timed(m, k):
+    def timed(m, k, profile=False):
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         l0 = m.launch_count()
-        e0.record()
+        if profile:  # the range `ncu --profile-from-start off` captures
+            torch.cuda.profiler.start()
         t0 = time.perf_counter()
+        marks = []
         for _ in range(k):
             m.sr_step(nsr)
-        m.synchronize()
-        e1.record()
-        torch.cuda.synchronize()
+            m.synchronize()
+            marks.append(time.perf_counter())
         wall = time.perf_counter() - t0
-        return wall, m.launch_count() - l0
+        if profile:
+            torch.cuda.profiler.stop()
+        per = [1e3 * (b - a) for a, b in zip([t0] + marks[:-1], marks)]
+        return wall, m.launch_count() - l0, per
 
-    rates, status, launches, clk = {}, {}, 0, None
+    rates, status, launches, clk, step_ms = {}, {}, 0, None, []
     for tau_d in (0.25, 0.35, 0.45):
         f = A.FKParams.from_buffer_copy(fk)
         f.tau_d = tau_d
@@ -479,14 +496,38 @@ def run_sr(args):
         if tau_d == 0.25:
             clocks = ClockSampler(env_int("LOCAL_RANK", 0))
             clocks.start()
-        wall, nl = timed(m, K)
+        wall, nl, per = timed(m, K, profile=tau_d == 0.25)
         if tau_d == 0.25:
             clk = clocks.stop()
             launches = nl
+            step_ms = [round(x, 2) for x in per]
         sym = m.get_sym()
         rates[tau_d] = K * nsr / wall
         status[tau_d] = dict(status=sym.status, c=[round(x, 6) for x in sym.c],
                              ntips=sym.ntips)
+        m.close()
+    # the three tau_d runs at once, one handle and stream each: one 512^2
+    # SR run leaves most of the GPU idle (latency-bound launches)
+    streams = [torch.cuda.Stream() for _ in range(3)]
+    runs = []
+    for tau_d, sm in zip((0.25, 0.35, 0.45), streams):
+        f = A.FKParams.from_buffer_copy(fk)
+        f.tau_d = tau_d
+        m = Monodomain(q, A.YH_MODEL_FK3V, f, stream=sm.cuda_stream)
+        m.set_state(*st)
+        m.sr_begin(A.YH_TEMPLATE_FROZEN, template=st)
+        m.sr_step(nsr // 4)
+        runs.append(m)
+    for m in runs:
+        m.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        for m in runs:
+            m.sr_step(nsr)
+    for m in runs:
+        m.synchronize()
+    concurrent = 3 * K * nsr / (time.perf_counter() - t0)
+    for m in runs:
         m.close()
     # the template retaken every step
     m = Monodomain(q, A.YH_MODEL_FK3V, fk)
@@ -494,7 +535,7 @@ def run_sr(args):
     m.sr_begin(A.YH_TEMPLATE_CURRENT)
     m.sr_step(nsr // 4)
     m.synchronize()
-    wall, _ = timed(m, 1)
+    wall, _, _ = timed(m, 1)
     current = nsr / wall
     # end to end: the state from pinned host memory each step, the state and
     # the drift/rotation read back at its end
@@ -555,16 +596,21 @@ def run_sr(args):
                    "l2": "state 3 MB: L2-resident (SR steps are latency-bound)",
                    "parallelism": "replicas x1"},
         "gcell_steps_per_s": round(v * N / 1e9, 3),
+        "step_ms": step_ms,
         "tau_d_sweep": {str(k): round(x, 2) for k, x in rates.items()},
         "sym": {str(k): x for k, x in status.items()},
         "current_template": {"value": round(current, 2), "unit": "SR steps/s"},
+        "three_runs_concurrent": {"value": round(concurrent, 2),
+                                  "unit": "SR steps/s (sum of the 3 tau_d runs)",
+                                  "note": "one handle and stream per run"},
         "compat_fp64_reference_sequence": {
             "value": round(compat_rate, 2), "unit": "SR steps/s",
             "model": "REF2V FP64",
             "sequence": "main.cu:894-954 through the drop-in symbols from "
                         "Python: 12 integral read-backs and a host solve "
                         "per step, as the reference"},
-        "roofline": None, "cpu_baseline": cpu,
+        "roofline": sr_roofline(v, N),
+        "cpu_baseline": cpu,
         "e2e": {"value": round(e2e, 2), "unit": "SR steps/s",
                 "h2d_bytes_per_step": 3 * 4 * N,
                 "d2h_bytes_per_step": 3 * 4 * N + C.sizeof(A.SymState)},

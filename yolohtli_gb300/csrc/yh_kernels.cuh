@@ -214,6 +214,42 @@ __host__ __device__ inline int solve3(const double I[12], double pt,
                                       double c[3]) {
   return solve3_cs(I, cos(pt), sin(pt), c);
 }
+// The same system by cofactors (Cramer's rule): one reciprocal and a short
+// chain of FMAs instead of the pivoted elimination's dependent divisions,
+// for the FP32 engine's last block, where this chain is serial FP64 work.
+// YH_ESINGULAR when |det| <= 1e-13 amax^3 (amax the largest entry), or the
+// system is not finite.
+__host__ __device__ inline int solve3_cofactor(const double I[12], double cs,
+                                               double sn, double c[3]) {
+  double A[3][3], b[3];
+  double amax = 0.0;
+  for (int r = 0; r < 3; ++r) {
+    A[r][0] = I[3 * r] * cs + I[3 * r + 1] * sn;
+    A[r][1] = I[3 * r + 1] * cs - I[3 * r] * sn;
+    A[r][2] = I[3 * r + 2];
+    b[r] = I[9 + r];
+    for (int k = 0; k < 3; ++k) amax = fmax(amax, fabs(A[r][k]));
+  }
+  if (!(amax > 0.0) || !isfinite(amax)) return YH_ESINGULAR;
+  // cofactors C[r][k] of A
+  const double C00 = A[1][1] * A[2][2] - A[1][2] * A[2][1];
+  const double C01 = A[1][2] * A[2][0] - A[1][0] * A[2][2];
+  const double C02 = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+  const double C10 = A[0][2] * A[2][1] - A[0][1] * A[2][2];
+  const double C11 = A[0][0] * A[2][2] - A[0][2] * A[2][0];
+  const double C12 = A[0][1] * A[2][0] - A[0][0] * A[2][1];
+  const double C20 = A[0][1] * A[1][2] - A[0][2] * A[1][1];
+  const double C21 = A[0][2] * A[1][0] - A[0][0] * A[1][2];
+  const double C22 = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+  const double det = A[0][0] * C00 + A[0][1] * C01 + A[0][2] * C02;
+  if (!(fabs(det) > 1e-13 * amax * amax * amax) || !isfinite(det))
+    return YH_ESINGULAR;
+  const double inv = 1.0 / det;
+  c[0] = (C00 * b[0] + C10 * b[1] + C20 * b[2]) * inv;
+  c[1] = (C01 * b[0] + C11 * b[1] + C21 * b[2]) * inv;
+  c[2] = (C02 * b[0] + C12 * b[1] + C22 * b[2]) * inv;
+  return YH_OK;
+}
 cudaError_t launch_sym_advance(const yh_param_var &p, yh_sym_state *sym,
                                cudaStream_t s);
 

@@ -148,6 +148,43 @@ __device__ __forceinline__ void tip_cell(const TipArgs &a, int i, int j,
                    cap, plot);
 }
 
+// tip_cell for FP32 levels: the same FP64 products, sums and square root
+// (where the cancellation is), the four root divisions in FP32 on the
+// rounded numerators and denominators. The roots kept lie in (0, 1), so
+// the change is about 1e-7 of a cell, and the FP64 chain a candidate waits
+// on is ~40 instructions shorter.
+template <bool GRAD, typename Real>
+__device__ __forceinline__ void tip_cell_f32div(
+    const TipArgs &a, int i, int j, double x1, double x2, double x3, double x4,
+    double y1, double y2, double y3, double y4, bool need_disc, float ptime,
+    const Real *present, int *count, yh_tip *vec, int cap, uint8_t *plot) {
+  const double Uth = a.Uth;
+  const double x3y1 = x3 * y1, x4y1 = x4 * y1, x3y2 = x3 * y2, x4y2 = x4 * y2;
+  const double x1y3 = x1 * y3, x2y3 = x2 * y3, x1y4 = x1 * y4, x2y4 = x2 * y4;
+  const double x2y1 = x2 * y1, x1y2 = x1 * y2, x4y3 = x4 * y3, x3y4 = x3 * y4;
+  const double den1 =
+      2.0 * (x3y1 - x4y1 - x3y2 + x4y2 - x1y3 + x2y3 + x1y4 - x2y4);
+  const double den2 =
+      2.0 * (x2y1 - x3y1 - x1y2 + x4y2 + x1y3 - x4y3 - x2y4 + x3y4);
+  const double ctn1 = x1 - x2 + x3 - x4 - y1 + y2 - y3 + y4;
+  const double ctn2 = x3y1 - 2.0 * x4y1 + x4y2 - x1y3 + 2.0 * x1y4 - x2y4;
+  const double disc =
+      sqrt(4.0 * (x3y1 - x3y2 - x4y1 + x4y2 - x1y3 + x1y4 + x2y3 - x2y4) *
+               (x4y1 - x1y4 + Uth * (x1 - x4 - y1 + y4)) +
+           (-ctn2 + Uth * ctn1) * (-ctn2 + Uth * ctn1));
+  const double px = ctn2 - Uth * ctn1;
+  const double py =
+      Uth * ctn1 - x3y1 + x4y2 + x1y3 - x2y4 + 2.0 * (x2y1 - x1y2);
+  if (need_disc && !(disc >= 0.0)) return;
+  const float d1 = (float)den1, d2 = (float)den2;
+  tip_record<GRAD>(a, i, j, __fdiv_rn((float)(px + disc), d1),
+                   __fdiv_rn((float)(py + disc), d2), ptime, present, count,
+                   vec, cap, plot);
+  tip_record<GRAD>(a, i, j, __fdiv_rn((float)(px - disc), d1),
+                   __fdiv_rn((float)(py - disc), d2), ptime, present, count,
+                   vec, cap, plot);
+}
+
 __device__ __forceinline__ bool near(double x, double y, double tol) {
   return x == y || (x <= y + tol && x >= y - tol);  // equals (helper_functions.cu:58-62)
 }
@@ -335,8 +372,9 @@ __global__ void __launch_bounds__(256)
       const int cj = blockIdx.y * 8 * kTipRows + s_cell[k].y;
       Real x[4], y[4];
       tip_corners(a, past, present, ci, cj, x, y);
-      tip_cell<GRAD>(a, ci, cj, x[0], x[1], x[2], x[3], y[0], y[1], y[2],
-                     y[3], !HOLES, ptime, present, count, vec, cap, plot);
+      tip_cell_f32div<GRAD>(a, ci, cj, x[0], x[1], x[2], x[3], y[0], y[1],
+                            y[2], y[3], !HOLES, ptime, present, count, vec,
+                            cap, plot);
     }
   } else {
     const int j = blockIdx.y * 8 + threadIdx.y;
@@ -702,7 +740,7 @@ __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
     double sn, cs;
     sincos(sym->phi[2], &sn, &cs);
     double c[3];
-    const int stt = solve3_cs(I, cs, sn, c);
+    const int stt = solve3_cofactor(I, cs, sn, c);
     sym->status = stt;
     if (stt == YH_OK)
       for (int kk = 0; kk < 3; ++kk) sym->c[kk] = c[kk];
