@@ -440,8 +440,8 @@ def sr_roofline(rate, cells):
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
             "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
             "peak_kind": kind, "alg_bytes_per_cell_step": 84,
-            "kernel": "the SR step (6 kernels and a memset)",
-            "note": "latency-bound: five dependent launches of 0.1-0.26 M "
+            "kernel": "the SR step (4 kernels and a memset)",
+            "note": "latency-bound: four dependent launches of 0.1-0.26 M "
                     "cells per step; see profiles/sr_step_fk3v_512.md"}
 
 

@@ -339,13 +339,19 @@ int yh_comoving_field(const yh_param_var *p, yh_sym_state *sym,
                       int advance_phi, void *stream);
 
 /* BFECC advection out <- in by the comoving field (FP32 row/column vectors
- * of yh_comoving_field), as three race-free passes through the caller's
- * scratch fields uf and ue.
+ * of yh_comoving_field): the three race-free passes in one launch (tiles in
+ * shared memory), or, when out aliases in, as three launches through the
+ * caller's scratch fields uf and ue. Both give the same bits.
  * Replaces advFDBFECC_wrapper (hostPrototypes.h:36-38, advFDBFECC.cu:18-362). */
 int yh_advect_bfecc(const yh_param_var *p, int model, yh_fields out,
                     yh_fields in, const float *adv_x_rows_f32,
                     const float *adv_y_cols_f32, const uint8_t *solid,
                     yh_fields uf, yh_fields ue, void *stream);
+/* The three launches always (uf and ue hold the passes' results). */
+int yh_advect_bfecc_3pass(const yh_param_var *p, int model, yh_fields out,
+                          yh_fields in, const float *adv_x_rows_f32,
+                          const float *adv_y_cols_f32, const uint8_t *solid,
+                          yh_fields uf, yh_fields ue, void *stream);
 
 /* phi += dt * c and step += 1 on the device (main.cu:935-952). */
 int yh_sym_advance(const yh_param_var *p, yh_sym_state *sym, void *stream);

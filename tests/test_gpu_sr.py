@@ -153,6 +153,51 @@ def test_bfecc_matches_oracle(model):
         assert max_abs(host(out[f]), want[f]) < 2e-6
 
 
+@pytest.mark.parametrize("model", [A.YH_MODEL_REF2V, A.YH_MODEL_FK3V])
+@pytest.mark.parametrize("holes", [False, True])
+@pytest.mark.parametrize("shape", [(64, 52), (97, 61), (33, 17)])
+def test_bfecc_one_launch_equals_three_launches(model, holes, shape):
+    # the fused kernel (tiles with rings in shared memory) against the three
+    # pass launches: the same bits, on grids that are no multiple of the tile
+    import torch
+    nx, ny = shape
+    p = A.param_defaults(nx, ny)
+    p.dt = 0.01
+    A.param_derive(p)
+    nf = A.NFIELDS[model]
+    solid = None
+    if holes:
+        rng = np.random.default_rng(nx)
+        jj, ii = np.mgrid[0:ny, 0:nx]
+        m = np.ones((ny, nx), np.uint8)
+        for _ in range(6):
+            cx, cy, r = rng.uniform(0, nx), rng.uniform(0, ny), rng.uniform(1.5, 4)
+            m[(ii - cx) ** 2 + (jj - cy) ** 2 <= r * r] = 0
+        solid = dev(m.ravel(), torch.uint8)
+        p.solidSwitch = True
+    st = [x.astype(np.float32) for x in smooth_state(nx, ny, 7, nf)]
+    for c, phi in (((1.3, -0.7, 0.02), (0.0, 0.0, 0.4)),
+                   ((-2.1, 0.9, -0.05), (0.0, 0.0, 2.5))):
+        sym = sym_tensor(c, phi)
+        ar = torch.zeros(ny, dtype=torch.float64, device="cuda")
+        ac = torch.zeros(nx, dtype=torch.float64, device="cuda")
+        arf = torch.zeros(ny, device="cuda")
+        acf = torch.zeros(nx, device="cuda")
+        ops.comoving_field(p, sym, ar, ac, arf, acf)
+        inp = [dev(x) for x in st]
+        outs = []
+        for three in (False, True):
+            out = [torch.full_like(inp[0], 7.0) for _ in range(nf)]
+            uf = [torch.zeros_like(inp[0]) for _ in range(nf)]
+            ue = [torch.zeros_like(inp[0]) for _ in range(nf)]
+            ops.advect_bfecc(p, model, out, inp, arf, acf, uf, ue, solid=solid,
+                             three_launches=three)
+            outs.append(out)
+        torch.cuda.synchronize()
+        for f in range(nf):
+            assert torch.equal(outs[0][f], outs[1][f]), (f, c)
+
+
 def ref2v_spiral(n, L=3.0, steps=6000):
     """A REF2V spiral grown from the reference's cross-field initial
     condition (main.cu:604-618) on an n x n grid of side L cm, with the FP32

@@ -41,6 +41,8 @@ SIGNATURES = {
     "yh_comoving_field": (_i, [_P(A.ParamVar), _v, _v, _v, _v, _v, _i, _v]),
     "yh_advect_bfecc": (_i, [_P(A.ParamVar), _i, A.Fields, A.Fields, _v, _v,
                              _v, A.Fields, A.Fields, _v]),
+    "yh_advect_bfecc_3pass": (_i, [_P(A.ParamVar), _i, A.Fields, A.Fields, _v, _v,
+                                   _v, A.Fields, A.Fields, _v]),
     "yh_sym_advance": (_i, [_P(A.ParamVar), _v, _v]),
     "yh_stimulate_box": (_i, [_P(A.ParamVar), _v, _v, _i, _i, _i, _i, _f, _v]),
     # solver handle

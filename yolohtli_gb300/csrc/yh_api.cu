@@ -350,6 +350,31 @@ extern "C" int yh_advect_bfecc(const yh_param_var *p, int model,
       !fields_ok(uf, model) || !fields_ok(ue, model))
     return YH_EINVAL;
   if (p->solidSwitch && !solid) return YH_EINVAL;
+  const Fld<float> fi = to_fld(in), fo = to_fld(out);
+  bool alias = false;
+  for (int f = 0; f < nfields(model); ++f)
+    for (int g = 0; g < nfields(model); ++g) alias |= fi.f[f] == fo.f[g];
+  if (alias || p->nx < 2 || p->ny < 2)  // in place: the three launches
+    return cuda_status(launch_bfecc<float>(
+        *p, nfields(model), fi, fo, adv_x_rows_f32, adv_y_cols_f32,
+        p->solidSwitch ? solid : nullptr, to_fld(uf), to_fld(ue),
+        (cudaStream_t)stream));
+  return cuda_status(launch_bfecc_fused(
+      *p, nfields(model), fi, fo, adv_x_rows_f32, adv_y_cols_f32,
+      p->solidSwitch ? solid : nullptr, (cudaStream_t)stream));
+}
+
+extern "C" int yh_advect_bfecc_3pass(const yh_param_var *p, int model,
+                                     yh_fields out, yh_fields in,
+                                     const float *adv_x_rows_f32,
+                                     const float *adv_y_cols_f32,
+                                     const uint8_t *solid, yh_fields uf,
+                                     yh_fields ue, void *stream) {
+  if (!p || !adv_x_rows_f32 || !adv_y_cols_f32) return YH_EINVAL;
+  if (!fields_ok(out, model) || !fields_ok(in, model) ||
+      !fields_ok(uf, model) || !fields_ok(ue, model))
+    return YH_EINVAL;
+  if (p->solidSwitch && !solid) return YH_EINVAL;
   return cuda_status(launch_bfecc<float>(
       *p, nfields(model), to_fld(in), to_fld(out), adv_x_rows_f32,
       adv_y_cols_f32, p->solidSwitch ? solid : nullptr, to_fld(uf),

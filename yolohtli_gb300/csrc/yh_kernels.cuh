@@ -157,6 +157,12 @@ cudaError_t launch_bfecc(const yh_param_var &p, int nf, const Fld<Real> &in,
                          const Real *adv_cols, const uint8_t *solid,
                          const Fld<Real> &uf, const Fld<Real> &ue,
                          cudaStream_t s);
+// The three passes in one launch (FP32, separable comoving field): the
+// same values, bit for bit; no uf/ue scratch in global memory.
+cudaError_t launch_bfecc_fused(const yh_param_var &p, int nf,
+                               const Fld<float> &in, const Fld<float> &out,
+                               const float *adv_rows, const float *adv_cols,
+                               const uint8_t *solid, cudaStream_t s);
 // The same passes reading a full nx*ny comoving field (adv_x, adv_y), as
 // the reference's advFDBFECC_kernel receives it.
 template <typename Real>

@@ -36,6 +36,10 @@ namespace yh {
 #ifndef YH_RES_CELLS
 #define YH_RES_CELLS 4
 #endif
+// Receivers back off 64 ns << min(spin, YH_RES_BACKOFF) between polls.
+#ifndef YH_RES_BACKOFF
+#define YH_RES_BACKOFF 4
+#endif
 constexpr int kResThreads = YH_RES_THREADS;  // most compute threads
 constexpr int kResCommMax = 128;  // communication threads (64 or 128)
 constexpr int kResBatch = 16;                // halo words per comm thread and pass
@@ -304,9 +308,9 @@ __device__ __forceinline__ bool res_receive(const ResArgs &A, int s, int e0,
         atomicExch(A.error, 1);
         return false;
       }
-      // back off (64 ns doubling to 1 us) so that polling takes few issue
-      // slots from the compute warps
-      __nanosleep(64u << (spin < 4 ? spin : 4));
+      // back off (64 ns doubling to 64 << YH_RES_BACKOFF ns) so that
+      // polling takes few issue slots from the compute warps
+      __nanosleep(64u << (spin < YH_RES_BACKOFF ? spin : YH_RES_BACKOFF));
 #pragma unroll
       for (int k = 0; k < kResBatch; ++k)
         if ((unsigned)(x[k] >> 32) != want) {

@@ -648,11 +648,11 @@ static cudaError_t enqueue_sr_step(yh_solver *h, bool first) {
     e = launch_phase_comoving(h->p, h->nf, h->cur, h->tan, tx, ty, tt,
                               advf_rows, advf_cols, h->solid, h->sym, h->ws,
                               r == reps - 1, h->s);
-  if (e == cudaSuccess)  // BFECC: nxt -> cur
-    e = launch_bfecc<float>(h->p, h->nf, h->nxt, h->cur, advf_rows, advf_cols,
-                            h->solid, h->uf, h->ue, h->s);
-  // RD, tips, phase x reps, 3 BFECC passes
-  if (e == cudaSuccess) h->launches += 2 + reps + 3;
+  if (e == cudaSuccess)  // BFECC, three passes in one launch: nxt -> cur
+    e = launch_bfecc_fused(h->p, h->nf, h->nxt, h->cur, advf_rows, advf_cols,
+                           h->solid, h->s);
+  // RD, tips, phase x reps, BFECC
+  if (e == cudaSuccess) h->launches += 2 + reps + 1;
   return e;
 }
 

@@ -1080,6 +1080,121 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The three passes in one launch. A block owns a 32x16 tile of the output:
+// pass 1 on the tile and a 2-cell ring (uf), pass 2 on the tile and a
+// 1-cell ring (ue), pass 3 on the tile, all in shared memory; every pass
+// reads one neighbour per axis, so the input tile with a 3-cell ring
+// covers them. Each cell's arithmetic is bfecc_pass's, in the same order,
+// so the result equals the three launches bit for bit; the ring cells are
+// computed by two or three blocks (1.4x the pass-1 work of a lone pass).
+constexpr int kFuseTX = 32, kFuseTY = 16;
+
+// Offset in a region of row pitch P of the global neighbour index n of C.
+__device__ __forceinline__ int bfecc_local(int n, int C, int nx, int P) {
+  const int d = n - C;
+  return d == 0 ? 0 : (d == -1 ? -1 : (d == 1 ? 1 : (d < 0 ? -P : P)));
+}
+
+template <int NF, bool HOLES>
+__global__ void __launch_bounds__(256)
+    bfecc_fused(const BfeccArgs<float> a, const Fld<float> in,
+                const Fld<float> out, const float *__restrict__ adv_rows,
+                const float *__restrict__ adv_cols,
+                const uint8_t *__restrict__ solid) {
+  grid_dep_wait();
+  constexpr int GX = kFuseTX + 6, GY = kFuseTY + 6;  // input, ring 3
+  constexpr int FX = kFuseTX + 4, FY = kFuseTY + 4;  // uf, ring 2
+  constexpr int EX = kFuseTX + 2, EY = kFuseTY + 2;  // ue, ring 1
+  __shared__ float s_g[NF][GY * GX];
+  __shared__ float s_f[NF][FY * FX];
+  __shared__ float s_e[NF][EY * EX];
+  const int nx = a.nx, ny = a.ny;
+  const int bi = blockIdx.x * kFuseTX, bj = blockIdx.y * kFuseTY;
+  const int t = threadIdx.x + 32 * threadIdx.y;
+  // input tile with a 3-cell ring (cells outside the grid are not read)
+  for (int k = t; k < GX * GY; k += 256) {
+    const int i = bi - 3 + k % GX, j = bj - 3 + k / GX;
+    if (i >= 0 && i < nx && j >= 0 && j < ny)
+#pragma unroll
+      for (int f = 0; f < NF; ++f) s_g[f][k] = in.f[f][i + nx * j];
+  }
+  __syncthreads();
+  // pass 1 on the tile and a 2-cell ring
+  for (int k = t; k < FX * FY; k += 256) {
+    const int li = k % FX, lj = k / FX;
+    const int i = bi - 2 + li, j = bj - 2 + lj;
+    if (i < 0 || i >= nx || j < 0 || j >= ny) continue;
+    const int C = i + nx * j;
+    bool sc;
+    const BIdx n = bfecc_idx<HOLES>(i, j, nx, ny, solid, sc);
+    float cx, cy, Rx, Ry;
+    bfecc_ratios(a, sc ? adv_rows[j] : 0.f, sc ? adv_cols[i] : 0.f, cx, cy,
+                 Rx, Ry);
+    const int g0 = (lj + 1) * GX + (li + 1);
+    const int oW = bfecc_local(n.W, C, nx, GX), oE = bfecc_local(n.E, C, nx, GX);
+    const int oS = bfecc_local(n.S, C, nx, GX), oN = bfecc_local(n.N, C, nx, GX);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      const float *g = s_g[f] + g0;
+      const float FDx = cx > 0.f ? g[0] - g[oW] : g[0] - g[oE];
+      const float FDy = cy > 0.f ? g[0] - g[oS] : g[0] - g[oN];
+      s_f[f][k] = g[0] - a.tc * (Rx * FDx + Ry * FDy);
+    }
+  }
+  __syncthreads();
+  // pass 2 on the tile and a 1-cell ring
+  for (int k = t; k < EX * EY; k += 256) {
+    const int li = k % EX, lj = k / EX;
+    const int i = bi - 1 + li, j = bj - 1 + lj;
+    if (i < 0 || i >= nx || j < 0 || j >= ny) continue;
+    const int C = i + nx * j;
+    bool sc;
+    const BIdx n = bfecc_idx<HOLES>(i, j, nx, ny, solid, sc);
+    float cx, cy, Rx, Ry;
+    bfecc_ratios(a, sc ? adv_rows[j] : 0.f, sc ? adv_cols[i] : 0.f, cx, cy,
+                 Rx, Ry);
+    const int f0 = (lj + 1) * FX + (li + 1);
+    const int g0 = (lj + 2) * GX + (li + 2);
+    const int ocE = bfecc_local(n.cE, C, nx, FX), oE2 = bfecc_local(n.E2, C, nx, FX);
+    const int ocW = bfecc_local(n.cW, C, nx, FX), oW2 = bfecc_local(n.W2, C, nx, FX);
+    const int ocN = bfecc_local(n.cN, C, nx, FX), oN2 = bfecc_local(n.N2, C, nx, FX);
+    const int ocS = bfecc_local(n.cS, C, nx, FX), oS2 = bfecc_local(n.S2, C, nx, FX);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      const float *q = s_f[f] + f0;
+      const float FDx = cx > 0.f ? q[ocE] - q[oE2] : q[ocW] - q[oW2];
+      const float FDy = cy > 0.f ? q[ocN] - q[oN2] : q[ocS] - q[oS2];
+      const float ub = q[0] - a.tc * (Rx * FDx + Ry * FDy);
+      const float g = s_g[f][g0];
+      s_e[f][k] = g - 0.5f * (ub - g);
+    }
+  }
+  __syncthreads();
+  // pass 3 on the tile
+  for (int k = t; k < kFuseTX * kFuseTY; k += 256) {
+    const int li = k % kFuseTX, lj = k / kFuseTX;
+    const int i = bi + li, j = bj + lj;
+    if (i >= nx || j >= ny) continue;
+    const int C = i + nx * j;
+    bool sc;
+    const BIdx n = bfecc_idx<HOLES>(i, j, nx, ny, solid, sc);
+    float cx, cy, Rx, Ry;
+    bfecc_ratios(a, sc ? adv_rows[j] : 0.f, sc ? adv_cols[i] : 0.f, cx, cy,
+                 Rx, Ry);
+    const int e0 = (lj + 1) * EX + (li + 1);
+    const int oW = bfecc_local(n.W, C, nx, EX), oE = bfecc_local(n.E, C, nx, EX);
+    const int oS = bfecc_local(n.S, C, nx, EX), oN = bfecc_local(n.N, C, nx, EX);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      const float *q = s_e[f] + e0;
+      const float FDx = cx > 0.f ? q[0] - q[oW] : q[0] - q[oE];
+      const float FDy = cy > 0.f ? q[0] - q[oS] : q[0] - q[oN];
+      const float r = q[0] - a.tc * (Rx * FDx + Ry * FDy);
+      out.f[f][C] = sc ? r : 0.f;
+    }
+  }
+}
+
 template <int NF, typename Real, bool HOLES, bool ADV2D>
 static cudaError_t bfecc_nf(const BfeccArgs<Real> &a, const Fld<Real> &in,
                             const Fld<Real> &out, const Real *ar,
@@ -1132,6 +1247,37 @@ cudaError_t launch_bfecc(const yh_param_var &p, int nf, const Fld<Real> &in,
                          cudaStream_t s) {
   return bfecc_dispatch<Real, false>(p, nf, in, out, adv_rows, adv_cols,
                                      solid, uf, ue, s);
+}
+
+cudaError_t launch_bfecc_fused(const yh_param_var &p, int nf,
+                               const Fld<float> &in, const Fld<float> &out,
+                               const float *adv_rows, const float *adv_cols,
+                               const uint8_t *solid, cudaStream_t s) {
+  BfeccArgs<float> a;
+  a.nx = p.nx;
+  a.ny = p.ny;
+  a.dt = (float)p.dt;
+  a.hx = (float)p.hx;
+  a.hy = (float)p.hy;
+  a.tc = (float)p.tc;
+  const bool holes = p.solidSwitch && solid;
+  if (p.nx < 2 || p.ny < 2) return cudaErrorInvalidValue;
+  // out must not alias in: a block's ring cells are other blocks' output
+  for (int f = 0; f < nf; ++f)
+    for (int g = 0; g < nf; ++g)
+      if (in.f[f] == out.f[g]) return cudaErrorInvalidValue;
+  const dim3 block(32, 8);
+  const dim3 grid((p.nx + kFuseTX - 1) / kFuseTX, (p.ny + kFuseTY - 1) / kFuseTY);
+#define YH_BF(NF, H)                                                          \
+  if (nf == NF && holes == H)                                                 \
+    return launch_pdl(bfecc_fused<NF, H>, grid, block, 0, s, a, in, out,      \
+                      adv_rows, adv_cols, solid);
+  YH_BF(2, false)
+  YH_BF(2, true)
+  YH_BF(3, false)
+  YH_BF(3, true)
+#undef YH_BF
+  return cudaErrorInvalidValue;
 }
 
 template <typename Real>

@@ -127,9 +127,10 @@ def comoving_field(p, sym, adv_rows, adv_cols, adv_rows_f=None,
 
 
 def advect_bfecc(p, model, out, inp, adv_rows_f, adv_cols_f, uf, ue,
-                 solid=None):
+                 solid=None, three_launches=False):
     lib = load()
-    return check("yh_advect_bfecc", lib.yh_advect_bfecc(
+    name = "yh_advect_bfecc_3pass" if three_launches else "yh_advect_bfecc"
+    return check(name, getattr(lib, name)(
         C.byref(p), model, fields(out), fields(inp), _p(adv_rows_f),
         _p(adv_cols_f), _p(solid), fields(uf), fields(ue), _stream()))
 
