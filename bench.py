@@ -296,6 +296,9 @@ def run_batch(args):
                                              for x in dev0[k]])
         b.synchronize()
 
+    # the library's schedule autotuner on the workload's initial state
+    restore()
+    tuned = b.autotune(256)
     for _ in range(args.warmup):
         restore()
         b.run(bw.nsteps, events())
@@ -373,9 +376,11 @@ def run_batch(args):
             "config": {"workload": bw.name, "instances": len(insts),
                        "cells": bw.cells, "steps_per_solve": bw.nsteps,
                        "sizes": "n ~ U{128,160,...,768}, square",
-                       "schedule": "groups of ~1M cells on 2 streams",
+                       "schedule": "autotuned: groups of ~%d cells on %d streams"
+                                   % tuned,
                        "l2": "1.48 GB of state per step, above the L2; "
-                             "each group's 25 MB stays in it",
+                             "each group's %.0f MB (two levels) stays in it"
+                             % (tuned[0] * 24 / 1e6),
                        "parallelism": "replicas x%d" % world},
             "roofline": {"bound": "hbm", "achieved": round(25.0 * value, 1),
                          "peak": peak, "unit": "GB/s",

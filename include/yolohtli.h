@@ -503,6 +503,13 @@ int yh_batch_run(yh_batch *b, int nsteps, const yh_batch_stim *stims,
  * instances first) on `streams` internal streams (1-64). The default is
  * 1,048,576 cells on 2 streams. */
 int yh_batch_set_schedule(yh_batch *b, long long group_cells, int streams);
+/* The schedule autotuner: times probe_steps steps (rounded up to even, no
+ * events) of every schedule of groups of 256 K, 512 K, 1 M or 2 M cells
+ * on 2, 3 or 4 streams on the current state, keeps the fastest and
+ * restores the state and the step count. The choice is returned in
+ * *group_cells and *streams (either may be NULL). */
+int yh_batch_autotune(yh_batch *b, int probe_steps, long long *group_cells,
+                      int *streams);
 int yh_batch_get_step(yh_batch *b, int *step);
 int yh_batch_get_launch_count(yh_batch *b, long long *n);
 

@@ -83,6 +83,56 @@ def test_batch_equals_the_single_grid_solver_bitwise():
     b.close()
 
 
+@pytest.mark.parametrize("schedule", [(1 << 12, 3), (1, 4), (1 << 30, 1)])
+def test_every_schedule_gives_the_same_bits(schedule):
+    # groups of one instance up to one group for all, on 1-4 streams
+    insts = _instances()
+    runs = [130, 170]
+    b = Batch([w.p for w in insts], [w.fk for w in insts],
+              [w.solid for w in insts])
+    b.set_schedule(*schedule)
+    for k, w in enumerate(insts):
+        b.set_state(k, *w.state0())
+    ev = [(k, st) for k, w in enumerate(insts) for st in w.stims]
+    for n in runs:
+        b.run(n, ev)
+    b.synchronize()
+    for k, wl in enumerate(insts):
+        got = b.get_state(k)
+        ref = _single(wl, runs)
+        for f in range(3):
+            assert np.array_equal(got[f], ref[f]), (schedule, k, f)
+    b.close()
+
+
+def test_autotune_restores_the_state_and_keeps_the_bits():
+    insts = _instances(seed=5)
+    b = Batch([w.p for w in insts], [w.fk for w in insts],
+              [w.solid for w in insts])
+    for k, w in enumerate(insts):
+        b.set_state(k, *w.state0())
+    ev = [(k, st) for k, w in enumerate(insts) for st in w.stims]
+    b.run(100, ev)
+    b.synchronize()
+    before = [b.get_state(k) for k in range(len(insts))]
+    launches = b.launch_count()
+    g, q = b.autotune(64)
+    assert g in (1 << 18, 1 << 19, 1 << 20, 1 << 21) and q in (2, 3, 4)
+    assert b.step_count() == 100 and b.launch_count() == launches
+    for k in range(len(insts)):
+        now = b.get_state(k)
+        for f in range(3):
+            assert np.array_equal(now[f], before[k][f]), (k, f)
+    b.run(70, ev)
+    b.synchronize()
+    for k, wl in enumerate(insts):
+        got = b.get_state(k)
+        ref = _single(wl, [100, 70])
+        for f in range(3):
+            assert np.array_equal(got[f], ref[f]), (k, f)
+    b.close()
+
+
 def test_batch_against_the_fp64_oracle():
     insts = _instances(seed=11)[:3]
     nsteps = 200

@@ -90,6 +90,14 @@ class Batch:
         check("yh_batch_set_schedule", self.lib.yh_batch_set_schedule(
             self.h, int(group_cells), int(streams)))
 
+    def autotune(self, probe_steps=256):
+        """Times the schedules on the current state (restored), keeps the
+        fastest; returns (group_cells, streams)."""
+        g, q = C.c_longlong(), C.c_int()
+        check("yh_batch_autotune", self.lib.yh_batch_autotune(
+            self.h, int(probe_steps), C.byref(g), C.byref(q)))
+        return g.value, q.value
+
     def synchronize(self):
         check("yh_batch_synchronize", self.lib.yh_batch_synchronize(self.h))
 

@@ -551,6 +551,65 @@ extern "C" int yh_batch_run(yh_batch *b, int nsteps, const yh_batch_stim *stims,
   return YH_OK;
 }
 
+extern "C" int yh_batch_autotune(yh_batch *b, int probe_steps,
+                                 long long *group_cells, int *streams) {
+  if (!b || probe_steps < 2) return YH_EINVAL;
+  probe_steps += probe_steps & 1;  // even: the state ends on its level
+  const size_t bytes = (size_t)3 * b->total * sizeof(float);
+  float *snap = nullptr;
+  cudaError_t e = cudaMalloc(&snap, bytes);
+  if (e != cudaSuccess) return st(e);
+  const int cur0 = b->cur, step0 = b->step;
+  const long long launches0 = b->launches;
+  float *state = level(b, cur0).f[0];  // the three fields of a level are contiguous
+  e = cudaMemcpyAsync(snap, state, bytes, cudaMemcpyDeviceToDevice, b->s);
+  auto restore = [&]() {
+    b->cur = cur0;
+    b->step = step0;
+    return cudaMemcpyAsync(level(b, cur0).f[0], snap, bytes,
+                           cudaMemcpyDeviceToDevice, b->s);
+  };
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&t0);
+  if (e == cudaSuccess) e = cudaEventCreate(&t1);
+  const long long sizes[] = {1 << 18, 1 << 19, 1 << 20, 1 << 21};
+  const int counts[] = {2, 3, 4};
+  long long best_g = kBatchGroupCells;
+  int best_s = kBatchStreams, rc = st(e);
+  float best_ms = 3.4e38f;
+  for (long long g : sizes)
+    for (int q : counts) {
+      if (rc) break;
+      rc = plan_schedule(b, g, q);
+      // the first run captures the groups' graphs; the second is timed
+      if (!rc) rc = yh_batch_run(b, probe_steps, nullptr, 0);
+      if (!rc) rc = st(restore());
+      if (!rc) rc = st(cudaEventRecord(t0, b->s));
+      if (!rc) rc = yh_batch_run(b, probe_steps, nullptr, 0);
+      if (!rc) rc = st(cudaEventRecord(t1, b->s));
+      if (!rc) rc = st(cudaEventSynchronize(t1));
+      float ms = 0.f;
+      if (!rc) rc = st(cudaEventElapsedTime(&ms, t0, t1));
+      if (!rc) rc = st(restore());
+      if (!rc && ms < best_ms) {
+        best_ms = ms;
+        best_g = g;
+        best_s = q;
+      }
+    }
+  if (!rc) rc = plan_schedule(b, best_g, best_s);
+  if (!rc) rc = st(restore());
+  if (!rc) rc = st(cudaStreamSynchronize(b->s));
+  b->launches = launches0;
+  if (t0) cudaEventDestroy(t0);
+  if (t1) cudaEventDestroy(t1);
+  cudaFree(snap);
+  if (rc) return rc;
+  if (group_cells) *group_cells = best_g;
+  if (streams) *streams = best_s;
+  return YH_OK;
+}
+
 extern "C" int yh_batch_set_schedule(yh_batch *b, long long group_cells,
                                      int streams) {
   if (!b || group_cells <= 0 || streams <= 0 || streams > 64) return YH_EINVAL;
