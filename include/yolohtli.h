@@ -44,7 +44,7 @@ enum {
   YH_EINVAL = -1,        /* bad argument (null pointer, size, flag)          */
   YH_ECUDA = -2,         /* a CUDA runtime call failed                       */
   YH_ENOMEM = -3,        /* device or host allocation failed                 */
-  YH_ESINGULAR = -4,     /* 3x3 drift/rotation system singular (|pivot|<tol) */
+  YH_ESINGULAR = -4,     /* 3x3 drift/rotation system singular (see the solves) */
   YH_ENONFINITE = -5,    /* NaN or Inf in the state                          */
   YH_EOVERFLOW = -6,     /* tip buffer full; extra tips were dropped         */
   YH_EUNSUPPORTED = -7,  /* option off this path: RK2/RK4, lap4, anisotropy,
@@ -280,10 +280,12 @@ size_t yh_phase_integrals_workspace(int nx, int ny);
  *  - template derivatives (negated 4th-order central of `state` when
  *    templ_x.u == NULL, else the stored template fields templ_x/y/t),
  *  - the 12 integrals over the open disc of radius^2 tipOffsetX*tipOffsetY
- *    around sym->centre, accumulated in FP64, deterministic two-level sum,
- *  - the FP64 3x3 solve with partial pivoting, rotated by sym->phi[2]:
- *    sym->c, sym->integrals, sym->status; then sym->c_adv = c,
- *    sym->phi_adv = phi.
+ *    around sym->centre, summed per thread, warp and block as float-float
+ *    pairs (~48 significant bits, no FP64 instruction per cell), the block
+ *    sums added in a fixed order, FP64 from the 12 integrals on,
+ *  - the FP64 3x3 solve by cofactors, rotated by sym->phi[2] (YH_ESINGULAR
+ *    when |det| <= 1e-13 amax^3, c then kept): sym->c, sym->integrals,
+ *    sym->status; then sym->c_adv = c, sym->phi_adv = phi.
  * Replaces slice_wrapper + trapz_wrapper + solve_matrix
  * (hostPrototypes.h:30-33,39-42; symmetryReduction.cu:72-222,329-420;
  * integralTrapz.cu:17-184). `workspace`: device memory of at least

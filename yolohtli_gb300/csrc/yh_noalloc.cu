@@ -14,7 +14,7 @@
 
 namespace {
 
-constexpr int kNoAllocMaxBlocks = 4096;  // 12 FP64 partials per block
+constexpr int kNoAllocMaxBlocks = 4096;  // 12 8-byte partial sums per block
 constexpr size_t kNoAllocBytes = 256 + (size_t)kNoAllocMaxBlocks * 12 * sizeof(double);
 constexpr int kMaxDevices = 64;
 
