@@ -236,50 +236,51 @@ __device__ __forceinline__ void tip_cell_newton(
 // current centre, ties broken by (y, x); writes the new centre unless no tip
 // was found or this is step 0 (slice_kernel uses tipx0/tipy0 at count == 0,
 // symmetryReduction.cu:98-101).
+// (d, y, x) lexicographically smaller: a total order, so the nearest tip
+// does not depend on the order the tips were found or compared in.
+__device__ __forceinline__ bool tip_before(double d, float y, float x,
+                                           double db, float yb, float xb) {
+  return d < db || (d == db && (y < yb || (y == yb && x < xb)));
+}
+
+// Warp 0 of the calling block: the nearest tip to the current centre,
+// lanes over the tips then a shuffle arg-min (no block-wide barrier); the
+// other threads return at once.
 __device__ void pick_centre_block(int t, const int *count, const yh_tip *vec,
                                   int cap, yh_sym_state *sym) {
-  __shared__ double s_d[256];
-  __shared__ float s_x[256], s_y[256];
+  if (t >= 32) return;
   const int n0 = *(volatile const int *)count;
   const int n = n0 < cap ? n0 : cap;
   const float cx = sym->centre[0], cy = sym->centre[1];
   double bd = 1e300;
   float bx = 0.f, by = 0.f;
-  for (int k = t; k < n; k += 256) {
+  for (int k = t; k < n; k += 32) {
     const float tx = ((volatile const float *)&vec[k].x)[0];
     const float ty = ((volatile const float *)&vec[k].y)[0];
     const double dx = (double)tx - cx, dy = (double)ty - cy;
     const double d = dx * dx + dy * dy;
-    if (d < bd || (d == bd && (ty < by || (ty == by && tx < bx)))) {
+    if (tip_before(d, ty, tx, bd, by, bx)) {
       bd = d;
       bx = tx;
       by = ty;
     }
   }
-  s_d[t] = bd;
-  s_x[t] = bx;
-  s_y[t] = by;
-  __syncthreads();
-  for (int off = 128; off > 0; off >>= 1) {
-    if (t < off) {
-      const int o = t + off;
-      const double d = s_d[o];
-      const float x = s_x[o], y = s_y[o];
-      const double db = s_d[t];
-      const float xb = s_x[t], yb = s_y[t];
-      if (d < db || (d == db && (y < yb || (y == yb && x < xb)))) {
-        s_d[t] = d;
-        s_x[t] = x;
-        s_y[t] = y;
-      }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const double d = __shfl_down_sync(0xffffffffu, bd, off);
+    const float x = __shfl_down_sync(0xffffffffu, bx, off);
+    const float y = __shfl_down_sync(0xffffffffu, by, off);
+    if (tip_before(d, y, x, bd, by, bx)) {
+      bd = d;
+      bx = x;
+      by = y;
     }
-    __syncthreads();
   }
   if (t == 0) {
     sym->ntips = n0;
     if (n > 0 && sym->step > 0) {
-      sym->centre[0] = s_x[0];
-      sym->centre[1] = s_y[0];
+      sym->centre[0] = bx;
+      sym->centre[1] = by;
     }
   }
 }
@@ -670,6 +671,17 @@ __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
   // (symmetryReduction.cu:98-104): float arithmetic, round-half-even.
   const int cx = __float2int_rn(sym->centre[0] - (float)(nx / 2));
   const int cy = __float2int_rn(sym->centre[1] - (float)(ny / 2));
+  // cos and sin of phi_adv = phi for the solve and the comoving field:
+  // block 0 takes them off the last block's serial tail (the counter's
+  // 256-byte slot holds them; the completion fence publishes them)
+  double *rot = reinterpret_cast<double *>(done) + 1;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 &&
+      threadIdx.y == 0) {
+    double sn, cs;
+    sincos(sym->phi[2], &sn, &cs);
+    rot[0] = cs;
+    rot[1] = sn;
+  }
   const int i = nx / 2 + cx - a.R + (int)(blockIdx.x * kPhaseBX + threadIdx.x);
   const int j0 = ny / 2 + cy - a.R +
                  (int)(blockIdx.y * kPhaseBY * kPhaseRows + threadIdx.y);
@@ -686,26 +698,27 @@ __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
       for (int k = 0; k < 12; ++k) acc[k].add(s[k]);
     }
   }
-  // warp tree
-#pragma unroll
-  for (int k = 0; k < 12; ++k)
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc[k].add(acc[k].down(off, 32));
-  __shared__ Acc s_w[kPhaseBY][12];
+  // block sum, transposed through shared memory: warp q (0-7) sums
+  // integrals q and q + 8, 8 threads' values a lane, then a shuffle tree
+  // (one tree per integral instead of twelve in every warp)
+  constexpr int NT = kPhaseBX * kPhaseBY;
+  __shared__ Acc s_a[12][NT];
   __shared__ bool s_last;
   const int lane = threadIdx.x;  // blockDim.x == 32
   const int warp = threadIdx.y;
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < 12; ++k) s_w[warp][k] = acc[k];
-  __syncthreads();
   const int t = threadIdx.x + kPhaseBX * threadIdx.y;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) s_a[k][t] = acc[k];
+  __syncthreads();
   const unsigned nb = gridDim.x * gridDim.y;
   const unsigned bid = blockIdx.x + gridDim.x * blockIdx.y;
-  if (t < 12) {
-    Acc v = s_w[0][t];
-    for (int w = 1; w < kPhaseBY; ++w) v.add(s_w[w][t]);
-    v.store(&partials[(size_t)bid * 12 + t]);
+  for (int q = warp; q < 12; q += kPhaseBY) {
+    Acc v = s_a[q][lane];
+#pragma unroll
+    for (int m = 1; m < NT / 32; ++m) v.add(s_a[q][lane + 32 * m]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v.add(v.down(off, 32));
+    if (lane == 0) v.store(&partials[(size_t)bid * 12 + q]);
   }
   __syncthreads();
   if (t == 0) {
@@ -723,8 +736,20 @@ __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
     const int k = t >> 4, r = t & 15;
     Acc v;
     v.set(Real(0));
-    for (unsigned b = r; b < nb; b += 16)
-      v.add(Acc::load(&partials[(size_t)b * 12 + k]));
+    // the same order (r, r + 16, ...), four loads in flight at a time
+    for (unsigned b0 = r; b0 < nb; b0 += 64) {
+      Acc x[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const unsigned b = b0 + 16 * u;
+        if (b < nb)
+          x[u] = Acc::load(&partials[(size_t)b * 12 + k]);
+        else
+          x[u].set(Real(0));
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v.add(x[u]);
+    }
 #pragma unroll
     for (int off = 8; off > 0; off >>= 1) v.add(v.down(off, 16));
     if (r == 0) s_I[k] = a.hxhy * v.value();
@@ -737,8 +762,7 @@ __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
       sym->integrals[kk] = I[kk];
     }
     // phi_adv = phi: one angle for the solve and the comoving field
-    double sn, cs;
-    sincos(sym->phi[2], &sn, &cs);
+    const double cs = __ldcg(rot), sn = __ldcg(rot + 1);
     double c[3];
     const int stt = solve3_cofactor(I, cs, sn, c);
     sym->status = stt;
