@@ -732,15 +732,24 @@ __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
   // partials r, r+16, ... in order, then a 16-lane tree.
   __shared__ double s_I[12];
   __shared__ double s_c[3], s_cs, s_sn;
+  __shared__ double s_phi[3], s_cold[3];
+  if (t == 224) {  // warp 7 (no partial sums): the tail's other inputs
+    s_cs = __ldcg(rot);
+    s_sn = __ldcg(rot + 1);
+    for (int kk = 0; kk < 3; ++kk) {
+      s_phi[kk] = sym->phi[kk];
+      s_cold[kk] = sym->c[kk];
+    }
+  }
   if (t < 192) {
     const int k = t >> 4, r = t & 15;
     Acc v;
     v.set(Real(0));
-    // the same order (r, r + 16, ...), four loads in flight at a time
-    for (unsigned b0 = r; b0 < nb; b0 += 64) {
-      Acc x[4];
+    // the same order (r, r + 16, ...), sixteen loads in flight at a time
+    for (unsigned b0 = r; b0 < nb; b0 += 256) {
+      Acc x[16];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < 16; ++u) {
         const unsigned b = b0 + 16 * u;
         if (b < nb)
           x[u] = Acc::load(&partials[(size_t)b * 12 + k]);
@@ -748,7 +757,7 @@ __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
           x[u].set(Real(0));
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) v.add(x[u]);
+      for (int u = 0; u < 16; ++u) v.add(x[u]);
     }
 #pragma unroll
     for (int off = 8; off > 0; off >>= 1) v.add(v.down(off, 16));
@@ -762,19 +771,16 @@ __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
       sym->integrals[kk] = I[kk];
     }
     // phi_adv = phi: one angle for the solve and the comoving field
-    const double cs = __ldcg(rot), sn = __ldcg(rot + 1);
     double c[3];
-    const int stt = solve3_cofactor(I, cs, sn, c);
+    const int stt = solve3_cofactor(I, s_cs, s_sn, c);
     sym->status = stt;
-    if (stt == YH_OK)
-      for (int kk = 0; kk < 3; ++kk) sym->c[kk] = c[kk];
     for (int kk = 0; kk < 3; ++kk) {
-      s_c[kk] = sym->c[kk];
-      sym->c_adv[kk] = sym->c[kk];
-      sym->phi_adv[kk] = sym->phi[kk];
+      const double ck = stt == YH_OK ? c[kk] : s_cold[kk];
+      s_c[kk] = ck;
+      sym->c[kk] = ck;
+      sym->c_adv[kk] = ck;
+      sym->phi_adv[kk] = s_phi[kk];
     }
-    s_cs = cs;
-    s_sn = sn;
     *done = 0u;
   }
   if (tail.rows == nullptr) return;
@@ -790,7 +796,7 @@ __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
   for (int ii = t; ii < nx; ii += kPhaseBX * kPhaseBY)
     tail.cols[ii] = c0 - hxct * (float)ii;
   if (tail.advance && t == 0) {
-    for (int kk = 0; kk < 3; ++kk) sym->phi[kk] = sym->phi[kk] + s_c[kk] * tail.dt;
+    for (int kk = 0; kk < 3; ++kk) sym->phi[kk] = s_phi[kk] + s_c[kk] * tail.dt;
     sym->step += 1;
   }
 }
@@ -1132,9 +1138,27 @@ __global__ void __launch_bounds__(256)
   __shared__ float s_g[NF][GY * GX];
   __shared__ float s_f[NF][FY * FX];
   __shared__ float s_e[NF][EY * EX];
+  // bfecc_ratios splits by axis: cx, Rx depend on the row, cy, Ry on the
+  // column, so each is computed once per tile row / column. Off-tissue
+  // cells read their own value only (every difference is 0), so which
+  // ratios they get does not change their bits.
+  __shared__ float s_cx[GY], s_rx[GY], s_cy[GX], s_ry[GX];
   const int nx = a.nx, ny = a.ny;
   const int bi = blockIdx.x * kFuseTX, bj = blockIdx.y * kFuseTY;
   const int t = threadIdx.x + 32 * threadIdx.y;
+  if (t < GY) {
+    const int j = bj - 3 + t;
+    float cx = 0.f, cy, Rx = 0.f, Ry;
+    if (j >= 0 && j < ny) bfecc_ratios(a, adv_rows[j], 0.f, cx, cy, Rx, Ry);
+    s_cx[t] = cx;
+    s_rx[t] = Rx;
+  } else if (t >= 64 && t < 64 + GX) {
+    const int i = bi - 3 + (t - 64);
+    float cx, cy = 0.f, Rx, Ry = 0.f;
+    if (i >= 0 && i < nx) bfecc_ratios(a, 0.f, adv_cols[i], cx, cy, Rx, Ry);
+    s_cy[t - 64] = cy;
+    s_ry[t - 64] = Ry;
+  }
   // input tile with a 3-cell ring (cells outside the grid are not read)
   for (int k = t; k < GX * GY; k += 256) {
     const int i = bi - 3 + k % GX, j = bj - 3 + k / GX;
@@ -1151,9 +1175,8 @@ __global__ void __launch_bounds__(256)
     const int C = i + nx * j;
     bool sc;
     const BIdx n = bfecc_idx<HOLES>(i, j, nx, ny, solid, sc);
-    float cx, cy, Rx, Ry;
-    bfecc_ratios(a, sc ? adv_rows[j] : 0.f, sc ? adv_cols[i] : 0.f, cx, cy,
-                 Rx, Ry);
+    const float cx = s_cx[lj + 1], Rx = s_rx[lj + 1];
+    const float cy = s_cy[li + 1], Ry = s_ry[li + 1];
     const int g0 = (lj + 1) * GX + (li + 1);
     const int oW = bfecc_local(n.W, C, nx, GX), oE = bfecc_local(n.E, C, nx, GX);
     const int oS = bfecc_local(n.S, C, nx, GX), oN = bfecc_local(n.N, C, nx, GX);
@@ -1174,9 +1197,8 @@ __global__ void __launch_bounds__(256)
     const int C = i + nx * j;
     bool sc;
     const BIdx n = bfecc_idx<HOLES>(i, j, nx, ny, solid, sc);
-    float cx, cy, Rx, Ry;
-    bfecc_ratios(a, sc ? adv_rows[j] : 0.f, sc ? adv_cols[i] : 0.f, cx, cy,
-                 Rx, Ry);
+    const float cx = s_cx[lj + 2], Rx = s_rx[lj + 2];
+    const float cy = s_cy[li + 2], Ry = s_ry[li + 2];
     const int f0 = (lj + 1) * FX + (li + 1);
     const int g0 = (lj + 2) * GX + (li + 2);
     const int ocE = bfecc_local(n.cE, C, nx, FX), oE2 = bfecc_local(n.E2, C, nx, FX);
@@ -1202,9 +1224,8 @@ __global__ void __launch_bounds__(256)
     const int C = i + nx * j;
     bool sc;
     const BIdx n = bfecc_idx<HOLES>(i, j, nx, ny, solid, sc);
-    float cx, cy, Rx, Ry;
-    bfecc_ratios(a, sc ? adv_rows[j] : 0.f, sc ? adv_cols[i] : 0.f, cx, cy,
-                 Rx, Ry);
+    const float cx = s_cx[lj + 3], Rx = s_rx[lj + 3];
+    const float cy = s_cy[li + 3], Ry = s_ry[li + 3];
     const int e0 = (lj + 1) * EX + (li + 1);
     const int oW = bfecc_local(n.W, C, nx, EX), oE = bfecc_local(n.E, C, nx, EX);
     const int oS = bfecc_local(n.S, C, nx, EX), oN = bfecc_local(n.N, C, nx, EX);
