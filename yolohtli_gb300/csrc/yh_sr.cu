@@ -148,35 +148,34 @@ __device__ __forceinline__ void tip_cell(const TipArgs &a, int i, int j,
                    cap, plot);
 }
 
-// tip_cell for FP32 levels: the same FP64 products, sums and square root
-// (where the cancellation is), the four root divisions in FP32 on the
-// rounded numerators and denominators. The roots kept lie in (0, 1), so
-// the change is about 1e-7 of a cell, and the FP64 chain a candidate waits
-// on is ~40 instructions shorter.
+// tip_cell for FP32 levels, in fewer FP64 operations: the expanded sums
+// factor into products of corner differences, which are exact in FP64
+// for FP32 corners,
+//   den1/2 = (x3-x4)(y1-y2) - (x1-x2)(y3-y4)   (also the factor under the root)
+//   den2/2 = (x2-x3)(y1-y4) + (x4-x1)(y2-y3),
+// so the quantities are at least as accurate as the expanded form's; the
+// four root divisions run in FP32 on the rounded numerators and
+// denominators (the roots kept lie in (0, 1): ~1e-7 of a cell). GB300's
+// narrow FP64 pipe makes this chain the tip launch's critical path.
 template <bool GRAD, typename Real>
 __device__ __forceinline__ void tip_cell_f32div(
     const TipArgs &a, int i, int j, double x1, double x2, double x3, double x4,
     double y1, double y2, double y3, double y4, bool need_disc, float ptime,
     const Real *present, int *count, yh_tip *vec, int cap, uint8_t *plot) {
   const double Uth = a.Uth;
-  const double x3y1 = x3 * y1, x4y1 = x4 * y1, x3y2 = x3 * y2, x4y2 = x4 * y2;
-  const double x1y3 = x1 * y3, x2y3 = x2 * y3, x1y4 = x1 * y4, x2y4 = x2 * y4;
-  const double x2y1 = x2 * y1, x1y2 = x1 * y2, x4y3 = x4 * y3, x3y4 = x3 * y4;
-  const double den1 =
-      2.0 * (x3y1 - x4y1 - x3y2 + x4y2 - x1y3 + x2y3 + x1y4 - x2y4);
-  const double den2 =
-      2.0 * (x2y1 - x3y1 - x1y2 + x4y2 + x1y3 - x4y3 - x2y4 + x3y4);
-  const double ctn1 = x1 - x2 + x3 - x4 - y1 + y2 - y3 + y4;
-  const double ctn2 = x3y1 - 2.0 * x4y1 + x4y2 - x1y3 + 2.0 * x1y4 - x2y4;
-  const double disc =
-      sqrt(4.0 * (x3y1 - x3y2 - x4y1 + x4y2 - x1y3 + x1y4 + x2y3 - x2y4) *
-               (x4y1 - x1y4 + Uth * (x1 - x4 - y1 + y4)) +
-           (-ctn2 + Uth * ctn1) * (-ctn2 + Uth * ctn1));
+  const double d12 = x1 - x2, d34 = x3 - x4, e12 = y1 - y2, e34 = y3 - y4;
+  const double A = d34 * e12 - d12 * e34;  // den1 / 2
+  const double den2h = (x2 - x3) * (y1 - y4) + (x4 - x1) * (y2 - y3);
+  const double ctn1 = (d12 + d34) - (e12 + e34);
+  const double ctn2 =
+      y1 * (x3 - 2.0 * x4) + x4 * y2 - x1 * y3 + y4 * (2.0 * x1 - x2);
+  const double B = x4 * y1 - x1 * y4 + Uth * (x1 - x4 - y1 + y4);
   const double px = ctn2 - Uth * ctn1;
-  const double py =
-      Uth * ctn1 - x3y1 + x4y2 + x1y3 - x2y4 + 2.0 * (x2y1 - x1y2);
+  const double disc = sqrt(4.0 * A * B + px * px);
+  const double py = Uth * ctn1 + y1 * (2.0 * x2 - x3) + y2 * (x4 - 2.0 * x1) +
+                    x1 * y3 - x2 * y4;
   if (need_disc && !(disc >= 0.0)) return;
-  const float d1 = (float)den1, d2 = (float)den2;
+  const float d1 = (float)(2.0 * A), d2 = (float)(2.0 * den2h);
   tip_record<GRAD>(a, i, j, __fdiv_rn((float)(px + disc), d1),
                    __fdiv_rn((float)(py + disc), d2), ptime, present, count,
                    vec, cap, plot);
