@@ -1124,6 +1124,29 @@ __device__ __forceinline__ int bfecc_local(int n, int C, int nx, int P) {
   return d == 0 ? 0 : (d == -1 ? -1 : (d == 1 ? 1 : (d < 0 ? -P : P)));
 }
 
+// Offsets, in a region of row pitch P, of bfecc_idx's neighbours of (i, j)
+// in the order W, E, S, N, cW, W2, cE, E2, cS, S2, cN, N2: constants for a
+// cell off the grid's edges without holes (bfecc_idx gives the plain
+// neighbours there), bfecc_idx itself otherwise.
+template <bool HOLES>
+__device__ __forceinline__ void fused_offsets(int i, int j, int nx, int ny,
+                                              const uint8_t *solid, int P,
+                                              int (&o)[12]) {
+  if (!HOLES && i > 0 && i < nx - 1 && j > 0 && j < ny - 1) {
+    o[0] = -1; o[1] = 1; o[2] = -P; o[3] = P;
+    o[4] = 0; o[5] = -1; o[6] = 0; o[7] = 1;
+    o[8] = 0; o[9] = -P; o[10] = 0; o[11] = P;
+    return;
+  }
+  const int C = i + nx * j;
+  bool sc;
+  const BIdx n = bfecc_idx<HOLES>(i, j, nx, ny, solid, sc);
+  const int g[12] = {n.W, n.E, n.S, n.N, n.cW, n.W2, n.cE, n.E2,
+                     n.cS, n.S2, n.cN, n.N2};
+#pragma unroll
+  for (int q = 0; q < 12; ++q) o[q] = bfecc_local(g[q], C, nx, P);
+}
+
 template <int NF, bool HOLES>
 __global__ void __launch_bounds__(256)
     bfecc_fused(const BfeccArgs<float> a, const Fld<float> in,
@@ -1171,14 +1194,12 @@ __global__ void __launch_bounds__(256)
     const int li = k % FX, lj = k / FX;
     const int i = bi - 2 + li, j = bj - 2 + lj;
     if (i < 0 || i >= nx || j < 0 || j >= ny) continue;
-    const int C = i + nx * j;
-    bool sc;
-    const BIdx n = bfecc_idx<HOLES>(i, j, nx, ny, solid, sc);
+    int o[12];
+    fused_offsets<HOLES>(i, j, nx, ny, solid, GX, o);
     const float cx = s_cx[lj + 1], Rx = s_rx[lj + 1];
     const float cy = s_cy[li + 1], Ry = s_ry[li + 1];
     const int g0 = (lj + 1) * GX + (li + 1);
-    const int oW = bfecc_local(n.W, C, nx, GX), oE = bfecc_local(n.E, C, nx, GX);
-    const int oS = bfecc_local(n.S, C, nx, GX), oN = bfecc_local(n.N, C, nx, GX);
+    const int oW = o[0], oE = o[1], oS = o[2], oN = o[3];
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
       const float *g = s_g[f] + g0;
@@ -1193,17 +1214,14 @@ __global__ void __launch_bounds__(256)
     const int li = k % EX, lj = k / EX;
     const int i = bi - 1 + li, j = bj - 1 + lj;
     if (i < 0 || i >= nx || j < 0 || j >= ny) continue;
-    const int C = i + nx * j;
-    bool sc;
-    const BIdx n = bfecc_idx<HOLES>(i, j, nx, ny, solid, sc);
+    int o[12];
+    fused_offsets<HOLES>(i, j, nx, ny, solid, FX, o);
     const float cx = s_cx[lj + 2], Rx = s_rx[lj + 2];
     const float cy = s_cy[li + 2], Ry = s_ry[li + 2];
     const int f0 = (lj + 1) * FX + (li + 1);
     const int g0 = (lj + 2) * GX + (li + 2);
-    const int ocE = bfecc_local(n.cE, C, nx, FX), oE2 = bfecc_local(n.E2, C, nx, FX);
-    const int ocW = bfecc_local(n.cW, C, nx, FX), oW2 = bfecc_local(n.W2, C, nx, FX);
-    const int ocN = bfecc_local(n.cN, C, nx, FX), oN2 = bfecc_local(n.N2, C, nx, FX);
-    const int ocS = bfecc_local(n.cS, C, nx, FX), oS2 = bfecc_local(n.S2, C, nx, FX);
+    const int ocW = o[4], oW2 = o[5], ocE = o[6], oE2 = o[7];
+    const int ocS = o[8], oS2 = o[9], ocN = o[10], oN2 = o[11];
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
       const float *q = s_f[f] + f0;
@@ -1221,13 +1239,13 @@ __global__ void __launch_bounds__(256)
     const int i = bi + li, j = bj + lj;
     if (i >= nx || j >= ny) continue;
     const int C = i + nx * j;
-    bool sc;
-    const BIdx n = bfecc_idx<HOLES>(i, j, nx, ny, solid, sc);
+    const bool sc = !HOLES || solid[C] != 0;
+    int o[12];
+    fused_offsets<HOLES>(i, j, nx, ny, solid, EX, o);
     const float cx = s_cx[lj + 3], Rx = s_rx[lj + 3];
     const float cy = s_cy[li + 3], Ry = s_ry[li + 3];
     const int e0 = (lj + 1) * EX + (li + 1);
-    const int oW = bfecc_local(n.W, C, nx, EX), oE = bfecc_local(n.E, C, nx, EX);
-    const int oS = bfecc_local(n.S, C, nx, EX), oN = bfecc_local(n.N, C, nx, EX);
+    const int oW = o[0], oE = o[1], oS = o[2], oN = o[3];
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
       const float *q = s_e[f] + e0;
