@@ -625,47 +625,86 @@ def run_sr(args):
 
 
 def run_sr_reference(args):
-    """The reference's own kernels in its symmetry-reduced sequence
-    (main.cu:894-954; REF2V FP64, 512^2), headless."""
-    try:
-        import torch
-        from oracle import oracle as O
-        from oracle import refgpu as R
-    except Exception as e:
-        print(json.dumps({"impl": "reference", "unavailable": str(e)}), flush=True)
+    """--impl reference for the symmetry-reduced workload: the reference's
+    SR step sequence (main.cu:894-954) as the CPU restatement runs it (the
+    oracle port, FP64, OpenMP over the host cores) on this arm's case: the
+    fk_sr_512 start (built on the CPU too), the same disc, the frozen
+    template. The reference's own GPU kernels in their sequence (REF2V
+    FP64, the model it has) are reported beside it as reference_gpu."""
+    if env_int("RANK", 0) != 0:
         return
-    if not torch.cuda.is_available() or not R.available():
-        print(json.dumps({"impl": "reference", "unavailable":
-                          "no GPU or the reference kernels are not built"}), flush=True)
-        return
+    from oracle import oracle as O
     from yolohtli_gb300 import _abi as A
     from yolohtli_gb300 import workloads as W
-    n = 512
-    r = A.param_defaults(n, n)
-    r.Lx = r.Ly = 3.0 * n / 256
-    r.hx = r.hy = r.Lx / (n - 1)
-    r = sr_params(r, (n / 2, n / 2))
-    u, v = W.ref2v_cross(n, n)
-    gin = [torch.tensor(np.asarray(x, np.float64), device="cuda") for x in (u, v)]
-    R.sr_driver(r, gin, 5, O.solve)
-    k = 60
-    t0 = time.perf_counter()
-    R.sr_driver(r, gin, k, O.solve, count0=5)
-    rate = k / (time.perf_counter() - t0)
-    print(json.dumps({
-        "impl": "reference", "metric": "SR steps/s", "value": round(rate, 2),
-        "unit": "SR steps/s", "n_gpus": args.gpus, "steps": 1, "warmup": 1,
-        "higher_is_better": True, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "fk_sr_512", "grid": [n, n],
-                   "model": "REF2V FP64 (the reference's model; it has no FK3V)"},
-        "reference_gpu": {"value": round(rate, 2), "unit": "SR steps/s",
-                          "sequence": "main.cu:894-954 on the reference's "
-                                      "kernels: RD, tips, slices, 12 trapz "
-                                      "launches each read back, host solve, "
-                                      "Cxy, BFECC"},
-        "cpu_baseline": None,
-        "e2e": {"value": round(rate, 2), "unit": "SR steps/s",
-                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
+    wl = W.fk_sr_512(seed=0)
+    n = wl.p.nx
+    t_start = time.perf_counter()
+    pre = O.run(wl.p, wl.model, wl.fk, wl.state0(), wl.nsteps - 1, wl.stims,
+                dtype=np.float64)
+    st = O.run(wl.p, wl.model, wl.fk, pre, 1, wl.stims, step0=wl.nsteps - 1,
+               dtype=np.float64)
+    whole = wl.p.copy()
+    whole.tipx = whole.tipy = n / 2
+    whole.tipOffsetX = whole.tipOffsetY = n // 2
+    tips = O.tips(whole, pre[0], st[0])
+    tip = (float(tips[0, 0]), float(tips[0, 1])) if len(tips) else (n / 2, n / 2)
+    q = sr_params(wl.p, tip)
+    start_s = time.perf_counter() - t_start
+    sr = O.SR(q, A.YH_MODEL_FK3V, wl.fk, st,
+              template_mode=A.YH_TEMPLATE_FROZEN, template=st)
+    sample = 25  # SR steps per bench step
+    times = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        sr.step(sample)
+        if k >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    rate = sample * len(times) / sum(times)
+    cores = os.cpu_count() or 1
+    line = {
+        "impl": "reference", "metric": "SR steps/s", "value": round(rate, 3),
+        "unit": "SR steps/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "fk_sr_512", "grid": [n, n], "model": "FK3V",
+                   "tau_d": 0.25, "template": "frozen", "disc_radius_cells": 160,
+                   "dt_ms": q.dt, "start_tips": int(len(tips)),
+                   "parallelism": "host cores"},
+        "cpu_baseline": {
+            "value": round(rate, 3), "unit": "SR steps/s", "cores": cores,
+            "kind": "port",
+            "sample": "each step: %d SR steps (RD, tips, slices + integrals, "
+                      "solve, comoving field, BFECC) of the 512^2 FK3V case, "
+                      "FP64 C/OpenMP restatement of the reference's sequence; "
+                      "start state built on the CPU in %.1f s" % (sample, start_s)},
+        "e2e": {"value": round(rate, 3), "unit": "SR steps/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    try:
+        import torch
+        from oracle import refgpu as R
+        if torch.cuda.is_available() and R.available():
+            r = A.param_defaults(n, n)
+            r.Lx = r.Ly = 3.0 * n / 256
+            r.hx = r.hy = r.Lx / (n - 1)
+            r = sr_params(r, (n / 2, n / 2))
+            u, v = W.ref2v_cross(n, n)
+            gin = [torch.tensor(np.asarray(x, np.float64), device="cuda")
+                   for x in (u, v)]
+            R.sr_driver(r, gin, 5, O.solve)
+            k = 60
+            t0 = time.perf_counter()
+            R.sr_driver(r, gin, k, O.solve, count0=5)
+            line["reference_gpu"] = {
+                "value": round(k / (time.perf_counter() - t0), 2),
+                "unit": "SR steps/s", "model": "REF2V FP64 (the reference's)",
+                "sequence": "main.cu:894-954 on the reference's kernels "
+                            "(sm_103a, headless): RD, tips, slices, 12 trapz "
+                            "launches each read back, host solve, Cxy, BFECC"}
+    except Exception as e:  # the GPU leg is optional beside the CPU value
+        line["reference_gpu"] = {"unavailable": str(e)[:200]}
+    print(json.dumps(line), flush=True)
 
 
 def run_adjoint(args):
