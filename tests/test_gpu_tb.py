@@ -54,13 +54,18 @@ def test_blocked_steps_equal_single_steps(nx, ny, holes):
             assert d <= 2e-6, (k, f, d)
 
 
-@pytest.mark.parametrize("nx,ny", [(300, 170), (68, 21), (256, 128), (8, 9)])
+@pytest.mark.parametrize("nx,ny", [(300, 170), (68, 21), (256, 128), (8, 9),
+                                   (160, 50)])
 @pytest.mark.parametrize("holes", [False, True])
 def test_two_step_kernel_is_bitwise_two_single_steps(nx, ny, holes):
-    # depth 2 runs rd_2s_kernel (64 x 16 tiles, step 1 on a 1-cell ring from
-    # a 2-cell halo): the tiles at the domain's far edges are cut (300 = 4 x
-    # 64 + 44, 170 = 10 x 16 + 10), the step count is odd (one single step
-    # at the end), and every value must equal the single-step engine's bits
+    # depth 2 runs the two-step tile kernel (64 x 16 tiles, step 1 on a
+    # 1-cell ring from a 2-cell halo), its inputs staged by TMA bulk tensor
+    # copies where the rows allow (nx % 4; with holes nx % 16: 256, 160) and
+    # by plain loads otherwise: the tiles at the domain's far edges are cut
+    # (300 = 4 x 64 + 44, 170 = 10 x 16 + 10, 160 = 2 x 64 + 32), the
+    # boxes can exceed the grid (8 x 9), the step count is odd (one single
+    # step at the end), and every value must equal the single-step engine's
+    # bits
     p, st, solid = fk_case(nx, ny, holes)
     ref = run(p, st, solid, 97, 1)
     got = run(p, st, solid, 97, 2)

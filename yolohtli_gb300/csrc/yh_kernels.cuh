@@ -61,9 +61,12 @@ cudaError_t launch_rd_tb(const StepCoeffs<float> &a, const Fld<float> &in,
 // yh_rd_2s.cu: two FK3V steps per launch (codes: hole codes or null)
 bool rd_2s_supported(const StepCoeffs<float> &a, const Fld<float> &in,
                      const Fld<float> &out, bool holes, const uint8_t *codes);
+// With err (a device flag), the tile inputs arrive by TMA bulk tensor copies
+// where the rows allow it (nx % 4; with hole codes nx % 16); an expired
+// wait sets *err. The same bits either way.
 cudaError_t launch_rd_2s(const StepCoeffs<float> &a, const Fld<float> &in,
                          const Fld<float> &out, const uint8_t *codes,
-                         cudaStream_t s);
+                         int *err, cudaStream_t s);
 
 // yh_rd_resident.cu
 constexpr int kResMaxStims = 32;  // stimulus events per resident launch

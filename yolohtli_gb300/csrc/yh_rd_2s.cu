@@ -11,6 +11,9 @@
 // single steps. Both steps use the operations of the single-step kernels
 // (fk3v_cells4 / fk3v_update with lap5), so the result has the same bits as
 // two launches of rd_step_vec4.
+#include <cuda.h>          // CUtensorMap and its enums (types only)
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
+
 #include "yh_kernels.cuh"
 
 namespace yh {
@@ -31,60 +34,16 @@ __device__ __forceinline__ int load_index(int i, int n) {
   return i < 0 ? 0 : (i >= n ? n - 1 : i);  // 2 cells out: never used
 }
 
+// Steps 1 and 2 of a tile once U0 (u with its 2-cell halo, mirror ghosts
+// in place), the quad's v, w, hole codes and the ring cell's v, w, code are
+// loaded: the arithmetic of the single-step kernels.
 template <bool HOLES>
-__global__ void __launch_bounds__(kThreads)
-    rd_2s_kernel(const StepCoeffs<float> a, const Fld<float> in,
-                 const Fld<float> out, const uint8_t *__restrict__ codes) {
-  __shared__ __align__(16) float U0[kH0 * kS];
-  __shared__ __align__(16) float U1[kH1 * kS];
+__device__ __forceinline__ void two_steps(
+    const StepCoeffs<float> &a, const Fld<float> &out, const float *U0,
+    float *U1, int x0, int y0, int t, int qx, int ty, int gi0, int gj,
+    bool quad_ok, const float (&vv)[4], const float (&ww)[4], uint32_t code4,
+    int rr, int rc, bool ring_ok, float rv, float rw, uint32_t rcode) {
   const int nx = a.nx, ny = a.ny;
-  const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
-  const int t = threadIdx.x;
-  grid_dep_wait();
-  grid_dep_launch();
-  // u over the tile and a 2-cell halo
-  for (int idx = t; idx < kH0 * kW0; idx += kThreads) {
-    const int r = idx / kW0, c = idx - r * kW0;
-    const int gi = load_index(x0 - 2 + c, nx), gj = load_index(y0 - 2 + r, ny);
-    U0[r * kS + c + 2] = __ldg(in.f[0] + (size_t)gj * nx + gi);
-  }
-  // this thread's quad of the tile: row y0 + ty, cells x0 + 4 qx .. + 3
-  const int qx = t & 15, ty = t >> 4;
-  const int gi0 = x0 + 4 * qx, gj = y0 + ty;
-  const bool quad_ok = gi0 < nx && gj < ny;  // nx % 4 == 0: all four or none
-  float vv[4] = {0.f, 0.f, 0.f, 0.f}, ww[4] = {0.f, 0.f, 0.f, 0.f};
-  uint32_t code4 = 0x01010101u;
-  if (quad_ok) {
-    const size_t g = (size_t)gj * nx + gi0;
-    const float4 v4 = __ldg(reinterpret_cast<const float4 *>(in.f[1] + g));
-    const float4 w4 = __ldg(reinterpret_cast<const float4 *>(in.f[2] + g));
-    vv[0] = v4.x; vv[1] = v4.y; vv[2] = v4.z; vv[3] = v4.w;
-    ww[0] = w4.x; ww[1] = w4.y; ww[2] = w4.z; ww[3] = w4.w;
-    if (HOLES) code4 = __ldg(reinterpret_cast<const unsigned int *>(codes + g));
-  }
-  // this thread's ring cell (t < kRing), in step-1 tile coordinates
-  int rr = 0, rc = 0;
-  if (t < kW1) {
-    rr = 0; rc = t;                              // row above the tile
-  } else if (t < 2 * kW1) {
-    rr = kH1 - 1; rc = t - kW1;                  // row below
-  } else if (t < 2 * kW1 + kTH) {
-    rr = 1 + t - 2 * kW1; rc = 0;                // column left
-  } else {
-    rr = 1 + t - 2 * kW1 - kTH; rc = kW1 - 1;    // column right
-  }
-  const int rgi = x0 - 1 + rc, rgj = y0 - 1 + rr;
-  const bool ring_ok = t < kRing && rgi >= 0 && rgi < nx && rgj >= 0 && rgj < ny;
-  float rv = 0.f, rw = 0.f;
-  uint32_t rcode = 1u;
-  if (ring_ok) {
-    const size_t g = (size_t)rgj * nx + rgi;
-    rv = __ldg(in.f[1] + g);
-    rw = __ldg(in.f[2] + g);
-    if (HOLES) rcode = __ldg(codes + g);
-  }
-  __syncthreads();
-
   // step 1: the quad (v, w kept in registers) and the ring cell
   float u1[4], v1[4], w1[4];
   const bool plain = !HOLES || code4 == 0x01010101u;
@@ -151,6 +110,229 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+template <bool HOLES>
+__global__ void __launch_bounds__(kThreads)
+    rd_2s_kernel(const StepCoeffs<float> a, const Fld<float> in,
+                 const Fld<float> out, const uint8_t *__restrict__ codes) {
+  __shared__ __align__(16) float U0[kH0 * kS];
+  __shared__ __align__(16) float U1[kH1 * kS];
+  const int nx = a.nx, ny = a.ny;
+  const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
+  const int t = threadIdx.x;
+  grid_dep_wait();
+  grid_dep_launch();
+  // u over the tile and a 2-cell halo
+  for (int idx = t; idx < kH0 * kW0; idx += kThreads) {
+    const int r = idx / kW0, c = idx - r * kW0;
+    const int gi = load_index(x0 - 2 + c, nx), gj = load_index(y0 - 2 + r, ny);
+    U0[r * kS + c + 2] = __ldg(in.f[0] + (size_t)gj * nx + gi);
+  }
+  // this thread's quad of the tile: row y0 + ty, cells x0 + 4 qx .. + 3
+  const int qx = t & 15, ty = t >> 4;
+  const int gi0 = x0 + 4 * qx, gj = y0 + ty;
+  const bool quad_ok = gi0 < nx && gj < ny;  // nx % 4 == 0: all four or none
+  float vv[4] = {0.f, 0.f, 0.f, 0.f}, ww[4] = {0.f, 0.f, 0.f, 0.f};
+  uint32_t code4 = 0x01010101u;
+  if (quad_ok) {
+    const size_t g = (size_t)gj * nx + gi0;
+    const float4 v4 = __ldg(reinterpret_cast<const float4 *>(in.f[1] + g));
+    const float4 w4 = __ldg(reinterpret_cast<const float4 *>(in.f[2] + g));
+    vv[0] = v4.x; vv[1] = v4.y; vv[2] = v4.z; vv[3] = v4.w;
+    ww[0] = w4.x; ww[1] = w4.y; ww[2] = w4.z; ww[3] = w4.w;
+    if (HOLES) code4 = __ldg(reinterpret_cast<const unsigned int *>(codes + g));
+  }
+  // this thread's ring cell (t < kRing), in step-1 tile coordinates
+  int rr = 0, rc = 0;
+  if (t < kW1) {
+    rr = 0; rc = t;                              // row above the tile
+  } else if (t < 2 * kW1) {
+    rr = kH1 - 1; rc = t - kW1;                  // row below
+  } else if (t < 2 * kW1 + kTH) {
+    rr = 1 + t - 2 * kW1; rc = 0;                // column left
+  } else {
+    rr = 1 + t - 2 * kW1 - kTH; rc = kW1 - 1;    // column right
+  }
+  const int rgi = x0 - 1 + rc, rgj = y0 - 1 + rr;
+  const bool ring_ok = t < kRing && rgi >= 0 && rgi < nx && rgj >= 0 && rgj < ny;
+  float rv = 0.f, rw = 0.f;
+  uint32_t rcode = 1u;
+  if (ring_ok) {
+    const size_t g = (size_t)rgj * nx + rgi;
+    rv = __ldg(in.f[1] + g);
+    rw = __ldg(in.f[2] + g);
+    if (HOLES) rcode = __ldg(codes + g);
+  }
+  __syncthreads();
+  two_steps<HOLES>(a, out, U0, U1, x0, y0, t, qx, ty, gi0, gj, quad_ok, vv,
+                   ww, code4, rr, rc, ring_ok, rv, rw, rcode);
+}
+
+// The same two steps with the tile's inputs staged by the tensor memory
+// accelerator: one thread issues four 2D bulk tensor copies (u over the
+// tile and a 2-cell halo, 72 x 20 from (x0 - 4, y0 - 2); v and w over the
+// tile and its ring, 72 x 18 from (x0 - 4, y0 - 1); the hole codes, 96 x 18
+// bytes from (x0 - 16, y0 - 1)) on one mbarrier, in place of the threads'
+// ~11 loads each. Every box starts at an x that is a multiple of 16 bytes
+// (x0 is a multiple of 64). Cells outside the grid arrive as zeros; the
+// mirror ghosts at x = -1, nx and y = -1, ny are then copied in shared
+// memory (the cells two out are never read). The wait is bounded by 1 s
+// of %globaltimer, after which the block sets *err and returns.
+struct TileMaps {
+  CUtensorMap u, v, w, c;
+};
+
+constexpr int kVW = 72, kVH = kTH + 2;  // v, w box: the tile and its ring
+constexpr int kCW = 96;                 // hole-code box width (bytes)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void tma_2d(void *dst, const CUtensorMap *map,
+                                       int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::"
+      "bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y),
+      "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// true once phase 0 of the barrier completed; false after 1 s
+__device__ __forceinline__ bool bar_wait0(uint64_t *bar) {
+  const uint32_t b = smem_u32(bar);
+  unsigned long long t0 = 0;
+  for (int spin = 0;; ++spin) {
+    uint32_t done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; "
+        "selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(b)
+        : "memory");
+    if (done) return true;
+    if (spin == 0) t0 = gtimer();
+    else if (gtimer() - t0 > 1000000000ull) return false;
+  }
+}
+
+template <bool HOLES>
+__global__ void __launch_bounds__(kThreads)
+    rd_2s_tma_kernel(const StepCoeffs<float> a, const __grid_constant__ TileMaps m,
+                     const Fld<float> out, int *err) {
+  __shared__ __align__(128) float U0[kH0 * kS];
+  __shared__ __align__(128) float Vs[kVH * kVW];
+  __shared__ __align__(128) float Ws[kVH * kVW];
+  __shared__ __align__(128) uint8_t Cs[kVH * kCW];
+  __shared__ __align__(16) float U1[kH1 * kS];
+  __shared__ __align__(8) uint64_t bar;
+  const int nx = a.nx, ny = a.ny;
+  const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
+  const int t = threadIdx.x;
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar))
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  grid_dep_wait();
+  grid_dep_launch();
+  if (t == 0) {
+    const uint32_t bytes = (uint32_t)(sizeof(float) * (kH0 * kS + 2 * kVH * kVW) +
+                                      (HOLES ? kVH * kCW : 0));
+    asm volatile(
+        "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+            smem_u32(&bar)),
+        "r"(bytes)
+        : "memory");
+    tma_2d(U0, &m.u, x0 - 4, y0 - 2, &bar);
+    tma_2d(Vs, &m.v, x0 - 4, y0 - 1, &bar);
+    tma_2d(Ws, &m.w, x0 - 4, y0 - 1, &bar);
+    if (HOLES) tma_2d(Cs, &m.c, x0 - 16, y0 - 1, &bar);
+  }
+  if (!bar_wait0(&bar)) {
+    if (t == 0) atomicExch(err, 1);
+    return;
+  }
+  // mirror ghosts of u: x = -1 <- 1, x = nx <- nx - 2 (columns), then the
+  // rows y = -1 <- 1, y = ny <- ny - 2 (U0 row r is y0 - 2 + r, column s is
+  // x0 - 4 + s)
+  if (t < kH0) {
+    if (x0 == 0) U0[t * kS + 3] = U0[t * kS + 5];
+    const int sR = nx - x0 + 4;
+    if (sR < kS) U0[t * kS + sR] = U0[t * kS + sR - 2];
+  }
+  __syncthreads();
+  if (t < kS) {
+    if (y0 == 0) U0[1 * kS + t] = U0[3 * kS + t];
+    const int rT = ny - y0 + 2;
+    if (rT < kH0) U0[rT * kS + t] = U0[(rT - 2) * kS + t];
+  }
+  // this thread's quad of the tile: row y0 + ty, cells x0 + 4 qx .. + 3
+  const int qx = t & 15, ty = t >> 4;
+  const int gi0 = x0 + 4 * qx, gj = y0 + ty;
+  const bool quad_ok = gi0 < nx && gj < ny;
+  const float4 v4 = *reinterpret_cast<const float4 *>(Vs + (ty + 1) * kVW + 4 * qx + 4);
+  const float4 w4 = *reinterpret_cast<const float4 *>(Ws + (ty + 1) * kVW + 4 * qx + 4);
+  const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+  const float ww[4] = {w4.x, w4.y, w4.z, w4.w};
+  const uint32_t code4 =
+      HOLES ? *reinterpret_cast<const uint32_t *>(Cs + (ty + 1) * kCW + 4 * qx + 16)
+            : 0x01010101u;
+  int rr = 0, rc = 0;
+  if (t < kW1) {
+    rr = 0; rc = t;
+  } else if (t < 2 * kW1) {
+    rr = kH1 - 1; rc = t - kW1;
+  } else if (t < 2 * kW1 + kTH) {
+    rr = 1 + t - 2 * kW1; rc = 0;
+  } else {
+    rr = 1 + t - 2 * kW1 - kTH; rc = kW1 - 1;
+  }
+  const int rgi = x0 - 1 + rc, rgj = y0 - 1 + rr;
+  const bool ring_ok = t < kRing && rgi >= 0 && rgi < nx && rgj >= 0 && rgj < ny;
+  const float rv = ring_ok ? Vs[rr * kVW + rc + 3] : 0.f;
+  const float rw = ring_ok ? Ws[rr * kVW + rc + 3] : 0.f;
+  const uint32_t rcode = (HOLES && ring_ok) ? Cs[rr * kCW + rc + 15] : 1u;
+  __syncthreads();
+  two_steps<HOLES>(a, out, U0, U1, x0, y0, t, qx, ty, gi0, gj, quad_ok, vv,
+                   ww, code4, rr, rc, ring_ok, rv, rw, rcode);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); null when unavailable.
+PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+bool encode_2d(CUtensorMap *m, const void *base, bool bytes, int nx, int ny,
+               int bx, int by) {
+  const PFN_cuTensorMapEncodeTiled_v12000 fn = encode_tiled();
+  if (!fn) return false;
+  const size_t es = bytes ? 1 : sizeof(float);
+  const cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
+  const cuuint64_t strides[1] = {(cuuint64_t)nx * es};
+  const cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, bytes ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+            2, const_cast<void *>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 }  // namespace
 
 bool rd_2s_supported(const StepCoeffs<float> &a, const Fld<float> &in,
@@ -160,9 +342,39 @@ bool rd_2s_supported(const StepCoeffs<float> &a, const Fld<float> &in,
          (!codes || (reinterpret_cast<uintptr_t>(codes) & 3) == 0);
 }
 
+// The tensor-memory-accelerator form needs 16-byte rows for every box:
+// nx % 4 for the FP32 fields, nx % 16 for the hole codes.
+static bool tma_ok(const StepCoeffs<float> &a, const uint8_t *codes) {
+#ifdef YH_RD2S_NO_TMA
+  (void)a; (void)codes;
+  return false;
+#else
+  return (a.nx % 4) == 0 &&
+         (!codes || ((a.nx % 16) == 0 &&
+                     (reinterpret_cast<uintptr_t>(codes) & 15) == 0)) &&
+         encode_tiled() != nullptr;
+#endif
+}
+
 cudaError_t launch_rd_2s(const StepCoeffs<float> &a, const Fld<float> &in,
                          const Fld<float> &out, const uint8_t *codes,
-                         cudaStream_t s) {
+                         int *err, cudaStream_t s) {
+  if (err && tma_ok(a, codes)) {
+    TileMaps m;
+    bool ok = encode_2d(&m.u, in.f[0], false, a.nx, a.ny, kS, kH0) &&
+              encode_2d(&m.v, in.f[1], false, a.nx, a.ny, kVW, kVH) &&
+              encode_2d(&m.w, in.f[2], false, a.nx, a.ny, kVW, kVH);
+    if (codes) ok = ok && encode_2d(&m.c, codes, true, a.nx, a.ny, kCW, kVH);
+    else m.c = m.u;
+    if (ok) {
+      const dim3 grid((a.nx + kTW - 1) / kTW, (a.ny + kTH - 1) / kTH);
+      if (codes)
+        return launch_pdl(rd_2s_tma_kernel<true>, grid, dim3(kThreads), 0, s, a,
+                          m, out, err);
+      return launch_pdl(rd_2s_tma_kernel<false>, grid, dim3(kThreads), 0, s, a,
+                        m, out, err);
+    }
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((a.nx + kTW - 1) / kTW, (a.ny + kTH - 1) / kTH);
   cfg.blockDim = dim3(kThreads);

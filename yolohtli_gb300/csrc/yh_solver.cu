@@ -139,11 +139,11 @@ extern "C" int yh_create(const yh_param_var *p, int model,
     if (e == cudaSuccess)
       h->plan = resident_plan(make_step_coeffs<float>(h->p, h->model, &h->fk), dev);
   }
-  if (e == cudaSuccess && h->plan.ok) {
+  // the flag a bounded wait sets when it gives up (resident engine, TMA)
+  if (e == cudaSuccess) e = cudaMalloc(&h->res_error, 256);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->res_error, 0, 256, h->s);
+  if (e == cudaSuccess && h->plan.ok)
     e = cudaMalloc(&h->res_halo, resident_halo_bytes(h->plan, p->nx));
-    if (e == cudaSuccess) e = cudaMalloc(&h->res_error, 256);
-    if (e == cudaSuccess) e = cudaMemsetAsync(h->res_error, 0, 256, h->s);
-  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
   if (e != cudaSuccess) {
     yh_destroy(h);
@@ -320,7 +320,7 @@ static cudaError_t enqueue_plain(yh_solver *h, int len) {
       const int k = std::min(left, h->time_block);
       if (k == 2 && rd_2s_supported(a, h->cur, h->nxt, h->solid != nullptr,
                                     h->codes))
-        e = launch_rd_2s(a, h->cur, h->nxt, h->codes, h->s);
+        e = launch_rd_2s(a, h->cur, h->nxt, h->codes, h->res_error, h->s);
       else
         e = launch_rd_tb(a, h->cur, h->nxt, h->solid, k, h->s);
       left -= k;
