@@ -402,6 +402,13 @@ int yh_get_time_block(yh_solver *h, int *steps_per_launch);
  * without gateDiff); YH_EUNSUPPORTED otherwise. */
 enum { YH_ENGINE_STEP = 0, YH_ENGINE_BLOCKED = 1, YH_ENGINE_RESIDENT = 2 };
 int yh_set_engine(yh_solver *h, int engine, int steps_per_launch);
+/* Failure self-test of the bounded device-side waits: a 128^2 FK3V grid on
+ * the resident engine, first with one block publishing none of its
+ * boundary rows (its neighbours' waits run out after their 1 s bound; the
+ * launch ends with every block returned and *muted_status = YH_ETIMEOUT),
+ * then normally on the same context (*after_status = YH_OK). Returns
+ * YH_EUNSUPPORTED where the resident engine does not run. */
+int yh_selftest_resident_timeout(int *muted_status, int *after_status);
 int yh_get_engine(yh_solver *h, int *engine, int *steps_per_launch);
 
 /* Autotuner: times probe_steps plain steps from the current state for each

@@ -107,3 +107,18 @@ def test_fk_spiral_protocol_resident_vs_step_1500_steps():
     d = max_abs(a[0], b[0])
     print("FK3V 256^2 1500 steps: resident vs step max |du| = %.2e" % d)
     assert d <= 1e-5
+
+
+def test_bounded_waits_report_a_timeout_and_leave_the_context_usable():
+    # one block of a resident launch publishes none of its boundary rows: its
+    # neighbours' waits run out after their 1 s bound and the launch ends
+    # with YH_ETIMEOUT; the next launch on the same context runs normally
+    import ctypes as C
+    from yolohtli_gb300._loader import load
+    muted, after = C.c_int(), C.c_int()
+    rc = load().yh_selftest_resident_timeout(C.byref(muted), C.byref(after))
+    if rc == A.YH_EUNSUPPORTED:
+        pytest.skip("the resident engine does not run on this device")
+    assert rc == A.YH_OK
+    assert muted.value == A.YH_ETIMEOUT
+    assert after.value == A.YH_OK

@@ -78,6 +78,7 @@ SIGNATURES = {
     "yh_batch_autotune": (_i, [_v, _i, _P(C.c_longlong), _P(_i)]),
     "yh_batch_get_step": (_i, [_v, _P(_i)]),
     "yh_batch_get_launch_count": (_i, [_v, _P(C.c_longlong)]),
+    "yh_selftest_resident_timeout": (_i, [_P(_i), _P(_i)]),
     # adjoint
     "yh_adjoint_create": (_i, [_P(A.ParamVar), _P(A.FKParams), _i, _i, _i, _i,
                                _i, _d, _v, _P(_v)]),

@@ -80,14 +80,15 @@ ResidentPlan resident_plan(const StepCoeffs<float> &a, int device);
 // bytes of the tagged boundary-row buffers of a plan
 size_t resident_halo_bytes(const ResidentPlan &pl, int nx);
 // io: the state, updated in place; prev_u (may be null): receives u of the
-// level before the last step.
+// level before the last step. mute >= 0: that block publishes no boundary
+// row, so its neighbours' bounded waits run out (the failure self-test).
 cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
                                float *prev_u, const uint8_t *solid,
                                int nsteps, int step0,
                                const yh_stim *stims, int nstims,
                                const ResidentPlan &pl,
                                unsigned long long *halo, int *error,
-                               cudaStream_t s);
+                               cudaStream_t s, int mute = -1);
 
 // yh_sr.cu
 // holes: the hole-domain branch of the reference (a disc around the grid

@@ -53,6 +53,7 @@ struct ResArgs {
   const uint8_t *solid;         // nullptr: no holes
   unsigned long long *halo;     // [2][nb][2][nx] tagged boundary rows of u
   int *error;                   // set to 1 when a wait gave up
+  int mute;                     // a block that publishes nothing (-1: none)
   int threads;            // compute threads; the rest of the block receives
   int nsteps, step0;
   int nb, rq, rrem, rmax;
@@ -231,7 +232,7 @@ __device__ __forceinline__ void res_item(const StepCoeffs<float> &a, int lr,
   st_cells<CW>(nxt + (lr + 1) * nx + i0, ou);
   st_cells<CW>(vp, ov);
   if (W3) st_cells<CW>(wp, ow);
-  if (publish) st_tagged_vec<CW>(pp + i0, ou, tag);
+  if (publish && pub) st_tagged_vec<CW>(pp + i0, ou, tag);
 }
 
 // u = value on the tissue cells of global row gy held in local buffer row
@@ -382,8 +383,9 @@ __global__ void __launch_bounds__(kResThreads + NC, 1)
                           (hole_pattern(sn, sc, ss) << 3));
     }
     // the boundary rows of the state after 0 steps, tag 0, buffer 0
-    if (lr == 0 && !bottom) st_tagged(A.halo + (size_t)b * 2 * nx + i, u, 0u);
-    if (lr == R - 1 && !top)
+    if (lr == 0 && !bottom && b != A.mute)
+      st_tagged(A.halo + (size_t)b * 2 * nx + i, u, 0u);
+    if (lr == R - 1 && !top && b != A.mute)
       st_tagged(A.halo + (size_t)b * 2 * nx + nx + i, u, 0u);
   }
   // halo rows of the state after 0 steps
@@ -417,7 +419,8 @@ __global__ void __launch_bounds__(kResThreads + NC, 1)
       // the order rows 0, R-1, 1 .. R-2 (virtual row vr), nq items per row,
       // thread t taking items t, t + T, ...
       unsigned long long *pub =
-          A.halo + (size_t)((s + 1) & 1) * par_stride + (size_t)b * 2 * nx;
+          b == A.mute ? nullptr
+                      : A.halo + (size_t)((s + 1) & 1) * par_stride + (size_t)b * 2 * nx;
       for (int vr = vr0, q = q0; vr < R;) {
         const int lr = vr == 0 ? 0 : (vr == 1 ? R - 1 : vr - 1);
         res_item<MODEL, HOLES, CW>(a, lr, q, R, bottom, top, cur, nxt, Vs, Ws,
@@ -506,10 +509,11 @@ cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
                                const yh_stim *stims, int nstims,
                                const ResidentPlan &pl,
                                unsigned long long *halo, int *error,
-                               cudaStream_t s) {
+                               cudaStream_t s, int mute) {
   if (!pl.ok || nstims > kResMaxStims || nsteps < 0) return cudaErrorInvalidValue;
   if (nsteps == 0) return cudaSuccess;
   ResArgs A;
+  A.mute = mute;
   A.a = a;
   A.io = io;
   A.prev_u = prev_u;

@@ -306,6 +306,51 @@ static int run_resident(yh_solver *h, int nsteps, const yh_stim *ev,
   return YH_OK;
 }
 
+// Failure self-test of the bounded device-side waits: a small FK3V grid on
+// the resident engine, once with one block publishing nothing (its
+// neighbours' waits run out after their 1 s bound, set the error flag and
+// every block returns), once normally on the same context. No fault, trap
+// or unbounded wait is involved.
+extern "C" int yh_selftest_resident_timeout(int *muted_status,
+                                            int *after_status) {
+  if (!muted_status || !after_status) return YH_EINVAL;
+  const int n = 128;
+  yh_param_var p;
+  yh_fk_params fk;
+  int rc = yh_param_defaults(&p, n, n);
+  if (!rc) rc = yh_fk_defaults(&fk);
+  if (rc) return rc;
+  p.hx = p.hy = 0.025;
+  p.Lx = p.Ly = 0.025 * (n - 1);
+  p.dt = 0.05;
+  p.diff_par = p.diff_per = p.Dxx = p.Dyy = 0.001;
+  p.Dxy = 0.0;
+  p.gateDiff = false;
+  rc = yh_param_derive(&p);
+  if (rc) return rc;
+  yh_solver *h = nullptr;
+  rc = yh_create(&p, YH_MODEL_FK3V, &fk, nullptr, nullptr, &h);
+  if (rc) return rc;
+  if (!h->plan.ok || h->plan.nb < 3) {
+    yh_destroy(h);
+    return YH_EUNSUPPORTED;
+  }
+  const StepCoeffs<float> a = make_step_coeffs<float>(h->p, h->model, &h->fk);
+  cudaError_t e = launch_rd_resident(a, h->cur, nullptr, h->solid, 4, 0,
+                                     nullptr, 0, h->plan, h->res_halo,
+                                     h->res_error, h->s, 1);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  *muted_status = e == cudaSuccess ? resident_status(h) : st(e);
+  e = cudaMemsetAsync(h->res_error, 0, sizeof(int), h->s);
+  if (e == cudaSuccess)
+    e = launch_rd_resident(a, h->cur, nullptr, h->solid, 4, 0, nullptr, 0,
+                           h->plan, h->res_halo, h->res_error, h->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  *after_status = e == cudaSuccess ? resident_status(h) : st(e);
+  yh_destroy(h);
+  return YH_OK;
+}
+
 // `len` plain steps starting from h->cur, leaving the result in h->cur.
 // With time_block > 1 the temporally blocked kernel takes that many steps
 // per launch (its depth is fixed per launch, so the ping-pong flips once per
