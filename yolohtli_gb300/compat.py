@@ -1,8 +1,8 @@
 """The reference's own host entry points as this library exports them
 (include/yolohtli_compat.h): ctypes bindings with their C++ signatures
-(hostPrototypes.h:22-51), for Python drivers written against the
+(hostPrototypes.h:22-51), for Python programs written against the
 reference's API and for the tests and the benchmark that call them. FP64
-(REAL = double) device buffers; call set_params once with the driver's
+(REAL = double) device buffers; call set_params once with the program's
 paramVar, as yh_compat_set_params is called after the reference's
 cudaMemcpyToSymbol block (main.cu:309-402)."""
 import ctypes as C
