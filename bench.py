@@ -376,8 +376,8 @@ def run_batch(args):
             "config": {"workload": bw.name, "instances": len(insts),
                        "cells": bw.cells, "steps_per_solve": bw.nsteps,
                        "sizes": "n ~ U{128,160,...,768}, square",
-                       "schedule": "autotuned: groups of ~%d cells on %d streams"
-                                   % tuned,
+                       "schedule": "autotuned: groups of ~%d cells on %d "
+                                   "streams, %d steps per launch" % tuned,
                        "l2": "1.48 GB of state per step, above the L2; "
                              "each group's %.0f MB (two levels) stays in it"
                              % (tuned[0] * 24 / 1e6),

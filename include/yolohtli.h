@@ -496,6 +496,7 @@ int yh_batch_create(int count, const yh_param_var *params,
                     const yh_fk_params *fk, const uint8_t *const *masks,
                     void *stream, yh_batch **out);
 int yh_batch_destroy(yh_batch *b);
+/* YH_ETIMEOUT if a depth-2 launch's bounded TMA wait gave up. */
 int yh_batch_synchronize(yh_batch *b);
 /* State of instance k (host or device pointers, nx*ny floats each). */
 int yh_batch_set_state(yh_batch *b, int k, const float *u, const float *v,
@@ -512,13 +513,18 @@ int yh_batch_run(yh_batch *b, int nsteps, const yh_batch_stim *stims,
  * instances first) on `streams` internal streams (1-64). The default is
  * 1,048,576 cells on 2 streams. */
 int yh_batch_set_schedule(yh_batch *b, long long group_cells, int streams);
+/* Steps per launch: 1 (the default) or 2 (64 x 16 tiles, inputs staged by
+ * TMA bulk tensor copies, the same bits; YH_EUNSUPPORTED unless every
+ * instance's rows allow it: nx % 16 == 0 for instances with holes). */
+int yh_batch_set_depth(yh_batch *b, int depth);
 /* The schedule autotuner: times probe_steps steps (rounded up to even, no
  * events) of every schedule of groups of 256 K, 512 K, 1 M or 2 M cells
- * on 2, 3 or 4 streams on the current state, keeps the fastest and
- * restores the state and the step count. The choice is returned in
- * *group_cells and *streams (either may be NULL). */
+ * on 2, 3 or 4 streams at depth 1 and (where supported) 2 on the current
+ * state, keeps the fastest and restores the state and the step count. The
+ * choice is returned in *group_cells, *streams and *depth (any may be
+ * NULL). */
 int yh_batch_autotune(yh_batch *b, int probe_steps, long long *group_cells,
-                      int *streams);
+                      int *streams, int *depth);
 int yh_batch_get_step(yh_batch *b, int *step);
 int yh_batch_get_launch_count(yh_batch *b, long long *n);
 

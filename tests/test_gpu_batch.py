@@ -83,14 +83,19 @@ def test_batch_equals_the_single_grid_solver_bitwise():
     b.close()
 
 
+@pytest.mark.parametrize("depth", [1, 2])
 @pytest.mark.parametrize("schedule", [(1 << 12, 3), (1, 4), (1 << 30, 1)])
-def test_every_schedule_gives_the_same_bits(schedule):
-    # groups of one instance up to one group for all, on 1-4 streams
+def test_every_schedule_gives_the_same_bits(schedule, depth):
+    # groups of one instance up to one group for all, on 1-4 streams, one or
+    # two steps per launch (depth 2: TMA-staged 64 x 16 tiles; runs of odd
+    # length and events on either step of a launch, including two events
+    # on one step)
     insts = _instances()
     runs = [130, 170]
     b = Batch([w.p for w in insts], [w.fk for w in insts],
               [w.solid for w in insts])
     b.set_schedule(*schedule)
+    b.set_depth(depth)
     for k, w in enumerate(insts):
         b.set_state(k, *w.state0())
     ev = [(k, st) for k, w in enumerate(insts) for st in w.stims]
@@ -116,8 +121,9 @@ def test_autotune_restores_the_state_and_keeps_the_bits():
     b.synchronize()
     before = [b.get_state(k) for k in range(len(insts))]
     launches = b.launch_count()
-    g, q = b.autotune(64)
+    g, q, d = b.autotune(64)
     assert g in (1 << 18, 1 << 19, 1 << 20, 1 << 21) and q in (2, 3, 4)
+    assert d in (1, 2)
     assert b.step_count() == 100 and b.launch_count() == launches
     for k in range(len(insts)):
         now = b.get_state(k)

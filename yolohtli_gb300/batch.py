@@ -92,11 +92,15 @@ class Batch:
 
     def autotune(self, probe_steps=256):
         """Times the schedules on the current state (restored), keeps the
-        fastest; returns (group_cells, streams)."""
-        g, q = C.c_longlong(), C.c_int()
+        fastest; returns (group_cells, streams, steps per launch)."""
+        g, q, d = C.c_longlong(), C.c_int(), C.c_int()
         check("yh_batch_autotune", self.lib.yh_batch_autotune(
-            self.h, int(probe_steps), C.byref(g), C.byref(q)))
-        return g.value, q.value
+            self.h, int(probe_steps), C.byref(g), C.byref(q), C.byref(d)))
+        return g.value, q.value, d.value
+
+    def set_depth(self, depth):
+        """Steps per launch: 1, or 2 (TMA-staged 64 x 16 tiles)."""
+        check("yh_batch_set_depth", self.lib.yh_batch_set_depth(self.h, int(depth)))
 
     def synchronize(self):
         check("yh_batch_synchronize", self.lib.yh_batch_synchronize(self.h))

@@ -30,7 +30,7 @@
 #include <new>
 #include <vector>
 
-#include "yh_kernels.cuh"
+#include "yh_tile2s.cuh"
 
 namespace yh {
 template <typename Real>
@@ -134,6 +134,155 @@ __global__ void __launch_bounds__(kBatchThreads)
       make_float4(ow[0], ow[1], ow[2], ow[3]);
 }
 
+// Depth 2: two steps of a group per launch in the two-step tile scheme
+// (64 x 16 tiles, inputs staged by TMA from the instance's tensor maps,
+// the same bits as two single steps). unit.y: tile column (low 16 bits) and
+// tile row (high 16 bits) of 64 x 16 tiles. The events of step gs apply to
+// the staged u before its mirror ghosts are copied, those of step gs + 1 to
+// the step-1 u (tile and ring) before its ghosts are copied: the values the
+// single-step kernel reads.
+struct BatchMaps {
+  CUtensorMap u[2], v[2], w[2], c;  // fields of level 0 / 1, hole codes
+};
+
+struct EventHook {
+  const BatchInst *I;
+  int gs, x0, y0, nx, ny, t;
+  __device__ void operator()(float *U1) const {
+    using namespace tile2s;
+    bool any = false;
+    for (int e = 0; e < I->nev; ++e) any |= I->ev[e].step == gs;
+    if (!any) return;  // the same for every thread of the block
+    for (int e = 0; e < I->nev; ++e) {
+      const yh_stim &ev = I->ev[e];
+      if (ev.step != gs) continue;
+      for (int k = t; k < kH1 * kW1; k += kThreads) {
+        const int r = k / kW1, c = k - r * kW1;
+        const int x = x0 - 1 + c, y = y0 - 1 + r;
+        if (x >= 0 && x < nx && y >= 0 && y < ny && in_box(ev, x, y))
+          U1[r * kS + c + 3] = ev.value;
+      }
+    }
+    __syncthreads();
+  }
+};
+
+__global__ void __launch_bounds__(tile2s::kThreads)
+    rd_batch_2s_kernel(const BatchInst *__restrict__ insts,
+                       const BatchMaps *__restrict__ maps,
+                       const int2 *__restrict__ units, int lvl, Fld<float> out,
+                       const int *__restrict__ base, int di, int *err) {
+  using namespace tile2s;
+  __shared__ BatchInst I;
+  __shared__ __align__(128) float U0[kH0 * kS];
+  __shared__ __align__(128) float Vs[kVH * kVW];
+  __shared__ __align__(128) float Ws[kVH * kVW];
+  __shared__ __align__(128) uint8_t Cs[kVH * kCW];
+  __shared__ __align__(16) float U1[kH1 * kS];
+  __shared__ __align__(8) uint64_t bar;
+  const int2 un = units[blockIdx.x];
+  const int t = threadIdx.x;
+  {
+    const int *src = reinterpret_cast<const int *>(insts + un.x);
+    int *dst = reinterpret_cast<int *>(&I);
+    for (int k = t; k < (int)(sizeof(BatchInst) / 4); k += kThreads)
+      dst[k] = __ldg(src + k);
+  }
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar))
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  grid_dep_wait();
+  grid_dep_launch();
+  __syncthreads();
+  const StepCoeffs<float> &a = I.a;
+  const int nx = a.nx, ny = a.ny;
+  const int x0 = (un.y & 0xffff) * kTW, y0 = (un.y >> 16) * kTH;
+  const bool holes = I.holes != 0;
+  const BatchMaps *M = maps + un.x;
+  if (t == 0) {
+    const uint32_t bytes = (uint32_t)(sizeof(float) * (kH0 * kS + 2 * kVH * kVW) +
+                                      (holes ? kVH * kCW : 0));
+    asm volatile(
+        "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+            smem_u32(&bar)),
+        "r"(bytes)
+        : "memory");
+    tma_2d(U0, &M->u[lvl], x0 - 4, y0 - 2, &bar);
+    tma_2d(Vs, &M->v[lvl], x0 - 4, y0 - 1, &bar);
+    tma_2d(Ws, &M->w[lvl], x0 - 4, y0 - 1, &bar);
+    if (holes) tma_2d(Cs, &M->c, x0 - 16, y0 - 1, &bar);
+  }
+  if (!bar_wait0(&bar)) {
+    if (t == 0) atomicExch(err, 1);
+    return;
+  }
+  const int gs = *base + di;
+  // events of step gs on the in-grid cells of U0 (row r: y0 - 2 + r,
+  // column s: x0 - 4 + s)
+  for (int e = 0; e < I.nev; ++e) {
+    const yh_stim &ev = I.ev[e];
+    if (ev.step != gs) continue;
+    for (int k = t; k < kH0 * kS; k += kThreads) {
+      const int r = k / kS, c = k - r * kS;
+      const int x = x0 - 4 + c, y = y0 - 2 + r;
+      if (x >= 0 && x < nx && y >= 0 && y < ny && in_box(ev, x, y))
+        U0[k] = ev.value;
+    }
+  }
+  __syncthreads();
+  // mirror ghosts of u: columns x = -1, nx, then rows y = -1, ny
+  if (t < kH0) {
+    if (x0 == 0) U0[t * kS + 3] = U0[t * kS + 5];
+    const int sR = nx - x0 + 4;
+    if (sR < kS) U0[t * kS + sR] = U0[t * kS + sR - 2];
+  }
+  __syncthreads();
+  if (t < kS) {
+    if (y0 == 0) U0[1 * kS + t] = U0[3 * kS + t];
+    const int rT = ny - y0 + 2;
+    if (rT < kH0) U0[rT * kS + t] = U0[(rT - 2) * kS + t];
+  }
+  const int qx = t & 15, ty = t >> 4;
+  const int gi0 = x0 + 4 * qx, gj = y0 + ty;
+  const bool quad_ok = gi0 < nx && gj < ny;
+  const float4 v4 = *reinterpret_cast<const float4 *>(Vs + (ty + 1) * kVW + 4 * qx + 4);
+  const float4 w4 = *reinterpret_cast<const float4 *>(Ws + (ty + 1) * kVW + 4 * qx + 4);
+  const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+  const float ww[4] = {w4.x, w4.y, w4.z, w4.w};
+  const uint32_t code4 =
+      holes ? *reinterpret_cast<const uint32_t *>(Cs + (ty + 1) * kCW + 4 * qx + 16)
+            : 0x01010101u;
+  int rr = 0, rc = 0;
+  if (t < kW1) {
+    rr = 0; rc = t;
+  } else if (t < 2 * kW1) {
+    rr = kH1 - 1; rc = t - kW1;
+  } else if (t < 2 * kW1 + kTH) {
+    rr = 1 + t - 2 * kW1; rc = 0;
+  } else {
+    rr = 1 + t - 2 * kW1 - kTH; rc = kW1 - 1;
+  }
+  const int rgi = x0 - 1 + rc, rgj = y0 - 1 + rr;
+  const bool ring_ok = t < kRing && rgi >= 0 && rgi < nx && rgj >= 0 && rgj < ny;
+  const float rv = ring_ok ? Vs[rr * kVW + rc + 3] : 0.f;
+  const float rw = ring_ok ? Ws[rr * kVW + rc + 3] : 0.f;
+  const uint32_t rcode = (holes && ring_ok) ? Cs[rr * kCW + rc + 15] : 1u;
+  __syncthreads();
+  Fld<float> o;
+  o.f[0] = out.f[0] + I.off;
+  o.f[1] = out.f[1] + I.off;
+  o.f[2] = out.f[2] + I.off;
+  const EventHook hook{&I, gs + 1, x0, y0, nx, ny, t};
+  if (holes)
+    two_steps<true>(a, o, U0, U1, x0, y0, t, qx, ty, gi0, gj, quad_ok, vv, ww,
+                    code4, rr, rc, ring_ok, rv, rw, rcode, hook);
+  else
+    two_steps<false>(a, o, U0, U1, x0, y0, t, qx, ty, gi0, gj, quad_ok, vv,
+                     ww, code4, rr, rc, ring_ok, rv, rw, rcode, hook);
+}
+
 __global__ void batch_set_base(int *base, int value) { *base = value; }
 
 inline int st(cudaError_t e) {
@@ -171,6 +320,14 @@ struct yh_batch {
   cudaEvent_t fork = nullptr;
   std::vector<cudaGraphExec_t> graphs;  // [group][starting level]
   std::vector<int> order;        // instances, largest first
+  // depth 2: two steps per launch, 64 x 16 tiles staged by TMA
+  int depth = 1;
+  bool tma2 = false;             // every instance's tensor maps encoded
+  BatchMaps *d_maps = nullptr;   // [instance]
+  int2 *d_units2 = nullptr;
+  std::vector<int> ubeg2, uend2;
+  std::vector<cudaGraphExec_t> graphs2;  // [group][starting level]
+  int *d_err = nullptr;          // set when a TMA wait gave up
 };
 
 namespace {
@@ -228,6 +385,47 @@ int graph_for(yh_batch *b, int g, int lvl, cudaStream_t s,
   return YH_OK;
 }
 
+// Depth 2: steps di and di + 1 (from the group's base) of group g from
+// level lvl into level lvl ^ 1.
+cudaError_t launch_step2(yh_batch *b, int g, int lvl, int di, cudaStream_t s) {
+  return launch_pdl(rd_batch_2s_kernel, dim3(b->uend2[g] - b->ubeg2[g]),
+                    dim3(tile2s::kThreads), 0, s, (const BatchInst *)b->d_inst,
+                    (const BatchMaps *)b->d_maps,
+                    (const int2 *)(b->d_units2 + b->ubeg2[g]), lvl,
+                    level(b, lvl ^ 1), (const int *)(b->d_base + g), di,
+                    b->d_err);
+}
+
+// Graph of kBatchGraphSteps steps of group g at depth 2 (launch k: steps
+// 2k, 2k + 1 from level lvl ^ (k & 1)); it ends on lvl again.
+int graph_for2(yh_batch *b, int g, int lvl, cudaStream_t s,
+               cudaGraphExec_t *out) {
+  cudaGraphExec_t &slot = b->graphs2[2 * g + lvl];
+  if (slot) {
+    *out = slot;
+    return YH_OK;
+  }
+  cudaGraph_t gr = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return st(e);
+  cudaError_t eb = cudaSuccess;
+  for (int k = 0; k < kBatchGraphSteps / 2 && eb == cudaSuccess; ++k)
+    eb = launch_step2(b, g, lvl ^ (k & 1), 2 * k, s);
+  e = cudaStreamEndCapture(s, &gr);
+  if (eb != cudaSuccess || e != cudaSuccess) {
+    if (gr) cudaGraphDestroy(gr);
+    return st(eb != cudaSuccess ? eb : e);
+  }
+  e = cudaGraphInstantiate(&slot, gr, 0);
+  cudaGraphDestroy(gr);
+  if (e != cudaSuccess) {
+    slot = nullptr;
+    return st(e);
+  }
+  *out = slot;
+  return YH_OK;
+}
+
 // `len` steps of every group from b->step with the events currently in the
 // records; groups run on the internal streams, forked from and joined to
 // the caller's stream.
@@ -237,6 +435,50 @@ int run_segment(yh_batch *b, int len) {
     e = cudaStreamWaitEvent(b->streams[q], b->fork, 0);
   if (e != cudaSuccess) return st(e);
   const int ngroups = (int)b->ubeg.size();
+  if (b->depth == 2) {
+    int end_lvl = b->cur;
+    for (int g = 0; g < ngroups; ++g) {
+      cudaStream_t s = b->streams[g % b->nstreams];
+      int lvl = b->cur, step = b->step, left = len;
+      while (left >= kBatchGraphSteps) {
+        cudaGraphExec_t ex = nullptr;
+        int rc = graph_for2(b, g, lvl, s, &ex);
+        if (rc) return rc;
+        batch_set_base<<<1, 1, 0, s>>>(b->d_base + g, step);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaGraphLaunch(ex, s);
+        if (e != cudaSuccess) return st(e);
+        b->launches += kBatchGraphSteps / 2;
+        step += kBatchGraphSteps;
+        left -= kBatchGraphSteps;
+      }
+      if (left > 0) {
+        batch_set_base<<<1, 1, 0, s>>>(b->d_base + g, step);
+        e = cudaGetLastError();
+        int di = 0;
+        for (; left >= 2 && e == cudaSuccess; left -= 2, di += 2) {
+          e = launch_step2(b, g, lvl, di, s);
+          lvl ^= 1;
+          b->launches += 1;
+        }
+        if (left == 1 && e == cudaSuccess) {
+          e = launch_step(b, g, lvl, di, s);
+          lvl ^= 1;
+          b->launches += 1;
+        }
+        if (e != cudaSuccess) return st(e);
+      }
+      end_lvl = lvl;
+    }
+    for (int q = 0; q < b->nstreams && e == cudaSuccess; ++q) {
+      e = cudaEventRecord(b->joins[q], b->streams[q]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(b->s, b->joins[q], 0);
+    }
+    if (e != cudaSuccess) return st(e);
+    b->cur = end_lvl;
+    b->step += len;
+    return YH_OK;
+  }
   for (int g = 0; g < ngroups; ++g) {
     cudaStream_t s = b->streams[g % b->nstreams];
     int lvl = b->cur, step = b->step, left = len;
@@ -281,6 +523,9 @@ int plan_schedule(yh_batch *b, long long group_cells, int nstreams) {
   for (auto &gx : b->graphs)
     if (gx) cudaGraphExecDestroy(gx);
   b->graphs.clear();
+  for (auto &gx : b->graphs2)
+    if (gx) cudaGraphExecDestroy(gx);
+  b->graphs2.clear();
   for (cudaStream_t q : b->streams) cudaStreamDestroy(q);
   for (cudaEvent_t v : b->joins) cudaEventDestroy(v);
   b->streams.clear();
@@ -290,12 +535,23 @@ int plan_schedule(yh_batch *b, long long group_cells, int nstreams) {
   std::vector<int2> units;
   b->ubeg.clear();
   b->uend.clear();
+  b->ubeg2.clear();
+  b->uend2.clear();
+  std::vector<int2> units2;  // depth 2: 64 x 16 tiles
   long long acc = group_cells;  // start a group at the first instance
   for (int k : b->order) {
     if (acc >= group_cells) {
       if (!b->ubeg.empty()) b->uend.push_back((int)units.size());
       b->ubeg.push_back((int)units.size());
+      if (!b->ubeg2.empty()) b->uend2.push_back((int)units2.size());
+      b->ubeg2.push_back((int)units2.size());
       acc = 0;
+    }
+    {
+      const int tx2 = (b->inst[k].a.nx + tile2s::kTW - 1) / tile2s::kTW;
+      const int ty2 = (b->inst[k].a.ny + tile2s::kTH - 1) / tile2s::kTH;
+      for (int y = 0; y < ty2; ++y)
+        for (int x = 0; x < tx2; ++x) units2.push_back(make_int2(k, (y << 16) | x));
     }
     const int tx = (b->inst[k].a.nx / 4 + kTileQ - 1) / kTileQ;
     const int ty = (b->inst[k].a.ny + kTileR - 1) / kTileR;
@@ -304,11 +560,20 @@ int plan_schedule(yh_batch *b, long long group_cells, int nstreams) {
     acc += (long long)b->cells[k];
   }
   b->uend.push_back((int)units.size());
+  b->uend2.push_back((int)units2.size());
   b->nunits = (int)units.size();
   const int ngroups = (int)b->ubeg.size();
   b->graphs.assign(2 * ngroups, nullptr);
+  b->graphs2.assign(2 * ngroups, nullptr);
   cudaFree(b->d_units);
   b->d_units = nullptr;
+  cudaFree(b->d_units2);
+  b->d_units2 = nullptr;
+  e = cudaMalloc(&b->d_units2, units2.size() * sizeof(int2));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_units2, units2.data(), units2.size() * sizeof(int2),
+                        cudaMemcpyHostToDevice, b->s);
+  if (e != cudaSuccess) return st(e);
   cudaFree(b->d_base);
   b->d_base = nullptr;
   e = cudaMalloc(&b->d_units, units.size() * sizeof(int2));
@@ -363,6 +628,8 @@ extern "C" int yh_batch_destroy(yh_batch *b) {
   for (cudaStream_t q : b->streams) cudaStreamSynchronize(q);
   for (auto &g : b->graphs)
     if (g) cudaGraphExecDestroy(g);
+  for (auto &g : b->graphs2)
+    if (g) cudaGraphExecDestroy(g);
   for (cudaStream_t q : b->streams) cudaStreamDestroy(q);
   for (cudaEvent_t v : b->joins) cudaEventDestroy(v);
   if (b->fork) cudaEventDestroy(b->fork);
@@ -372,6 +639,9 @@ extern "C" int yh_batch_destroy(yh_batch *b) {
   cudaFree(b->d_inst);
   cudaFreeHost(b->h_stage);
   cudaFree(b->d_units);
+  cudaFree(b->d_units2);
+  cudaFree(b->d_maps);
+  cudaFree(b->d_err);
   cudaFree(b->d_base);
   if (b->own_stream && b->s) cudaStreamDestroy(b->s);
   delete b;
@@ -441,6 +711,42 @@ extern "C" int yh_batch_create(int count, const yh_param_var *params,
   if (e == cudaSuccess) e = cudaMalloc(&b->d_inst, count * sizeof(BatchInst));
   if (e == cudaSuccess) e = cudaMallocHost(&b->h_stage, count * sizeof(BatchInst));
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_err, 0, sizeof(int), b->s);
+  // depth 2: every instance's tensor maps (rows of 16-byte multiples; the
+  // hole codes need nx % 16)
+  if (e == cudaSuccess) {
+    std::vector<BatchMaps> maps(count);
+    bool ok = tile2s::encode_tiled() != nullptr;
+    for (int k = 0; k < count && ok; ++k) {
+      const int nx = params[k].nx, ny = params[k].ny;
+      const long long off = b->inst[k].off;
+      BatchMaps &m = maps[k];
+      for (int l = 0; l < 2 && ok; ++l) {
+        const Fld<float> f = level(b, l);
+        ok = tile2s::encode_2d(&m.u[l], f.f[0] + off, false, nx, ny, tile2s::kS,
+                               tile2s::kH0) &&
+             tile2s::encode_2d(&m.v[l], f.f[1] + off, false, nx, ny,
+                               tile2s::kVW, tile2s::kVH) &&
+             tile2s::encode_2d(&m.w[l], f.f[2] + off, false, nx, ny,
+                               tile2s::kVW, tile2s::kVH);
+      }
+      if (ok && b->inst[k].holes)
+        ok = nx % 16 == 0 &&
+             tile2s::encode_2d(&m.c, b->codes + off, true, nx, ny, tile2s::kCW,
+                               tile2s::kVH);
+      else
+        m.c = m.u[0];
+    }
+    b->tma2 = ok;
+    if (ok) {
+      e = cudaMalloc(&b->d_maps, count * sizeof(BatchMaps));
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->d_maps, maps.data(), count * sizeof(BatchMaps),
+                            cudaMemcpyHostToDevice, b->s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(b->s);  // maps is local
+    }
+  }
   int rc = st(e);
   if (rc == YH_OK) rc = plan_schedule(b, kBatchGroupCells, kBatchStreams);
   if (rc == YH_OK) rc = upload_records(b);
@@ -455,7 +761,21 @@ extern "C" int yh_batch_create(int count, const yh_param_var *params,
 
 extern "C" int yh_batch_synchronize(yh_batch *b) {
   if (!b) return YH_EINVAL;
-  return st(cudaStreamSynchronize(b->s));
+  cudaError_t e = cudaStreamSynchronize(b->s);
+  int err = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return st(e);
+  return err ? YH_ETIMEOUT : YH_OK;
+}
+
+extern "C" int yh_batch_set_depth(yh_batch *b, int depth) {
+  if (!b || (depth != 1 && depth != 2)) return YH_EINVAL;
+  if (depth == 2 && !b->tma2) return YH_EUNSUPPORTED;
+  const cudaError_t e = cudaStreamSynchronize(b->s);
+  if (e != cudaSuccess) return st(e);
+  b->depth = depth;
+  return YH_OK;
 }
 
 extern "C" int yh_batch_set_state(yh_batch *b, int k, const float *u,
@@ -552,7 +872,8 @@ extern "C" int yh_batch_run(yh_batch *b, int nsteps, const yh_batch_stim *stims,
 }
 
 extern "C" int yh_batch_autotune(yh_batch *b, int probe_steps,
-                                 long long *group_cells, int *streams) {
+                                 long long *group_cells, int *streams,
+                                 int *depth) {
   if (!b || probe_steps < 2) return YH_EINVAL;
   probe_steps += probe_steps & 1;  // even: the state ends on its level
   const size_t bytes = (size_t)3 * b->total * sizeof(float);
@@ -575,11 +896,13 @@ extern "C" int yh_batch_autotune(yh_batch *b, int probe_steps,
   const long long sizes[] = {1 << 18, 1 << 19, 1 << 20, 1 << 21};
   const int counts[] = {2, 3, 4};
   long long best_g = kBatchGroupCells;
-  int best_s = kBatchStreams, rc = st(e);
+  int best_s = kBatchStreams, best_d = 1, rc = st(e);
   float best_ms = 3.4e38f;
+  for (int d = 1; d <= (b->tma2 ? 2 : 1); ++d)
   for (long long g : sizes)
     for (int q : counts) {
       if (rc) break;
+      b->depth = d;
       rc = plan_schedule(b, g, q);
       // the first run captures the groups' graphs; the second is timed
       if (!rc) rc = yh_batch_run(b, probe_steps, nullptr, 0);
@@ -595,8 +918,10 @@ extern "C" int yh_batch_autotune(yh_batch *b, int probe_steps,
         best_ms = ms;
         best_g = g;
         best_s = q;
+        best_d = d;
       }
     }
+  b->depth = best_d;
   if (!rc) rc = plan_schedule(b, best_g, best_s);
   if (!rc) rc = st(restore());
   if (!rc) rc = st(cudaStreamSynchronize(b->s));
@@ -607,6 +932,7 @@ extern "C" int yh_batch_autotune(yh_batch *b, int probe_steps,
   if (rc) return rc;
   if (group_cells) *group_cells = best_g;
   if (streams) *streams = best_s;
+  if (depth) *depth = best_d;
   return YH_OK;
 }
 
