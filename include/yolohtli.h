@@ -50,8 +50,10 @@ enum {
   YH_EUNSUPPORTED = -7,  /* option off this path: RK2/RK4, lap4, anisotropy,
                             Dirichlet boundaries                             */
   YH_ENOTREADY = -8,     /* call order (e.g. yh_sr_step before yh_sr_begin)  */
-  YH_ETIMEOUT = -9       /* a bounded device-side wait gave up (resident
+  YH_ETIMEOUT = -9,      /* a bounded device-side wait gave up (resident
                             solver); the state is not valid                  */
+  YH_ECORRUPT = -10      /* checkpoint file: bad magic, version, byte order,
+                            sizes or checksum, or a short file               */
 };
 
 enum { YH_MODEL_REF2V = 0,   /* the reference's 2-variable cubic model
@@ -433,12 +435,30 @@ int yh_sr_begin(yh_solver *h, int template_mode, const float *tu,
 int yh_sr_step(yh_solver *h, int nsteps);
 int yh_get_sym(yh_solver *h, yh_sym_state *out);
 
-/* Steps taken so far. */
+/* Steps taken so far, the clock that stimulus events are matched against.
+ * yh_set_step moves that clock (step >= 0) and leaves the state as it is. */
 int yh_get_step(yh_solver *h, int *step);
+int yh_set_step(yh_solver *h, int step);
 
 /* Kernel launches this handle has performed so far (graph replays count
  * every kernel node they run). */
 int yh_get_launch_count(yh_solver *h, long long *n);
+
+/* Counts the state values (every field, every cell) that are NaN or Inf, in
+ * one launch; *bad_values (may be NULL) gets the count. YH_ENONFINITE when
+ * it is not zero. */
+int yh_check_finite(yh_solver *h, long long *bad_values);
+
+/* Checkpoint and resume of a plain run (the file format is under layer 4).
+ * Save writes the state, the step count, the parameters and the mask.
+ * Load restores the state and the step count into a handle created for the
+ * same problem. It returns YH_EINVAL when the file's grid, model, step
+ * coefficients (rx, ry, rscale, dt, tc, gateDiff, the REF2V constants),
+ * FK3V parameters or mask differ from the handle's. Neither the previous
+ * time level (tip tracking) nor a symmetry-reduction state is part of a
+ * checkpoint: a symmetry-reduced run resumes with a new yh_sr_begin. */
+int yh_save_checkpoint(yh_solver *h, const char *path);
+int yh_load_checkpoint(yh_solver *h, const char *path);
 
 /* tipAlgorithm 3 (abouzarTip_kernel / abubuFilament,
  * tipTracker.cu:434-517): marks (sets to 1, never clears) the cells whose
@@ -627,6 +647,46 @@ int yh_write_tips(const char *tip_path, const char *size_path,
  * n x 3 (printSym, printFunctions.cu:249-264). */
 int yh_write_sym_list(const char *path, const double *c, const double *phi,
                       int n);
+
+/* This library's own binary checkpoint. The reference's only state file,
+ * raw_data.dat, keeps 6 decimals, and its reload path is dead. Host code,
+ * no GPU. All integers are little-endian. Layout:
+ *   a 64-byte header:
+ *     bytes 0-7    magic "YHCKPT\0\0"
+ *     8-11         format version, uint32 (1)
+ *     12-15        byte-order mark, uint32 0x01020304
+ *     16-35        nx, ny, model, nfields, mask flag, int32 each
+ *     36-39        sizeof(yh_param_var), int32
+ *     40-47        step, int64
+ *     48-55        payload bytes, uint64
+ *     56-63        FNV-1a 64-bit hash of the payload, uint64
+ *   the payload:
+ *     the yh_param_var, the yh_fk_params, the mask (nx*ny bytes, only when
+ *     the flag is 1; nonzero = tissue), then nfields float32 arrays of nx*ny
+ *     cells (u, v and, for FK3V, w).
+ * Every function returns YH_EINVAL for an argument error or an open or write
+ * error, and YH_ECORRUPT for a file that fails a check of the format, its
+ * sizes or its hash. */
+typedef struct yh_checkpoint_header {
+  int nx, ny, model, nfields, has_mask;
+  long long step;
+} yh_checkpoint_header;
+
+/* mask may be NULL: no mask is stored. w is ignored for REF2V. */
+int yh_write_checkpoint(const char *path, const yh_param_var *p, int model,
+                        const yh_fk_params *fk, const uint8_t *mask,
+                        long long step, const float *u, const float *v,
+                        const float *w);
+/* Reads and checks only the header: the sizes the caller needs before
+ * yh_read_checkpoint. */
+int yh_read_checkpoint_header(const char *path, yh_checkpoint_header *out);
+/* Reads the whole file and checks its hash. Any output may be NULL to skip
+ * it. The arrays hold nx*ny elements, as the header gives. The mask is set
+ * to 1 (all tissue) when the file holds none. On an error the outputs hold
+ * whatever had been read. */
+int yh_read_checkpoint(const char *path, yh_param_var *p, int *model,
+                       yh_fk_params *fk, uint8_t *mask, long long *step,
+                       float *u, float *v, float *w);
 
 #ifdef __cplusplus
 }

@@ -56,7 +56,9 @@ def test_struct_sizes_match_ctypes():
     lib = load()
     for name, ct in [("yh_param_var", A.ParamVar), ("yh_fk_params", A.FKParams),
                      ("yh_tip", A.Tip), ("yh_fields", A.Fields),
-                     ("yh_sym_state", A.SymState), ("yh_stim", A.Stim)]:
+                     ("yh_sym_state", A.SymState), ("yh_stim", A.Stim),
+                     ("yh_batch_stim", A.BatchStim),
+                     ("yh_checkpoint_header", A.CheckpointHeader)]:
         assert lib.yh_sizeof(name.encode()) == C.sizeof(ct), name
 
 

@@ -16,13 +16,14 @@ YH_EOVERFLOW = -6
 YH_EUNSUPPORTED = -7
 YH_ENOTREADY = -8
 YH_ETIMEOUT = -9
+YH_ECORRUPT = -10
 
 STATUS_NAMES = {
     YH_OK: "YH_OK", YH_EINVAL: "YH_EINVAL", YH_ECUDA: "YH_ECUDA",
     YH_ENOMEM: "YH_ENOMEM", YH_ESINGULAR: "YH_ESINGULAR",
     YH_ENONFINITE: "YH_ENONFINITE", YH_EOVERFLOW: "YH_EOVERFLOW",
     YH_EUNSUPPORTED: "YH_EUNSUPPORTED", YH_ENOTREADY: "YH_ENOTREADY",
-    YH_ETIMEOUT: "YH_ETIMEOUT",
+    YH_ETIMEOUT: "YH_ETIMEOUT", YH_ECORRUPT: "YH_ECORRUPT",
 }
 
 YH_ENGINE_STEP = 0
@@ -163,6 +164,13 @@ class ApdFields(C.Structure):
 class BatchStim(C.Structure):
     """yh_batch_stim: a stimulus event of one instance of a batch."""
     _fields_ = [("instance", C.c_int), ("s", Stim)]
+
+
+class CheckpointHeader(C.Structure):
+    """yh_checkpoint_header: the sizes a checkpoint file holds."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("model", C.c_int),
+                ("nfields", C.c_int), ("has_mask", C.c_int),
+                ("step", C.c_longlong)]
 
 
 def param_defaults(nx, ny):

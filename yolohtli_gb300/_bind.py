@@ -64,7 +64,11 @@ SIGNATURES = {
     "yh_sr_step": (_i, [_v, _i]),
     "yh_get_sym": (_i, [_v, _P(A.SymState)]),
     "yh_get_step": (_i, [_v, _P(_i)]),
+    "yh_set_step": (_i, [_v, _i]),
     "yh_get_launch_count": (_i, [_v, _P(C.c_longlong)]),
+    "yh_check_finite": (_i, [_v, _P(C.c_longlong)]),
+    "yh_save_checkpoint": (_i, [_v, C.c_char_p]),
+    "yh_load_checkpoint": (_i, [_v, C.c_char_p]),
     # batched solver
     "yh_batch_create": (_i, [_i, _P(A.ParamVar), _P(A.FKParams), _P(_v), _v,
                              _P(_v)]),
@@ -102,6 +106,14 @@ SIGNATURES = {
     "yh_write_raw_window": (_i, [C.c_char_p, _P(A.ParamVar), _v, _v]),
     "yh_write_tips": (_i, [C.c_char_p, C.c_char_p, _P(A.Tip), _i, _i]),
     "yh_write_sym_list": (_i, [C.c_char_p, _v, _v, _i]),
+    # this library's binary checkpoint
+    "yh_write_checkpoint": (_i, [C.c_char_p, _P(A.ParamVar), _i,
+                                 _P(A.FKParams), _v, C.c_longlong, _v, _v,
+                                 _v]),
+    "yh_read_checkpoint_header": (_i, [C.c_char_p, _P(A.CheckpointHeader)]),
+    "yh_read_checkpoint": (_i, [C.c_char_p, _P(A.ParamVar), _P(_i),
+                                _P(A.FKParams), _v, _P(C.c_longlong), _v, _v,
+                                _v]),
 }
 
 

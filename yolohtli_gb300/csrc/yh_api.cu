@@ -219,6 +219,8 @@ extern "C" const char *yh_status_string(int s) {
     case YH_EOVERFLOW: return "tip buffer overflow";
     case YH_EUNSUPPORTED: return "option not supported on this path";
     case YH_ENOTREADY: return "call order";
+    case YH_ETIMEOUT: return "device-side wait timed out";
+    case YH_ECORRUPT: return "corrupt checkpoint file";
   }
   return "unknown status";
 }
@@ -233,6 +235,9 @@ extern "C" size_t yh_sizeof(const char *type_name) {
   if (!strcmp(type_name, "yh_fields")) return sizeof(yh_fields);
   if (!strcmp(type_name, "yh_sym_state")) return sizeof(yh_sym_state);
   if (!strcmp(type_name, "yh_stim")) return sizeof(yh_stim);
+  if (!strcmp(type_name, "yh_batch_stim")) return sizeof(yh_batch_stim);
+  if (!strcmp(type_name, "yh_checkpoint_header"))
+    return sizeof(yh_checkpoint_header);
   return 0;
 }
 

@@ -350,3 +350,219 @@ extern "C" int yh_write_sym_list(const char *path, const double *c,
   fclose(o);
   return bad ? YH_EINVAL : YH_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Binary checkpoint (this library's format; the header file gives the byte
+// layout). The header is packed field by field at fixed offsets, so struct
+// padding never reaches the file; the payload is streamed through a 1 MiB
+// buffer with its FNV-1a 64-bit hash computed on the way.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr char kMagic[8] = {'Y', 'H', 'C', 'K', 'P', 'T', 0, 0};
+constexpr uint32_t kVersion = 1;
+constexpr uint32_t kByteOrder = 0x01020304u;
+constexpr size_t kHeaderBytes = 64;
+constexpr size_t kChunk = 1 << 20;
+
+struct Fnv1a64 {  // FNV-1a, 64-bit offset basis and prime
+  uint64_t h = 0xcbf29ce484222325ull;
+  void add(const void *data, size_t n) {
+    const uint8_t *b = (const uint8_t *)data;
+    for (size_t k = 0; k < n; ++k) {
+      h ^= b[k];
+      h *= 0x100000001b3ull;
+    }
+  }
+};
+
+struct Header {
+  int32_t nx, ny, model, nfields, has_mask, param_bytes;
+  int64_t step;
+  uint64_t payload, hash;
+};
+
+inline int nfields_of(int model) { return model == YH_MODEL_FK3V ? 3 : 2; }
+
+inline uint64_t payload_bytes(int nx, int ny, int nf, int has_mask) {
+  const uint64_t n = (uint64_t)nx * (uint64_t)ny;
+  return sizeof(yh_param_var) + sizeof(yh_fk_params) +
+         (has_mask ? n : 0) + (uint64_t)nf * n * sizeof(float);
+}
+
+template <typename T>
+inline void put(uint8_t *b, size_t off, T x) { memcpy(b + off, &x, sizeof(T)); }
+template <typename T>
+inline T get(const uint8_t *b, size_t off) {
+  T x;
+  memcpy(&x, b + off, sizeof(T));
+  return x;
+}
+
+void pack(const Header &h, uint8_t *b) {
+  memset(b, 0, kHeaderBytes);
+  memcpy(b, kMagic, 8);
+  put<uint32_t>(b, 8, kVersion);
+  put<uint32_t>(b, 12, kByteOrder);
+  put<int32_t>(b, 16, h.nx);
+  put<int32_t>(b, 20, h.ny);
+  put<int32_t>(b, 24, h.model);
+  put<int32_t>(b, 28, h.nfields);
+  put<int32_t>(b, 32, h.has_mask);
+  put<int32_t>(b, 36, h.param_bytes);
+  put<int64_t>(b, 40, h.step);
+  put<uint64_t>(b, 48, h.payload);
+  put<uint64_t>(b, 56, h.hash);
+}
+
+// YH_ECORRUPT unless every header field is one this library writes.
+int unpack(const uint8_t *b, Header *h) {
+  if (memcmp(b, kMagic, 8) != 0) return YH_ECORRUPT;
+  if (get<uint32_t>(b, 8) != kVersion) return YH_ECORRUPT;
+  if (get<uint32_t>(b, 12) != kByteOrder) return YH_ECORRUPT;
+  h->nx = get<int32_t>(b, 16);
+  h->ny = get<int32_t>(b, 20);
+  h->model = get<int32_t>(b, 24);
+  h->nfields = get<int32_t>(b, 28);
+  h->has_mask = get<int32_t>(b, 32);
+  h->param_bytes = get<int32_t>(b, 36);
+  h->step = get<int64_t>(b, 40);
+  h->payload = get<uint64_t>(b, 48);
+  h->hash = get<uint64_t>(b, 56);
+  if (h->nx < 1 || h->ny < 1 ||
+      (int64_t)h->nx * h->ny > (int64_t)(1LL << 31) - 1)
+    return YH_ECORRUPT;
+  if (h->model != YH_MODEL_REF2V && h->model != YH_MODEL_FK3V)
+    return YH_ECORRUPT;
+  if (h->nfields != nfields_of(h->model)) return YH_ECORRUPT;
+  if (h->has_mask != 0 && h->has_mask != 1) return YH_ECORRUPT;
+  if (h->param_bytes != (int32_t)sizeof(yh_param_var)) return YH_ECORRUPT;
+  if (h->step < 0) return YH_ECORRUPT;
+  if (h->payload != payload_bytes(h->nx, h->ny, h->nfields, h->has_mask))
+    return YH_ECORRUPT;
+  return YH_OK;
+}
+
+// Opens path and reads and checks its header; *in is open on success.
+int open_checkpoint(const char *path, FILE **in, Header *h) {
+  *in = fopen(path, "rb");
+  if (!*in) return YH_EINVAL;
+  uint8_t b[kHeaderBytes];
+  int rc = fread(b, 1, kHeaderBytes, *in) == kHeaderBytes ? unpack(b, h)
+                                                          : YH_ECORRUPT;
+  if (rc) {
+    fclose(*in);
+    *in = nullptr;
+  }
+  return rc;
+}
+
+// Reads n payload bytes into dst (NULL: read and hash, keep nothing).
+bool read_hashed(FILE *in, void *dst, uint64_t n, Fnv1a64 *hash,
+                 std::vector<uint8_t> *buf) {
+  uint8_t *d = (uint8_t *)dst;
+  while (n > 0) {
+    const size_t m = (size_t)(n < kChunk ? n : kChunk);
+    uint8_t *to = d ? d : buf->data();
+    if (fread(to, 1, m, in) != m) return false;
+    hash->add(to, m);
+    if (d) d += m;
+    n -= m;
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" int yh_write_checkpoint(const char *path, const yh_param_var *p,
+                                   int model, const yh_fk_params *fk,
+                                   const uint8_t *mask, long long step,
+                                   const float *u, const float *v,
+                                   const float *w) {
+  if (!path || !p || !u || !v || step < 0) return YH_EINVAL;
+  if (model != YH_MODEL_REF2V && model != YH_MODEL_FK3V) return YH_EINVAL;
+  if (model == YH_MODEL_FK3V && (!fk || !w)) return YH_EINVAL;
+  if (p->nx < 1 || p->ny < 1 ||
+      (long long)p->nx * p->ny > (1LL << 31) - 1)
+    return YH_EINVAL;
+  Header h;
+  h.nx = p->nx;
+  h.ny = p->ny;
+  h.model = model;
+  h.nfields = nfields_of(model);
+  h.has_mask = mask ? 1 : 0;
+  h.param_bytes = (int32_t)sizeof(yh_param_var);
+  h.step = step;
+  h.payload = payload_bytes(h.nx, h.ny, h.nfields, h.has_mask);
+  yh_fk_params fk0;
+  memset(&fk0, 0, sizeof(fk0));
+  if (fk) fk0 = *fk;
+  const size_t n = (size_t)h.nx * h.ny;
+  struct Part { const void *data; size_t bytes; };
+  const Part parts[6] = {{p, sizeof(yh_param_var)},
+                         {&fk0, sizeof(fk0)},
+                         {mask, mask ? n : 0},
+                         {u, n * sizeof(float)},
+                         {v, n * sizeof(float)},
+                         {w, h.nfields > 2 ? n * sizeof(float) : 0}};
+  Fnv1a64 hash;
+  for (const Part &q : parts) hash.add(q.data, q.bytes);
+  h.hash = hash.h;
+  uint8_t b[kHeaderBytes];
+  pack(h, b);
+  FILE *o = fopen(path, "wb");
+  if (!o) return YH_EINVAL;
+  bool ok = fwrite(b, 1, kHeaderBytes, o) == kHeaderBytes;
+  for (const Part &q : parts)
+    if (ok && q.bytes) ok = fwrite(q.data, 1, q.bytes, o) == q.bytes;
+  ok = (fclose(o) == 0) && ok;
+  return ok ? YH_OK : YH_EINVAL;
+}
+
+extern "C" int yh_read_checkpoint_header(const char *path,
+                                         yh_checkpoint_header *out) {
+  if (!path || !out) return YH_EINVAL;
+  FILE *in;
+  Header h;
+  const int rc = open_checkpoint(path, &in, &h);
+  if (rc) return rc;
+  fclose(in);
+  out->nx = h.nx;
+  out->ny = h.ny;
+  out->model = h.model;
+  out->nfields = h.nfields;
+  out->has_mask = h.has_mask;
+  out->step = h.step;
+  return YH_OK;
+}
+
+extern "C" int yh_read_checkpoint(const char *path, yh_param_var *p,
+                                  int *model, yh_fk_params *fk, uint8_t *mask,
+                                  long long *step, float *u, float *v,
+                                  float *w) {
+  if (!path) return YH_EINVAL;
+  FILE *in;
+  Header h;
+  int rc = open_checkpoint(path, &in, &h);
+  if (rc) return rc;
+  std::vector<uint8_t> buf(kChunk);
+  yh_param_var pv;
+  const size_t n = (size_t)h.nx * h.ny;
+  Fnv1a64 hash;
+  bool ok = read_hashed(in, &pv, sizeof(pv), &hash, &buf) &&
+            read_hashed(in, fk, sizeof(yh_fk_params), &hash, &buf) &&
+            (!h.has_mask || read_hashed(in, mask, n, &hash, &buf)) &&
+            read_hashed(in, u, n * sizeof(float), &hash, &buf) &&
+            read_hashed(in, v, n * sizeof(float), &hash, &buf) &&
+            (h.nfields < 3 || read_hashed(in, w, n * sizeof(float), &hash, &buf));
+  // nothing may follow the payload
+  ok = ok && fgetc(in) == EOF;
+  fclose(in);
+  if (!ok || hash.h != h.hash || pv.nx != h.nx || pv.ny != h.ny)
+    return YH_ECORRUPT;
+  if (p) *p = pv;
+  if (model) *model = h.model;
+  if (step) *step = h.step;
+  if (mask && !h.has_mask) memset(mask, 1, n);
+  return YH_OK;
+}

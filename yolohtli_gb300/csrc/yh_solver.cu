@@ -68,6 +68,7 @@ struct yh_solver {
   ResidentPlan plan{};       // resident solver layout (plan.ok: usable)
   unsigned long long *res_halo = nullptr;  // tagged boundary rows
   int *res_error = nullptr;  // device flag set when a bounded wait gave up
+  unsigned long long *nonfinite = nullptr;  // yh_check_finite's count
   GraphCache plain[2];
   GraphCache sr[2];
 };
@@ -169,6 +170,7 @@ extern "C" int yh_destroy(yh_solver *h) {
   cudaFree(h->adv_f);
   cudaFree(h->res_halo);
   cudaFree(h->res_error);
+  cudaFree(h->nonfinite);
   if (h->own_stream) cudaStreamDestroy(h->s);
   delete h;
   return YH_OK;
@@ -228,6 +230,12 @@ extern "C" int yh_state_device(yh_solver *h, yh_fields *cur) {
 extern "C" int yh_get_step(yh_solver *h, int *step) {
   if (!h || !step) return YH_EINVAL;
   *step = h->step;
+  return YH_OK;
+}
+
+extern "C" int yh_set_step(yh_solver *h, int step) {
+  if (!h || step < 0) return YH_EINVAL;
+  h->step = step;
   return YH_OK;
 }
 
@@ -746,4 +754,121 @@ extern "C" int yh_get_sym(yh_solver *h, yh_sym_state *out) {
                                   cudaMemcpyDeviceToHost, h->s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
   return st(e);
+}
+
+// ---------------------------------------------------------------------------
+// Finite check and checkpoint / resume
+// ---------------------------------------------------------------------------
+
+// Counts the non-finite values of field blockIdx.y (exponent bits all ones:
+// Inf or NaN, IEEE 754 binary32), one atomic per warp that found any.
+__global__ void __launch_bounds__(256)
+    count_nonfinite_kernel(Fld<float> f, size_t n, unsigned long long *count) {
+  const unsigned *a = (const unsigned *)f.f[blockIdx.y];
+  unsigned c = 0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    c += (a[k] & 0x7f800000u) == 0x7f800000u;
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, (unsigned long long)c);
+}
+
+extern "C" int yh_check_finite(yh_solver *h, long long *bad_values) {
+  if (!h) return YH_EINVAL;
+  cudaError_t e = cudaSuccess;
+  if (!h->nonfinite) e = cudaMalloc(&h->nonfinite, sizeof(unsigned long long));
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(h->nonfinite, 0, sizeof(unsigned long long), h->s);
+  if (e != cudaSuccess) return st(e);
+  // 4 cells per thread, at most 8 blocks of 256 per SM of a 152-SM GB300
+  const size_t per_block = 256 * 4;
+  const size_t blocks = std::min<size_t>((h->n + per_block - 1) / per_block,
+                                         152 * 8);
+  count_nonfinite_kernel<<<dim3((unsigned)blocks, h->nf), 256, 0, h->s>>>(
+      h->cur, h->n, h->nonfinite);
+  h->launches += 1;
+  unsigned long long c = 0;
+  e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&c, h->nonfinite, sizeof(c), cudaMemcpyDeviceToHost,
+                        h->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  if (e != cudaSuccess) return st(e);
+  const int rc = resident_status(h);
+  if (rc) return rc;
+  if (bad_values) *bad_values = (long long)c;
+  return c ? YH_ENONFINITE : YH_OK;
+}
+
+// The handle's mask on the host (empty when it has none).
+static int host_mask(yh_solver *h, std::vector<uint8_t> *mask) {
+  mask->clear();
+  if (!h->solid) return YH_OK;
+  mask->resize(h->n);
+  cudaError_t e = cudaMemcpyAsync(mask->data(), h->solid, h->n,
+                                  cudaMemcpyDeviceToHost, h->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  return st(e);
+}
+
+extern "C" int yh_save_checkpoint(yh_solver *h, const char *path) {
+  if (!h || !path) return YH_EINVAL;
+  std::vector<float> u(h->n), v(h->n), w(h->nf > 2 ? h->n : 0);
+  std::vector<uint8_t> mask;
+  int rc = yh_get_state(h, u.data(), v.data(), h->nf > 2 ? w.data() : nullptr);
+  if (!rc) rc = host_mask(h, &mask);
+  if (rc) return rc;
+  return yh_write_checkpoint(path, &h->p, h->model,
+                             h->model == YH_MODEL_FK3V ? &h->fk : nullptr,
+                             mask.empty() ? nullptr : mask.data(), h->step,
+                             u.data(), v.data(),
+                             h->nf > 2 ? w.data() : nullptr);
+}
+
+// The parameters the step's coefficients are made of (make_step_coeffs).
+static bool same_step(const yh_param_var &a, const yh_param_var &b) {
+  return a.nx == b.nx && a.ny == b.ny && a.gateDiff == b.gateDiff &&
+         a.rx == b.rx && a.ry == b.ry && a.rscale == b.rscale &&
+         a.dt == b.dt && a.tc == b.tc && a.mu == b.mu && a.alpha == b.alpha &&
+         a.eps == b.eps && a.delta == b.delta && a.gamma == b.gamma &&
+         a.beta == b.beta && a.theta == b.theta;
+}
+
+static bool same_fk(const yh_fk_params &a, const yh_fk_params &b) {
+  return a.tau_d == b.tau_d && a.tau_r == b.tau_r && a.tau_si == b.tau_si &&
+         a.tau_0 == b.tau_0 && a.tau_v_plus == b.tau_v_plus &&
+         a.tau_v1_minus == b.tau_v1_minus && a.tau_v2_minus == b.tau_v2_minus &&
+         a.tau_w_plus == b.tau_w_plus && a.tau_w_minus == b.tau_w_minus &&
+         a.u_c == b.u_c && a.u_v == b.u_v && a.u_csi == b.u_csi && a.k == b.k;
+}
+
+extern "C" int yh_load_checkpoint(yh_solver *h, const char *path) {
+  if (!h || !path) return YH_EINVAL;
+  yh_checkpoint_header hd;
+  int rc = yh_read_checkpoint_header(path, &hd);
+  if (rc) return rc;
+  if (hd.nx != h->p.nx || hd.ny != h->p.ny || hd.model != h->model ||
+      hd.has_mask != (h->solid ? 1 : 0) || hd.step > 0x7fffffffLL)
+    return YH_EINVAL;
+  std::vector<float> u(h->n), v(h->n), w(h->nf > 2 ? h->n : 0);
+  std::vector<uint8_t> mask(hd.has_mask ? h->n : 0), mine;
+  yh_param_var p;
+  yh_fk_params fk;
+  int model = -1;
+  long long step = 0;
+  rc = yh_read_checkpoint(path, &p, &model, &fk,
+                          hd.has_mask ? mask.data() : nullptr, &step, u.data(),
+                          v.data(), h->nf > 2 ? w.data() : nullptr);
+  if (rc) return rc;
+  if (!same_step(p, h->p) || (h->model == YH_MODEL_FK3V && !same_fk(fk, h->fk)))
+    return YH_EINVAL;
+  rc = host_mask(h, &mine);
+  if (rc) return rc;
+  for (size_t k = 0; k < mine.size(); ++k)
+    if ((mine[k] != 0) != (mask[k] != 0)) return YH_EINVAL;
+  rc = yh_set_state(h, u.data(), v.data(), h->nf > 2 ? w.data() : nullptr);
+  if (!rc) rc = st(cudaStreamSynchronize(h->s));
+  if (rc) return rc;
+  h->step = (int)step;
+  return YH_OK;
 }

@@ -110,11 +110,60 @@ class Monodomain:
         check("yh_get_step", self.lib.yh_get_step(self.h, C.byref(s)))
         return s.value
 
+    def set_step(self, step):
+        check("yh_set_step", self.lib.yh_set_step(self.h, int(step)))
+
     def launch_count(self):
         n = C.c_longlong()
         check("yh_get_launch_count",
               self.lib.yh_get_launch_count(self.h, C.byref(n)))
         return n.value
+
+    def check_finite(self):
+        """The number of NaN or Inf values in the state (0: all finite)."""
+        n = C.c_longlong()
+        st = self.lib.yh_check_finite(self.h, C.byref(n))
+        if st not in (A.YH_OK, A.YH_ENONFINITE):
+            check("yh_check_finite", st)
+        return n.value
+
+    def save_checkpoint(self, path):
+        """State, step count, parameters and mask in this library's binary
+        checkpoint file (yolohtli_gb300.checkpoint)."""
+        check("yh_save_checkpoint",
+              self.lib.yh_save_checkpoint(self.h, str(path).encode()))
+
+    def load_checkpoint(self, path):
+        """Restores state and step count from a checkpoint of the same
+        problem (grid, model, step coefficients, FK3V parameters, mask)."""
+        check("yh_load_checkpoint",
+              self.lib.yh_load_checkpoint(self.h, str(path).encode()))
+
+    def run_checked(self, nsteps, stims=(), every=1000):
+        """run() in segments of `every` steps, each followed by
+        check_finite(). The state and step count after the last finite
+        segment are kept on the host. When a segment ends with a NaN or Inf
+        in the state, the handle is rolled back to them and YolohtliError
+        (YH_ENONFINITE) is raised. The explicit step is deterministic, so
+        running the same segment again fails again: the caller changes dt
+        or the state first. Returns the number of segments run."""
+        every = max(1, int(every))
+        good = (self.get_state(), self.step_count())
+        left, segments = int(nsteps), 0
+        while left > 0:
+            m = min(every, left)
+            self.run(m, stims)
+            segments += 1
+            if self.check_finite():
+                state, step = good
+                self.set_state(*state)
+                self.set_step(step)
+                self.synchronize()
+                check("yh_check_finite", A.YH_ENONFINITE)
+            left -= m
+            if left > 0:
+                good = (self.get_state(), self.step_count())
+        return segments
 
     def track_tips(self):
         check("yh_track_tips", self.lib.yh_track_tips(self.h))
