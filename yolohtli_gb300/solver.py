@@ -42,6 +42,10 @@ class Monodomain:
         self.h = h
 
     @property
+    def has_mask(self):
+        return self._solid is not None
+
+    @property
     def n(self):
         return self.p.nx * self.p.ny
 
