@@ -91,7 +91,7 @@ def test_logged_run_on_the_gpu(tmp_path):
     from yolohtli_gb300.solver import Monodomain
     wl = W.fk_spiral_256(n=128, nsteps=400)
     sim = Monodomain(wl.p, wl.model, wl.fk, solid=wl.solid)
-    sim.set_state(wl.u, wl.v, wl.w)
+    sim.set_state(*wl.state0())
     with runlog.RunLog(tmp_path / "run.jsonl") as log:
         lines = runlog.run_logged(sim, 400, log, stims=wl.stims, every=100,
                                   peak_gbs=6778.7)
@@ -99,7 +99,7 @@ def test_logged_run_on_the_gpu(tmp_path):
     assert all(r["nonfinite"] == 0 and r["gcell_steps_per_s"] > 0
                for r in lines)
     ref = Monodomain(wl.p, wl.model, wl.fk, solid=wl.solid)
-    ref.set_state(wl.u, wl.v, wl.w)
+    ref.set_state(*wl.state0())
     ref.run(400, wl.stims)
     for x, y in zip(sim.get_state(), ref.get_state()):
         assert x.tobytes() == y.tobytes()
