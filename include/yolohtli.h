@@ -546,6 +546,8 @@ int yh_batch_set_depth(yh_batch *b, int depth);
 int yh_batch_autotune(yh_batch *b, int probe_steps, long long *group_cells,
                       int *streams, int *depth);
 int yh_batch_get_step(yh_batch *b, int *step);
+/* Moves the batch's step clock (step >= 0); the states are unchanged. */
+int yh_batch_set_step(yh_batch *b, int step);
 int yh_batch_get_launch_count(yh_batch *b, long long *n);
 
 /* ------------------------------------------------------------------ */

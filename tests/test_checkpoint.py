@@ -166,3 +166,26 @@ def test_status_strings_of_the_failure_codes():
     assert lib.yh_status_string(A.YH_ETIMEOUT) == b"device-side wait timed out"
     assert lib.yh_status_string(A.YH_ECORRUPT) == b"corrupt checkpoint file"
     assert lib.yh_status_string(A.YH_ENONFINITE) == b"non-finite state"
+
+
+def test_same_problem_is_the_load_rule(tmp_path):
+    p, fk, fields, m = _case(A.YH_MODEL_FK3V)
+    path = tmp_path / "s.yhck"
+    ck.write(path, p, A.YH_MODEL_FK3V, fk, 3, *fields, mask=m)
+    c = ck.read(path)
+    assert ck.same_problem(c, p, A.YH_MODEL_FK3V, fk, m)
+    assert ck.same_problem(c, p, A.YH_MODEL_FK3V, fk, m * 7)  # nonzero = tissue
+    q = p.copy()
+    q.Lx += 1.0   # not a step coefficient
+    assert ck.same_problem(c, q, A.YH_MODEL_FK3V, fk, m)
+    q = p.copy()
+    q.rx *= 1.5
+    assert not ck.same_problem(c, q, A.YH_MODEL_FK3V, fk, m)
+    f2 = A.fk_defaults()
+    f2.k = 11.0
+    assert not ck.same_problem(c, p, A.YH_MODEL_FK3V, f2, m)
+    m2 = m.copy()
+    m2[0] = 1 - m2[0]
+    assert not ck.same_problem(c, p, A.YH_MODEL_FK3V, fk, m2)
+    assert not ck.same_problem(c, p, A.YH_MODEL_FK3V, fk, None)
+    assert not ck.same_problem(c, p, A.YH_MODEL_REF2V, fk, m)

@@ -161,3 +161,75 @@ def test_run_checked_rolls_back_to_the_last_finite_segment():
     assert s.step_count() == 130 and s.check_finite() == 0
     for h in (m, ref, s):
         h.close()
+
+
+def _batch_case(seed=5):
+    """Three grids of different shapes, D, tau_d, masks and events."""
+    rng = np.random.default_rng(seed)
+    params, fks, masks, states, stims = [], [], [], [], []
+    for k, (nx, ny) in enumerate([(64, 48), (96, 64), (32, 32)]):
+        p = A.fk_tissue_params(nx, ny, D=float(rng.uniform(5e-4, 1.5e-3)))
+        fk = A.fk_defaults()
+        fk.tau_d *= float(rng.uniform(0.8, 1.2))
+        solid = None if k == 1 else W.hole_mask(nx, ny, 3, 2.0, 4.0, rng)
+        st = [np.zeros(nx * ny, np.float32), np.ones(nx * ny, np.float32),
+              np.ones(nx * ny, np.float32)]
+        if solid is not None:
+            for f in st:
+                f[solid == 0] = 0
+        params.append(p)
+        fks.append(fk)
+        masks.append(solid)
+        states.append(st)
+        stims += [(k, W.stim(20 + 10 * k, 0, 0, nx // 2, ny // 2)),
+                  (k, W.stim(90 + 5 * k, nx // 3, ny // 3, nx // 3 + 8,
+                             ny // 3 + 6))]
+    return params, fks, masks, states, stims
+
+
+def _make_batch(params, fks, masks, states):
+    from yolohtli_gb300.batch import Batch
+    b = Batch(params, fks, masks)
+    for k, st in enumerate(states):
+        b.set_state(k, *st)
+    return b
+
+
+def test_batch_resume_equals_the_uninterrupted_run(tmp_path):
+    params, fks, masks, states, stims = _batch_case()
+    d = tmp_path / "batch"
+    a = _make_batch(params, fks, masks, states)
+    a.run(60, stims)
+    a.save_checkpoint(d)
+    a.run(60, stims)  # crosses every instance's second event
+    want = [a.get_state(k) for k in range(3)]
+    half = [[np.full_like(f, 0.5) for f in st] for st in states]
+    b = _make_batch(params, fks, masks, half)
+    b.load_checkpoint(d)
+    assert b.step_count() == 60
+    b.run(60, stims)
+    for k in range(3):
+        for x, y in zip(b.get_state(k), want[k]):
+            assert x.tobytes() == y.tobytes()
+    # another problem (instance 2's tau_d) is refused and changes nothing
+    fks2 = [A.FKParams.from_buffer_copy(f) for f in fks]
+    fks2[2].tau_d *= 1.1
+    c = _make_batch(params, fks2, masks, states)
+    with pytest.raises(YolohtliError) as e:
+        c.load_checkpoint(d)
+    assert e.value.status == A.YH_EINVAL
+    assert c.step_count() == 0
+    for k in range(3):
+        for x, y in zip(c.get_state(k), states[k]):
+            assert x.tobytes() == y.tobytes()
+    # a corrupt file is reported and changes nothing
+    f1 = d / "instance_0001.yhck"
+    raw = bytearray(f1.read_bytes())
+    raw[-1] ^= 1
+    f1.write_bytes(bytes(raw))
+    with pytest.raises(YolohtliError) as e:
+        b.load_checkpoint(d)
+    assert e.value.status == A.YH_ECORRUPT
+    assert b.step_count() == 120
+    for h in (a, b, c):
+        h.close()

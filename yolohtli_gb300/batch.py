@@ -110,6 +110,45 @@ class Batch:
         check("yh_batch_get_step", self.lib.yh_batch_get_step(self.h, C.byref(s)))
         return s.value
 
+    def set_step(self, step):
+        check("yh_batch_set_step", self.lib.yh_batch_set_step(self.h, int(step)))
+
+    @staticmethod
+    def checkpoint_path(directory, k):
+        import os
+        return os.path.join(str(directory), "instance_%04d.yhck" % k)
+
+    def save_checkpoint(self, directory):
+        """One checkpoint file per instance (yolohtli_gb300.checkpoint), all
+        at the batch's step, in `directory` (created if missing)."""
+        import os
+        from . import checkpoint as ck
+        os.makedirs(str(directory), exist_ok=True)
+        step = self.step_count()
+        for k in range(self.count):
+            ck.write(self.checkpoint_path(directory, k), self.params[k],
+                     A.YH_MODEL_FK3V, self.fks[k], step, *self.get_state(k),
+                     mask=self._masks[k])
+
+    def load_checkpoint(self, directory):
+        """Restores every instance's state and the step from the files of
+        save_checkpoint. Every file is read and checked first: a corrupt
+        file raises YH_ECORRUPT, another problem (an instance's grid, step
+        coefficients, FK3V parameters or mask) or files at different steps
+        raise YH_EINVAL, and the batch is left as it was."""
+        from . import checkpoint as ck
+        got = [ck.read(self.checkpoint_path(directory, k))
+               for k in range(self.count)]
+        for k, c in enumerate(got):
+            if not ck.same_problem(c, self.params[k], A.YH_MODEL_FK3V,
+                                   self.fks[k], self._masks[k]):
+                check("yh_batch_load_checkpoint", A.YH_EINVAL)
+        if len({c.step for c in got}) != 1:
+            check("yh_batch_load_checkpoint", A.YH_EINVAL)
+        for k, c in enumerate(got):
+            self.set_state(k, *c.fields)
+        self.set_step(got[0].step)
+
     def launch_count(self):
         n = C.c_longlong()
         check("yh_batch_get_launch_count",

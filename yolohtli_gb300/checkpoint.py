@@ -70,3 +70,26 @@ def read(path):
         _path(path), C.byref(p), C.byref(model), C.byref(fk),
         None if mask is None else mask.ctypes.data, C.byref(step), *ptrs))
     return Checkpoint(p, model.value, fk, mask, step.value, fields)
+
+
+# The parameters the step's coefficients are made of: the fields that
+# yh_load_checkpoint compares (make_step_coeffs in csrc/yh_api.cu).
+STEP_FIELDS = ("nx", "ny", "gateDiff", "rx", "ry", "rscale", "dt", "tc", "mu",
+               "alpha", "eps", "delta", "gamma", "beta", "theta")
+
+
+def same_problem(ckpt, p, model, fk, mask):
+    """True when checkpoint `ckpt` belongs to the problem (p, model, fk,
+    mask): the rule of yh_load_checkpoint, restated for callers that keep
+    the parameters on the host (the batched solver)."""
+    if ckpt.model != model:
+        return False
+    if any(getattr(ckpt.p, f) != getattr(p, f) for f in STEP_FIELDS):
+        return False
+    if model == A.YH_MODEL_FK3V and any(
+            getattr(ckpt.fk, f) != getattr(fk, f) for f in A.FK_NAMES):
+        return False
+    if (ckpt.mask is None) != (mask is None):
+        return False
+    return mask is None or np.array_equal(ckpt.mask != 0,
+                                          np.asarray(mask).ravel() != 0)

@@ -948,6 +948,14 @@ extern "C" int yh_batch_get_step(yh_batch *b, int *step) {
   return YH_OK;
 }
 
+// Each launch takes its step base from b->step (batch_set_base), so moving
+// the clock needs nothing recaptured.
+extern "C" int yh_batch_set_step(yh_batch *b, int step) {
+  if (!b || step < 0) return YH_EINVAL;
+  b->step = step;
+  return YH_OK;
+}
+
 extern "C" int yh_batch_get_launch_count(yh_batch *b, long long *n) {
   if (!b || !n) return YH_EINVAL;
   *n = b->launches;
