@@ -148,11 +148,37 @@ def cpu_baseline(wl, seconds=10.0):
                           elapsed)}
 
 
+def issue_roofline(key, gcs, clocks, sms=152):
+    """The instruction-issue bound of the dominant kernel: warp instructions
+    per cell-step from its ncu capture (profiles/traffic.json,
+    "warp_inst_per_cell_step") x cell-steps/s, against the issue ceiling of
+    one warp instruction per cycle per scheduler (4 per SM) at the SM clock
+    sampled during the timed region."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        w = json.load(f).get("warp_inst_per_cell_step", {}).get(key)
+    mhz = clocks.get("sm_mhz") if clocks else None
+    if w is None or not mhz:
+        return None
+    achieved = gcs * 1e9 * w
+    peak = sms * 4 * mhz * 1e6
+    return {"warp_inst_per_cell_step": w,
+            "thread_inst_per_cell_step": round(32 * w, 1),
+            "achieved_warp_inst_per_s": round(achieved / 1e12, 4),
+            "peak_warp_inst_per_s": round(peak / 1e12, 4), "unit": "T/s",
+            "frac": round(achieved / peak, 4), "sm_mhz": mhz,
+            "note": "warp instructions per cell-step from ncu x cell-steps/s "
+                    "over %d SMs x 4 schedulers x 1 issue/cycle at the "
+                    "sampled SM clock" % sms}
+
+
 def config_of(wl, args, tb, autotuned=False, engine="cpu"):
     state_mb = 12.0 * wl.cells / 2 ** 20
     return {"workload": wl.name, "grid": [wl.p.nx, wl.p.ny],
             "steps_per_solve": wl.nsteps, "model": "FK3V",
-            "holes": int(round(300 * wl.cells / 2 ** 20)),
+            "holes": 0 if wl.solid is None else int(round(300 * wl.cells / 2 ** 20)),
             "s2_patches": len(wl.stims),
             "cells": wl.cells, "dt_ms": wl.p.dt, "dx_cm": wl.p.hx,
             "engine": engine, "time_block": tb, "engine_autotuned": autotuned,
@@ -227,13 +253,16 @@ def run_reference(args, wl):
         return
     from oracle import oracle as O
     cores = os.cpu_count() or 1
-    sample_steps = 64
-    st0 = wl.state0()
+    # consecutive windows of the solve: bench step k advances the state by
+    # the next sample_steps steps (stimulus events included), so the sample
+    # covers the first (warmup + steps) x sample_steps steps of the run
+    sample_steps = 256
+    st = wl.state0()
     times = []
     for k in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        O.run(wl.p, wl.model, wl.fk, st0, sample_steps, wl.stims, wl.solid,
-              dtype=np.float32)
+        st = O.run(wl.p, wl.model, wl.fk, st, sample_steps, wl.stims, wl.solid,
+                   step0=k * sample_steps, dtype=np.float32)
         dt = time.perf_counter() - t0
         if k >= args.warmup:
             times.append(dt)
@@ -249,9 +278,12 @@ def run_reference(args, wl):
         "cpu_baseline": {
             "value": round(value, 4), "unit": METRIC, "cores": cores,
             "kind": "port",
-            "sample": "each step: first %d steps of %s on the host cores, FP32 "
-                      "C/OpenMP transcription of the reference step "
-                      "(the reference has no CPU path)" % (sample_steps, wl.name)},
+            "sample": "each step: the next %d steps of %s (steps 0-%d over "
+                      "the run, the S2 patches included) on the host cores, "
+                      "FP32 C/OpenMP transcription of the reference step "
+                      "(the reference has no CPU path)" % (
+                          sample_steps, wl.name,
+                          (args.warmup + args.steps) * sample_steps)},
         "e2e": {"value": round(value, 4), "unit": METRIC,
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -261,28 +293,21 @@ def run_reference(args, wl):
     print(json.dumps(line), flush=True)
 
 
-def run_batch(args):
+def batch_measure(nsteps, solves, warmup, dist, world, loops=True):
     """The batched workload (fk_batch_256: 256 FK3V grids of 128^2 .. 768^2,
-    5,000 steps): the batched solver against a loop of single-grid solvers,
-    on one shared stream and on one stream per grid, all on this GPU."""
+    `nsteps` steps): the batched solver (schedule autotuned on the initial
+    state), then, with `loops`, a loop of single-grid solvers on one shared
+    stream and on one stream per grid, all on this GPU. Returns a dict."""
     import torch
-    rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
-    torch.cuda.set_device(env_int("LOCAL_RANK", 0))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device(
-            "cuda", env_int("LOCAL_RANK", 0)))
     from yolohtli_gb300 import _abi as A
     from yolohtli_gb300 import workloads as W
     from yolohtli_gb300.batch import Batch
     from yolohtli_gb300.solver import Monodomain
-    bw = W.fk_batch_256(seed=0, nsteps=args.nsteps)
+    bw = W.fk_batch_256(seed=0, nsteps=nsteps)
     insts = bw.instances
     b = Batch([w.p for w in insts], [w.fk for w in insts],
               [w.solid for w in insts])
     dev0 = [[torch.tensor(x, device="cuda") for x in w.state0()] for w in insts]
-
     lib = b.lib
 
     def events():
@@ -296,10 +321,9 @@ def run_batch(args):
                                              for x in dev0[k]])
         b.synchronize()
 
-    # the library's schedule autotuner on the workload's initial state
     restore()
     tuned = b.autotune(256)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         restore()
         b.run(bw.nsteps, events())
     b.synchronize()
@@ -309,7 +333,7 @@ def run_batch(args):
     clocks.start()
     launches0 = b.launch_count()
     sec = 0.0
-    for k in range(args.steps):
+    for k in range(solves):
         restore()
         ev = events()
         if k == 0:  # the range `ncu --profile-from-start off` captures
@@ -323,83 +347,114 @@ def run_batch(args):
     clk = clocks.stop()
     launches = b.launch_count() - launches0
     sec = max_over_ranks(sec, dist, "cuda")
-    value = job_value(bw.cells, bw.nsteps, args.steps, world, sec)
+    value = job_value(bw.cells, bw.nsteps, solves, world, sec)
 
     # end to end: host buffers in, u of every grid out, every solve
     hst = [[torch.tensor(x).pin_memory() for x in w.state0()] for w in insts]
     outs = [torch.empty(w.cells, dtype=torch.float32).pin_memory() for w in insts]
     b.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(solves):
         for k in range(len(insts)):
             lib.yh_batch_set_state(b.h, k, *[C.c_void_p(x.data_ptr()) for x in hst[k]])
         b.run(bw.nsteps, events())
         for k in range(len(insts)):
             lib.yh_batch_get_state(b.h, k, C.c_void_p(outs[k].data_ptr()), None, None)
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
-    e2e = {"value": round(job_value(bw.cells, bw.nsteps, args.steps, world, e2e_s), 3),
+    e2e = {"value": round(job_value(bw.cells, bw.nsteps, solves, world, e2e_s), 3),
            "unit": METRIC, "h2d_bytes_per_step": 12 * bw.cells,
            "d2h_bytes_per_step": 4 * bw.cells}
     b.close()
+    del dev0, hst, outs
+    torch.cuda.empty_cache()
 
     # loops of single-grid solvers (step engine): one shared stream, then
-    # one stream per grid
-    loops = {}
-    for mode in ("one_stream", "stream_per_grid"):
-        s0 = torch.cuda.Stream() if mode == "one_stream" else None
-        ms = [Monodomain(w.p, w.model, w.fk, solid=w.solid,
-                         stream=s0.cuda_stream if s0 else None) for w in insts]
-        for m in ms:
-            m.set_engine(A.YH_ENGINE_STEP, 1)
-        sec_l = 0.0
-        for rep in range(2):  # a warm-up solve, then the timed one
-            for m, w in zip(ms, insts):
-                m.set_state(*w.state0())
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            for m, w in zip(ms, insts):
-                base = m.step_count()
-                m.run(bw.nsteps, [W.stim(x.step + base, x.i0, x.j0, x.i1, x.j1, x.value)
-                                  for x in w.stims])
+    # one stream per grid; a warm-up solve, then the timed one
+    lp = {}
+    if loops:
+        for mode in ("one_stream", "stream_per_grid"):
+            s0 = torch.cuda.Stream() if mode == "one_stream" else None
+            ms = [Monodomain(w.p, w.model, w.fk, solid=w.solid,
+                             stream=s0.cuda_stream if s0 else None) for w in insts]
             for m in ms:
-                m.synchronize()
-            sec_l = time.perf_counter() - t0
-        for m in ms:
-            m.close()
-        loops[mode] = round(job_value(bw.cells, bw.nsteps, 1, world,
-                                      max_over_ranks(sec_l, dist, "cuda")), 3)
+                m.set_engine(A.YH_ENGINE_STEP, 1)
+            sec_l = 0.0
+            for rep in range(2):
+                for m, w in zip(ms, insts):
+                    m.set_state(*w.state0())
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for m, w in zip(ms, insts):
+                    base = m.step_count()
+                    m.run(bw.nsteps, [W.stim(x.step + base, x.i0, x.j0, x.i1,
+                                             x.j1, x.value) for x in w.stims])
+                for m in ms:
+                    m.synchronize()
+                sec_l = time.perf_counter() - t0
+            for m in ms:
+                m.close()
+            lp[mode] = round(job_value(bw.cells, bw.nsteps, 1, world,
+                                       max_over_ranks(sec_l, dist, "cuda")), 3)
+    return {"bw": bw, "value": value, "sec": sec, "solves": solves,
+            "tuned": tuned, "launches": launches, "clocks": clk, "e2e": e2e,
+            "loops": lp}
 
+
+def batch_config(bw, tuned, world):
+    return {"workload": bw.name, "instances": len(bw.instances),
+            "cells": bw.cells, "steps_per_solve": bw.nsteps,
+            "sizes": "n ~ U{128,160,...,768}, square",
+            "schedule": "autotuned: groups of ~%d cells on %d streams, %d "
+                        "steps per launch" % tuned[:3],
+            "parallelism": "replicas x%d" % world}
+
+
+def batch_summary(r):
+    """The batched workload's figures as one object of the headline line."""
+    lp = r["loops"]
+    out = {"metric": METRIC, "value": round(r["value"], 3), "unit": METRIC,
+           "config": batch_config(r["bw"], r["tuned"], 1),
+           "solves_timed": r["solves"], "e2e": r["e2e"],
+           "gpu_launches_per_solve": round(r["launches"] / r["solves"], 1),
+           "loop_baselines": dict(lp, unit=METRIC)}
+    for k, v in lp.items():
+        out["x_vs_" + k] = round(r["value"] / v, 3) if v else None
+    return out
+
+
+def run_batch(args):
+    """The batched workload's own line (see batch_measure)."""
+    import torch
+    rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
+    torch.cuda.set_device(env_int("LOCAL_RANK", 0))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(
+            "cuda", env_int("LOCAL_RANK", 0)))
+    r = batch_measure(args.nsteps, args.steps, args.warmup, dist, world)
     if rank == 0:
         peak, peak_kind = measured_peaks()
+        value = r["value"]
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": METRIC,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(1e3 * sec / args.steps, 3),
+            "ms_per_step": round(1e3 * r["sec"] / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": bw.name, "instances": len(insts),
-                       "cells": bw.cells, "steps_per_solve": bw.nsteps,
-                       "sizes": "n ~ U{128,160,...,768}, square",
-                       "schedule": "autotuned: groups of ~%d cells on %d "
-                                   "streams, %d steps per launch" % tuned,
-                       "l2": "1.48 GB of state per step, above the L2; "
-                             "each group's %.0f MB (two levels) stays in it"
-                             % (tuned[0] * 24 / 1e6),
-                       "parallelism": "replicas x%d" % world},
+            "config": batch_config(r["bw"], r["tuned"], world),
             "roofline": {"bound": "hbm", "achieved": round(25.0 * value, 1),
                          "peak": peak, "unit": "GB/s",
                          "frac": round(25.0 * value / peak, 4), "traffic": None,
                          "peak_kind": peak_kind, "alg_bytes_per_cell_step": 25,
-                         "kernel": "rd_batch_kernel",
                          "note": "achieved = 25 B x cell-steps/s over the whole "
-                                 "run; groups are L2-resident, so frac > 1 is "
-                                 "possible"},
-            "cpu_baseline": None, "e2e": e2e,
-            "loop_baselines": {"unit": METRIC, **loops,
-                               "note": "the same 256 grids run one by one "
-                                       "through single-grid solver handles "
-                                       "(step engine, graphs)"},
-            "gpu_launches": int(launches), "clocks": clk,
+                                 "run; state on chip, so frac > 1 is possible"},
+            "cpu_baseline": None, "e2e": r["e2e"],
+            "loop_baselines": dict(r["loops"], unit=METRIC,
+                                   note="the same 256 grids run one by one "
+                                        "through single-grid solver handles "
+                                        "(step engine, graphs)"),
+            "gpu_launches": int(r["launches"]), "clocks": r["clocks"],
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -711,45 +766,81 @@ def run_sr_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def run_adjoint(args):
+ADJ_BYTES = {"sqrt_n": 104, "store_all": 76}
+
+
+def adjoint_roofline(grads_per_s, cells, nsteps, mode="sqrt_n"):
+    """Algorithmic bytes of one gradient per cell-step: the forward step
+    reads D, u, v, w and writes u, v, w (28 B); the reverse step reads D,
+    u, v, w, the adjoint state lu, lv, lw, writes lu, lv, lw and updates
+    the D gradient (48 B). sqrt(N) checkpoints run every forward step twice
+    (the pass that records the checkpoints, the segment recompute):
+    2 x 28 + 48 = 104 B; with every state kept, 28 + 48 = 76 B."""
+    peak, kind = measured_peaks()
+    b = ADJ_BYTES[mode]
+    achieved = grads_per_s * b * cells * nsteps / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+            "peak_kind": kind, "alg_bytes_per_cell_step": b,
+            "note": "achieved = %d B x cells x steps per gradient x "
+                    "gradients/s (forward %s + reverse)" % (
+                        b, "+ recompute" if mode == "sqrt_n" else "")}
+
+
+def adjoint_cpu_baseline(p, fk, D, state0, target, nsteps, frame, spacing,
+                         smooth, sample_steps=200):
+    """The FP64 tangent-linear oracle (oracle/yh_oracle_tlm.c, dual numbers,
+    one directional derivative per run) on the host cores, on the first
+    `sample_steps` steps of the workload; scaled to the whole horizon."""
+    from oracle import oracle as O
+    from yolohtli_gb300 import _abi as A
+    dfk = A.FKParams()
+    dD = np.asarray(D, np.float32) * 0.01
+    t0 = time.perf_counter()
+    O.adj_tlm(p, fk, dfk, smooth, sample_steps, frame, spacing, D, dD, state0,
+              target)
+    sec = (time.perf_counter() - t0) * nsteps / sample_steps
+    return {"value": round(1.0 / sec, 5), "unit": "directional derivatives/s",
+            "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": "FP64 tangent-linear model (dual numbers) of the same "
+                      "forward map, first %d of %d steps on %dx%d, scaled to "
+                      "the horizon; a full gradient by this route takes "
+                      "%d directional derivatives (D and the 13 parameters)"
+                      % (sample_steps, nsteps, p.nx, p.ny, p.nx * p.ny + 13)}
+
+
+def adjoint_measure(nsteps, steps, warmup, dist, world, full=False):
     """The adjoint workload (fk_adjoint_512: 512^2 FK3V, D(x, y) of 8
-    Gaussian bumps in [5e-4, 1.5e-3], 10,000 steps, the loss on a 32 x 32
+    Gaussian bumps in [5e-4, 1.5e-3], `nsteps` steps, the loss on a 32 x 32
     probe lattice every 20 steps, target from the true D, gradient at
     1.1 D; the model's switches as tanh ramps of width 0.01, without which
     the loss's derivative is not usable at this horizon). A gradient is the
-    full one: dLoss/dD and dLoss/d(13 FK parameters). Reported: gradients
-    per second with sqrt(N) checkpoints (the headline), with every state
-    kept, and for 16 instances in one batched handle; the FP32 gradient
-    against the FP64 one; the FP64 gradient against central differences of
-    the FP64 loss along 20 random directions of (D, FK parameters)."""
+    full one: dLoss/dD and dLoss/d(13 FK parameters). Returns gradients per
+    second with sqrt(N) checkpoints and the ratio to the forward run; with
+    `full` also every state kept, 16 instances in one handle, and the
+    accuracy checks (FP32 against FP64, FP64 against central differences
+    along 20 random directions of (D, FK parameters))."""
     import torch
-    rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
-    torch.cuda.set_device(env_int("LOCAL_RANK", 0))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device(
-            "cuda", env_int("LOCAL_RANK", 0)))
     from yolohtli_gb300 import _abi as A
     from yolohtli_gb300 import workloads as W
     from yolohtli_gb300.adjoint import Adjoint, fk_array, fk_struct
-    n, nsteps = 512, args.nsteps
+    n = 512
     frame, spacing = 20, 16
     ck = max(1, int(round(nsteps ** 0.5)))
     p = A.fk_tissue_params(n, n)
     D_true, state0 = W.fk_adjoint_case(n, seed=0)
-    smooth = 0.01  # tanh switches: a derivative usable over 10,000 steps
+    smooth = 0.01
     fk0 = A.fk_defaults()
 
-    def make(fp64, steps, ckpt, batch=1):
-        a = Adjoint(p, fk0, steps, frame, spacing, ckpt, fp64=fp64,
+    def make(fp64, nst, ckpt, batch=1):
+        a = Adjoint(p, fk0, nst, frame, spacing, ckpt, fp64=fp64,
                     smooth=smooth, batch=batch)
         st = [torch.tensor(x, device="cuda").repeat(batch) for x in state0]
         Dt = torch.tensor(D_true, device="cuda").repeat(batch)
         tgt = torch.empty(a.target_shape, dtype=torch.float32, device="cuda")
         a.record(Dt, st, tgt)
         a.set_target(tgt)
-        return a, st, Dt * 1.1
+        return a, st, Dt * 1.1, tgt
 
     def timed(a, st, D, k, grad=True):
         g = torch.empty_like(D) if grad else None
@@ -760,8 +851,8 @@ def run_adjoint(args):
             loss = a.run(D, st, g, gfk)
         return time.perf_counter() - t0, loss, g, gfk
 
-    adj, st, D = make(False, nsteps, ck)
-    for _ in range(args.warmup):
+    adj, st, D, tgt = make(False, nsteps, ck)
+    for _ in range(warmup):
         timed(adj, st, D, 1)
     if dist:
         dist.barrier()
@@ -770,11 +861,11 @@ def run_adjoint(args):
     torch.cuda.profiler.stop()
     clocks = ClockSampler(env_int("LOCAL_RANK", 0))
     clocks.start()
-    sec, loss, g, gfk = timed(adj, st, D, args.steps)
+    sec, loss, g, gfk = timed(adj, st, D, steps)
     clk = clocks.stop()
-    fwd, _, _, _ = timed(adj, st, D, args.steps, grad=False)
+    fwd, _, _, _ = timed(adj, st, D, steps, grad=False)
     sec = max_over_ranks(sec, dist, "cuda")
-    value = world * args.steps / sec
+    value = world * steps / sec
     # end to end: D from the host, both gradients back, every gradient
     Dh = D.cpu().pin_memory()
     gh = torch.empty_like(Dh).pin_memory()
@@ -782,37 +873,60 @@ def run_adjoint(args):
     gfk_h = A.FKParams()
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         Dd.copy_(Dh, non_blocking=True)
         adj.run(Dd, st, g, gfk_h)
         gh.copy_(g)
     e2e_s = max_over_ranks(time.perf_counter() - t2, dist, "cuda")
+    out = {"value": value, "sec": sec, "loss": float(loss),
+           "forward_ratio": sec / fwd, "clocks": clk,
+           "checkpoint_steps": ck, "smooth": smooth, "n": n, "frame": frame,
+           "spacing": spacing,
+           "e2e": {"value": round(world * steps / e2e_s, 3),
+                   "unit": "gradients/s", "h2d_bytes_per_step": 4 * n * n,
+                   "d2h_bytes_per_step": 4 * n * n + 13 * 8},
+           "roofline": adjoint_roofline(value / world, n * n, nsteps)}
+    if env_int("RANK", 0) == 0 and world == 1:
+        out["cpu_baseline"] = adjoint_cpu_baseline(
+            p, fk0, (D.cpu().numpy()), state0, tgt.cpu().numpy(), nsteps,
+            frame, spacing, smooth)
+    if not full:
+        del adj
+        torch.cuda.empty_cache()
+        return out
     # every state kept (31 GB at this size): no recompute
     del adj
     torch.cuda.empty_cache()
-    a1, st1, D1 = make(False, nsteps, 1)
+    a1, st1, D1, _ = make(False, nsteps, 1)
     timed(a1, st1, D1, 1)
-    s1, _, _, _ = timed(a1, st1, D1, args.steps)
-    f1, _, _, _ = timed(a1, st1, D1, args.steps, grad=False)
+    s1, _, _, _ = timed(a1, st1, D1, steps)
+    f1, _, _, _ = timed(a1, st1, D1, steps, grad=False)
     del a1
     torch.cuda.empty_cache()
+    out["store_all_states"] = {
+        "value": round(steps / s1, 3), "unit": "gradients/s",
+        "forward_ratio": round(s1 / f1, 3),
+        "memory_gb": round(3 * 4 * n * n * nsteps / 1e9, 1),
+        "roofline": adjoint_roofline(steps / s1, n * n, nsteps, "store_all")}
     # 16 instances, one handle
     B = 16
-    ab, stb, Db = make(False, nsteps, ck, batch=B)
+    ab, stb, Db, _ = make(False, nsteps, ck, batch=B)
     timed(ab, stb, Db, 1)
-    sb, _, _, _ = timed(ab, stb, Db, max(1, args.steps // 2))
-    batch_rate = B * max(1, args.steps // 2) / sb
+    sb, _, _, _ = timed(ab, stb, Db, max(1, steps // 2))
+    batch_rate = B * max(1, steps // 2) / sb
     del ab
     torch.cuda.empty_cache()
-    # accuracy at the full size: the FP64 gradients against central
-    # differences of the FP64 loss (h = 1e-3 relative) along 20 random
-    # directions of (D, FK parameters); the FP32 gradients against FP64
-    b64, st64, D64 = make(True, nsteps, ck)
+    out["batched_16"] = {"value": round(batch_rate, 3),
+                         "unit": "instance gradients/s", "checkpoint_steps": ck,
+                         "note": "16 instances in one handle, one launch per step",
+                         "roofline": adjoint_roofline(batch_rate, n * n, nsteps)}
+    # accuracy at the full size
+    b64, st64, D64, _ = make(True, nsteps, ck)
     g64 = torch.empty_like(D64)
     f64 = A.FKParams()
     t3 = time.perf_counter()
     b64.run(D64, st64, g64, f64)
-    fp64_rate = 1.0 / (time.perf_counter() - t3)
+    out["fp64_gradients_per_s"] = round(1.0 / (time.perf_counter() - t3), 3)
     th0 = fk_array(fk0)
     rng = np.random.default_rng(3)
     ndir = 20
@@ -822,65 +936,166 @@ def run_adjoint(args):
         dth = rng.standard_normal(13) * th0
         for hrel in fd_err:
             Dp, Dm = D64 + hrel * d, D64 - hrel * d
-            step = (Dp.double() - Dm.double()) / 2
+            stp = (Dp.double() - Dm.double()) / 2
             b64.set_fk(fk_struct(th0 + hrel * dth))
             Lp = b64.run(Dp, st64)
             b64.set_fk(fk_struct(th0 - hrel * dth))
             Lm = b64.run(Dm, st64)
-            ad = 2 * (float((g64.double() * step).sum()) +
+            ad = 2 * (float((g64.double() * stp).sum()) +
                       hrel * float(np.dot(fk_array(f64), dth)))
             fd_err[hrel] = max(fd_err[hrel], abs((Lp - Lm) - ad) / max(abs(ad), 1e-300))
     b64.set_fk(fk0)
-    rel = float((g.double() - g64.double()).norm() / g64.double().norm())
-    rel_fk = float(np.abs(fk_array(gfk[0]) - fk_array(f64)).max() /
-                   np.abs(fk_array(f64)).max())
+    out["fd_check"] = {"directions": ndir,
+                       "max_rel_err": {"h_rel 1e-3": fd_err[1e-3],
+                                       "h_rel 1e-5": fd_err[1e-5]},
+                       "note": "directional derivatives of the FP64 adjoint "
+                               "along random directions of D (relative) and "
+                               "all 13 FK parameters (relative) against "
+                               "central differences of the FP64 loss, full "
+                               "size; the error falling as h^2 is the "
+                               "differences' truncation"}
+    out["fp32_vs_fp64_gradient_rel_l2"] = float(
+        (g.double() - g64.double()).norm() / g64.double().norm())
+    out["fp32_vs_fp64_fk_gradient_rel_max"] = float(
+        np.abs(fk_array(gfk[0]) - fk_array(f64)).max() / np.abs(fk_array(f64)).max())
+    return out
+
+
+def adjoint_config(r, nsteps, world):
+    n = r["n"]
+    return {"workload": "fk_adjoint_512", "grid": [n, n],
+            "steps_per_gradient": nsteps, "frames": nsteps // r["frame"],
+            "probes": [n // r["spacing"], n // r["spacing"]],
+            "checkpoint_steps": r["checkpoint_steps"],
+            "gradient": "dLoss/dD (512^2) and dLoss/d(13 FK parameters)",
+            "D": "8 Gaussian bumps in [5e-4, 1.5e-3]",
+            "switches": "FK3V's H(u - u_c), H(u - u_v) as tanh ramps of "
+                        "width %g" % r["smooth"],
+            "estimate": "1.1 x the true D",
+            "parallelism": "replicas x%d" % world}
+
+
+def run_adjoint(args):
+    """The adjoint workload's own line (see adjoint_measure)."""
+    import torch
+    rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
+    torch.cuda.set_device(env_int("LOCAL_RANK", 0))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(
+            "cuda", env_int("LOCAL_RANK", 0)))
+    r = adjoint_measure(args.nsteps, args.steps, args.warmup, dist, world,
+                        full=True)
     if rank == 0:
         line = {
-            "metric": "adjoint gradients/s", "value": round(value, 3),
+            "metric": "adjoint gradients/s", "value": round(r["value"], 3),
             "unit": "gradients/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(1e3 * sec / args.steps, 3),
+            "warmup": args.warmup,
+            "ms_per_step": round(1e3 * r["sec"] / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "fk_adjoint_512", "grid": [n, n],
-                       "steps_per_gradient": nsteps, "frames": nsteps // frame,
-                       "probes": [n // spacing, n // spacing],
-                       "checkpoint_steps": ck,
-                       "gradient": "dLoss/dD (512^2) and dLoss/d(13 FK parameters)",
-                       "D": "8 Gaussian bumps in [5e-4, 1.5e-3]",
-                       "switches": "FK3V's H(u - u_c), H(u - u_v) as tanh ramps of width %g" % smooth,
-                       "estimate": "1.1 x the true D",
-                       "parallelism": "replicas x%d" % world},
-            "loss": float(loss), "forward_ratio": round(sec / fwd, 3),
-            "store_all_states": {"value": round(args.steps / s1, 3),
-                                 "unit": "gradients/s",
-                                 "forward_ratio": round(s1 / f1, 3),
-                                 "memory_gb": round(3 * 4 * n * n * nsteps / 1e9, 1)},
-            "batched_16": {"value": round(batch_rate, 3),
-                           "unit": "instance gradients/s",
-                           "checkpoint_steps": ck,
-                           "note": "16 instances in one handle, one launch per step"},
-            "fd_check": {"directions": ndir,
-                         "max_rel_err": {"h_rel 1e-3": fd_err[1e-3],
-                                         "h_rel 1e-5": fd_err[1e-5]},
-                         "note": "directional derivatives of the FP64 "
-                                 "adjoint along random directions of D "
-                                 "(relative) and all 13 FK parameters "
-                                 "(relative) against central differences of "
-                                 "the FP64 loss, full size; the error "
-                                 "falling as h^2 is the differences' "
-                                 "truncation"},
-            "fp32_vs_fp64_gradient_rel_l2": rel,
-            "fp32_vs_fp64_fk_gradient_rel_max": rel_fk,
-            "fp64_gradients_per_s": round(fp64_rate, 3),
-            "roofline": None, "cpu_baseline": None,
-            "e2e": {"value": round(world * args.steps / e2e_s, 3),
-                    "unit": "gradients/s", "h2d_bytes_per_step": 4 * n * n,
-                    "d2h_bytes_per_step": 4 * n * n + 13 * 8},
-            "gpu_launches": None, "clocks": clk,
-        }
+            "config": adjoint_config(r, args.nsteps, world),
+            "loss": r["loss"], "forward_ratio": round(r["forward_ratio"], 3),
+            "roofline": r["roofline"], "cpu_baseline": r.get("cpu_baseline"),
+            "e2e": r["e2e"], "gpu_launches": None, "clocks": r["clocks"]}
+        for k in ("store_all_states", "batched_16", "fd_check",
+                  "fp32_vs_fp64_gradient_rel_l2",
+                  "fp32_vs_fp64_fk_gradient_rel_max", "fp64_gradients_per_s"):
+            line[k] = r[k]
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def adjoint_summary(r, nsteps):
+    return {"metric": "adjoint gradients/s", "value": round(r["value"], 3),
+            "unit": "gradients/s", "config": adjoint_config(r, nsteps, 1),
+            "forward_ratio": round(r["forward_ratio"], 3),
+            "roofline": r["roofline"], "cpu_baseline": r.get("cpu_baseline"),
+            "e2e": r["e2e"]}
+
+
+def run_spiral(args):
+    """Config 0 (fk_spiral_256): FK3V 256^2, 10,000 steps, S1 columns 0-9 at
+    t = 0, S2 on the lower-left quadrant at 320 ms, tips every sampleIt =
+    40 steps (param.sample = 2 ms, main.cu:156,961-964). One bench step = one
+    solve with its tip trajectory. With --out DIR the last solve's final
+    state goes to DIR/raw_data.dat, its tips to DIR/dataTip.dat and
+    DIR/dataTipSize.dat and the parameters to DIR/dataparamcsv.csv, the
+    reference's own formats (printFunctions.cu:58-78,149-197,266-403)."""
+    import torch
+    rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
+    torch.cuda.set_device(env_int("LOCAL_RANK", 0))
+    from yolohtli_gb300 import _abi as A
+    from yolohtli_gb300 import refio
+    from yolohtli_gb300 import workloads as W
+    from yolohtli_gb300.solver import Monodomain
+    wl = W.fk_spiral_256(nsteps=args.nsteps)
+    sample_it = 40
+    m = Monodomain(wl.p, wl.model, wl.fk)
+    m.set_state(*wl.state0())
+    engine, tb = m.autotune(256)
+
+    def solve():
+        base = m.step_count()
+        stims = [W.stim(s.step + base, s.i0, s.j0, s.i1, s.j1, s.value)
+                 for s in wl.stims]
+        m.set_state(*wl.state0())
+        tips = []
+        for _ in range(wl.nsteps // sample_it):
+            m.run(sample_it, stims)
+            m.track_tips()
+            t = m.get_tips()
+            t[:, 4] = wl.p.dt * (m.step_count() - base)
+            tips.append(t)
+        return tips
+
+    for _ in range(args.warmup):
+        solve()
+    m.synchronize()
+    clocks = ClockSampler(env_int("LOCAL_RANK", 0))
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        tips = solve()
+    m.synchronize()
+    sec = time.perf_counter() - t0
+    clk = clocks.stop()
+    u, v, w = m.get_state()
+    value = job_value(wl.cells, wl.nsteps, args.steps, world, sec)
+    ntips = sum(len(t) for t in tips)
+    if args.out:
+        os.makedirs(args.out, exist_ok=True)
+        refio.write_raw_data(os.path.join(args.out, "raw_data.dat"), wl.p, u, v)
+        tp, sz = (os.path.join(args.out, f) for f in ("dataTip.dat",
+                                                      "dataTipSize.dat"))
+        for f in (tp, sz):
+            if os.path.exists(f):
+                os.unlink(f)
+        for t in tips:
+            refio.write_tips(tp, sz, t, append=True)
+        refio.write_param_csv(os.path.join(args.out, "dataparamcsv.csv"), wl.p)
+    m.close()
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": round(value, 3), "unit": METRIC,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * sec / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl.name, "grid": [wl.p.nx, wl.p.ny],
+                       "steps_per_solve": wl.nsteps, "model": "FK3V",
+                       "tips_every_steps": sample_it, "engine":
+                           A.ENGINE_NAMES[engine], "time_block": tb,
+                       "parallelism": "replicas x%d" % world},
+            "tips": {"samples": len(tips), "total": ntips,
+                     "samples_with_tips": sum(1 for t in tips if len(t)),
+                     "last_tip_ms": max([float(t[0, 4]) for t in tips if len(t)]
+                                        or [None])},
+            "final_u": {"max": float(u.max()), "mean": float(u.mean()),
+                        "cells_above_0.5": int((u > 0.5).sum())},
+            "outputs": args.out, "clocks": clk}), flush=True)
 
 
 def main():
@@ -899,7 +1114,8 @@ def main():
                     help="explicit steps per solve (default: the workload's, "
                          "20,000 for fk_holes_1024, 5,000 for batch256)")
     ap.add_argument("--workload", default="holes1024",
-                    choices=["holes1024", "batch256", "adjoint512", "sr512"],
+                    choices=["holes1024", "batch256", "adjoint512", "sr512",
+                             "spiral256"],
                     help="holes1024: one 1024^2 grid with 300 holes (the "
                          "headline); batch256: 256 grids of 128^2..768^2 "
                          "through the batched solver")
@@ -907,9 +1123,23 @@ def main():
                     help="grid side (1024 = the benchmark; larger sides are "
                          "for profiling beyond the L2, holes scaled by area)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--out", default=None,
+                    help="spiral256: directory for the final state and the "
+                         "tip trajectory in the reference's file formats")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="the headline workload alone (without the batched "
+                         "and adjoint figures the default line carries)")
     args = ap.parse_args()
 
     from yolohtli_gb300 import workloads as W
+    if args.workload == "spiral256":
+        if args.nsteps is None:
+            args.nsteps = 10000
+        if args.impl == "reference":
+            run_reference(args, W.fk_spiral_256(nsteps=args.nsteps))
+        else:
+            run_spiral(args)
+        return
     if args.workload == "sr512":
         if args.nsteps is None:
             args.nsteps = 8000  # x 5 steps = the 40,000 SR steps of the case
@@ -1038,7 +1268,8 @@ def main():
     bytes_alg = 25.0 * wl.cells * steps_per_launch
     achieved = bytes_alg / avg_launch_s / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = profiled_traffic("%s_%s%d" % (wl.name, A.ENGINE_NAMES[engine], tb))
+    key = "%s_%s%d" % (wl.name, A.ENGINE_NAMES[engine], tb)
+    traffic = profiled_traffic(key)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "traffic": traffic, "peak_kind": peak_kind,
@@ -1051,6 +1282,10 @@ def main():
                 "note": "achieved = 25 B x cells x steps_per_launch / mean launch "
                         "time; frac > 1 is possible: the state stays in L2 and "
                         "temporal blocking re-reads it once per steps_per_launch"}
+    if traffic is not None:
+        roofline["dram_bytes_per_launch"] = traffic
+        roofline["dram_gbs"] = round(traffic / avg_launch_s / 1e9, 1)
+    roofline["issue"] = issue_roofline(key, value / world, clk)
 
     # end to end through the public C ABI with pinned host buffers
     e2e = None
@@ -1081,6 +1316,16 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl)
 
+    m.close()
+    del ic, flush
+    torch.cuda.empty_cache()
+    extras = {}
+    if not args.no_extras and args.grid == 1024:
+        # the batched and adjoint workloads, shortened to a few solves each:
+        # their own lines come from --workload batch256 / adjoint512
+        extras["batched"] = batch_summary(batch_measure(5000, 2, 1, dist, world))
+        extras["adjoint"] = adjoint_summary(
+            adjoint_measure(10000, 2, 1, dist, world), 10000)
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": METRIC,
@@ -1093,8 +1338,8 @@ def main():
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clk,
         }
+        line.update(extras)
         print(json.dumps(line), flush=True)
-    m.close()
     if dist:
         dist.destroy_process_group()
 

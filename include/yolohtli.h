@@ -198,7 +198,8 @@ typedef struct yh_sym_state {
   int step;             /* steps taken (the reference's param.count)        */
   int status;           /* YH_OK or YH_ESINGULAR from the last solve        */
   int ntips;            /* tips found by the last tip pass                  */
-  int pad_;
+  int nsingular;        /* solves that found the system singular (and kept
+                           the previous c) since the state was zeroed      */
 } yh_sym_state;
 
 /* A contour point: the reference's float3 of contour_vector
@@ -365,6 +366,26 @@ int yh_stimulate_box(const yh_param_var *p, float *u, const uint8_t *solid,
                      int i0, int j0, int i1, int j1, float value,
                      void *stream);
 
+/* FP64 instances of three operators above: the same kernel templates
+ * compiled for double, on FP64 device buffers (REAL = double, the
+ * reference's storage, typeDefinition.cuh:4). They separate rounding from
+ * discretisation: a run of these against the FP64 oracle isolates the
+ * discrete map, a run of the FP32 operators against them isolates FP32
+ * rounding. Not a fast path (GB300 issues FP64 at a small fraction of its
+ * FP32 rate). Arguments and status codes as the FP32 operators. */
+typedef struct yh_fields64 { double *u, *v, *w; } yh_fields64;
+int yh_reaction_diffusion_f64(const yh_param_var *p, int model,
+                              const yh_fk_params *fk, yh_fields64 out,
+                              yh_fields64 in, yh_fields64 vel_tan,
+                              const uint8_t *solid, void *stream);
+int yh_spiral_tip_f64(const yh_param_var *p, const double *g_past,
+                      const double *g_present, double physical_time,
+                      int *tip_count, yh_tip *tip_vector, int capacity,
+                      const uint8_t *solid, void *stream);
+int yh_stimulate_box_f64(const yh_param_var *p, double *u,
+                         const uint8_t *solid, int i0, int j0, int i1, int j1,
+                         double value, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Layer 2: solver handle                                               */
 /* ------------------------------------------------------------------ */
@@ -432,6 +453,11 @@ int yh_get_tips(yh_solver *h, yh_tip *out, int capacity, int *n);
  * takes the template from the host state (tu, tv, tw); CURRENT ignores it. */
 int yh_sr_begin(yh_solver *h, int template_mode, const float *tu,
                 const float *tv, const float *tw);
+/* nsteps symmetry-reduced steps. Returns YH_ESINGULAR when a solve during
+ * these steps found the drift/rotation system singular (the frame then kept
+ * its previous c and is not a valid comoving frame; the steps were taken);
+ * yh_get_sym's nsingular counts such solves since yh_sr_begin. Reads that
+ * count back once per call (one stream synchronisation). */
 int yh_sr_step(yh_solver *h, int nsteps);
 int yh_get_sym(yh_solver *h, yh_sym_state *out);
 
@@ -459,6 +485,13 @@ int yh_check_finite(yh_solver *h, long long *bad_values);
  * checkpoint: a symmetry-reduced run resumes with a new yh_sr_begin. */
 int yh_save_checkpoint(yh_solver *h, const char *path);
 int yh_load_checkpoint(yh_solver *h, const char *path);
+/* 1 when two (parameters, model, FK3V parameters) describe the same problem
+ * for a resume (grid, model, step coefficients, FK3V parameters: the rule
+ * yh_load_checkpoint applies before the mask), else 0. Host only. */
+int yh_checkpoint_same_problem(const yh_param_var *a, int model_a,
+                               const yh_fk_params *fk_a,
+                               const yh_param_var *b, int model_b,
+                               const yh_fk_params *fk_b);
 
 /* tipAlgorithm 3 (abouzarTip_kernel / abubuFilament,
  * tipTracker.cu:434-517): marks (sets to 1, never clears) the cells whose
@@ -674,7 +707,10 @@ typedef struct yh_checkpoint_header {
   long long step;
 } yh_checkpoint_header;
 
-/* mask may be NULL: no mask is stored. w is ignored for REF2V. */
+/* mask may be NULL: no mask is stored. w is ignored for REF2V. The file is
+ * written as path + ".tmp", flushed to the disk (fsync) and renamed over
+ * path, so an interrupted write leaves an existing checkpoint at path
+ * unchanged. */
 int yh_write_checkpoint(const char *path, const yh_param_var *p, int model,
                         const yh_fk_params *fk, const uint8_t *mask,
                         long long step, const float *u, const float *v,
@@ -684,8 +720,10 @@ int yh_write_checkpoint(const char *path, const yh_param_var *p, int model,
 int yh_read_checkpoint_header(const char *path, yh_checkpoint_header *out);
 /* Reads the whole file and checks its hash. Any output may be NULL to skip
  * it. The arrays hold nx*ny elements, as the header gives. The mask is set
- * to 1 (all tissue) when the file holds none. On an error the outputs hold
- * whatever had been read. */
+ * to 1 (all tissue) when the file holds none. The payload is streamed into
+ * the outputs before the hash is compared: on YH_ECORRUPT (or any error)
+ * they hold whatever had been read, so pass buffers whose contents may be
+ * lost, not a live state. */
 int yh_read_checkpoint(const char *path, yh_param_var *p, int *model,
                        yh_fk_params *fk, uint8_t *mask, long long *step,
                        float *u, float *v, float *w);

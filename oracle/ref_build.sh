@@ -5,13 +5,19 @@
 #   oracle/_ref/libref_host.so      (x86 host code of the same sources, for
 #                                    CPU checks of solve_matrix and
 #                                    parameterSetup in this container)
-# Needs the reference sources (YH_REFERENCE, default /root/reference);
-# writes only into oracle/_ref/. Nothing of the reference is copied.
+# Needs the reference sources (YH_REFERENCE, default: where this build
+# mounts them); writes only into oracle/_ref/. Nothing of the reference is
+# copied. With --if-present it exits 0 without building when the sources
+# are not there (the GPU machine, which uses the prebuilt cubin).
 set -e
 REF=${YH_REFERENCE:-/root/reference}
 here=$(cd "$(dirname "$0")" && pwd)
 out="$here/_ref"
-[ -d "$REF" ] || { echo "reference sources not found at $REF" >&2; exit 1; }
+if [ ! -d "$REF" ]; then
+  [ "$1" = "--if-present" ] && exit 0
+  echo "reference sources not found at $REF (set YH_REFERENCE)" >&2
+  exit 1
+fi
 mkdir -p "$out/obj"
 ARCH="-gencode arch=compute_103a,code=sm_103a"
 # the __constant__ definitions of main.cu:40-51 and the globals the kernel

@@ -55,7 +55,7 @@ def test_compat_exports_the_reference_host_symbols():
 def test_struct_sizes_match_ctypes():
     lib = load()
     for name, ct in [("yh_param_var", A.ParamVar), ("yh_fk_params", A.FKParams),
-                     ("yh_tip", A.Tip), ("yh_fields", A.Fields),
+                     ("yh_tip", A.Tip), ("yh_fields", A.Fields), ("yh_fields64", A.Fields64),
                      ("yh_sym_state", A.SymState), ("yh_stim", A.Stim),
                      ("yh_batch_stim", A.BatchStim),
                      ("yh_checkpoint_header", A.CheckpointHeader)]:

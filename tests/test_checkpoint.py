@@ -189,3 +189,40 @@ def test_same_problem_is_the_load_rule(tmp_path):
     assert not ck.same_problem(c, p, A.YH_MODEL_FK3V, fk, m2)
     assert not ck.same_problem(c, p, A.YH_MODEL_FK3V, fk, None)
     assert not ck.same_problem(c, p, A.YH_MODEL_REF2V, fk, m)
+
+
+@pytest.mark.parametrize("field", ["nx", "ny", "gateDiff", "rx", "ry", "rscale",
+                                   "dt", "tc", "mu", "alpha", "eps", "delta",
+                                   "gamma", "beta", "theta"])
+def test_same_problem_covers_every_step_coefficient(field):
+    """Every input of the step coefficients decides whether a checkpoint
+    belongs to a handle (yh_checkpoint_same_problem, the C rule the single
+    grid and the batch both use)."""
+    lib = load()
+    p, fk, _, _ = _case(A.YH_MODEL_FK3V)
+    q = p.copy()
+    v = getattr(q, field)
+    setattr(q, field, (not v) if isinstance(v, bool) else v + 1)
+    same = lambda a, b: lib.yh_checkpoint_same_problem(
+        C.byref(a), A.YH_MODEL_FK3V, C.byref(fk), C.byref(b),
+        A.YH_MODEL_FK3V, C.byref(fk))
+    assert same(p, p) == 1
+    assert same(p, q) == 0
+
+
+def test_write_replaces_the_file_only_when_complete(tmp_path):
+    """A save goes to path.tmp and is renamed over path: a failed write
+    leaves the earlier file in place and no temporary behind."""
+    p, fk, fields, m = _case(A.YH_MODEL_FK3V)
+    path = tmp_path / "s.yhck"
+    ck.write(path, p, A.YH_MODEL_FK3V, fk, 3, *fields, mask=m)
+    good = path.read_bytes()
+    # a directory in place of the temporary file makes the write fail
+    (tmp_path / "s.yhck.tmp").mkdir()
+    with pytest.raises(YolohtliError):
+        ck.write(path, p, A.YH_MODEL_FK3V, fk, 4, *fields, mask=m)
+    assert path.read_bytes() == good
+    (tmp_path / "s.yhck.tmp").rmdir()
+    ck.write(path, p, A.YH_MODEL_FK3V, fk, 4, *fields, mask=m)
+    assert ck.read(path).step == 4
+    assert sorted(x.name for x in tmp_path.iterdir()) == ["s.yhck"]

@@ -108,3 +108,38 @@ def test_ref2v_with_diffusing_v_stays_at_one_step_per_launch():
     m2 = Monodomain(q, A.YH_MODEL_REF2V, None)
     m2.set_time_block(6)
     assert m2.time_block() == 6
+
+
+@pytest.fixture(scope="module")
+def reentry_state():
+    """The 512^2 re-entry of the symmetry-reduced workload's start protocol
+    (S1 at t = 0, S2 on the lower-left quadrant at 430 ms) at 1000 ms,
+    where spiral tips are in the tissue."""
+    wl = W.fk_sr_512()
+    m = Monodomain(wl.p, wl.model, wl.fk)
+    m.set_state(*wl.state0())
+    m.run(wl.nsteps, wl.stims)
+    st = m.get_state()
+    m.close()
+    return wl, st
+
+
+@pytest.mark.parametrize("k", [2, 4])
+@pytest.mark.parametrize("nsteps", [40, 41, 129])
+def test_tips_after_a_blocked_run_use_the_previous_level(reentry_state, k,
+                                                         nsteps):
+    """yh_track_tips compares the state with the u level one step back,
+    whatever the engine: a blocked run takes its last step on its own."""
+    wl, st = reentry_state
+    got = []
+    for kk in (1, k):
+        m = Monodomain(wl.p, wl.model, wl.fk)
+        m.set_state(*st)
+        m.set_time_block(kk)
+        m.run(nsteps)
+        m.track_tips()
+        got.append(m.get_tips())
+        m.close()
+    assert len(got[0]) > 0
+    assert len(got[0]) == len(got[1])
+    assert np.array_equal(got[0][:, :2], got[1][:, :2])

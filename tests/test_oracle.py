@@ -120,6 +120,30 @@ def test_fp32_transcription_tracks_fp64():
     assert np.abs(a[0] - b[0]).max() < 1e-5
 
 
+def test_fk3v_switch_sensitivity():
+    """The FK3V discrete map amplifies a tiny change of the state once
+    fronts move: H(u - u_c) and H(u - u_v) switch the gate rates (v by
+    dt/tau_v+ = 0.015 in one step), so a cell whose u lands on the other
+    side of u_c a step earlier shifts its front. In FP64 a 1e-10 change of
+    the spiral protocol's initial u (256^2) stays ~1e-10 for hundreds of
+    steps and exceeds 1e-6 relative L2 by step 2000: the growth that FP32
+    rounding (~1e-7 per step) meets far sooner. A tolerance of 1e-5 after
+    N steps therefore holds only for N of a few hundred with FP32 fields."""
+    from yolohtli_gb300 import workloads as W
+    wl = W.fk_spiral_256(nsteps=2000)
+    s0 = [x.astype(np.float64) for x in wl.state0()]
+    s1 = [x.copy() for x in s0]
+    s1[0] = s1[0] + 1e-10 * np.random.default_rng(5).standard_normal(wl.cells)
+    a = O.run(wl.p, wl.model, wl.fk, s0, 300, wl.stims)
+    b = O.run(wl.p, wl.model, wl.fk, s1, 300, wl.stims)
+    early = np.linalg.norm(b[0] - a[0]) / np.linalg.norm(a[0])
+    a = O.run(wl.p, wl.model, wl.fk, a, 1700, wl.stims, step0=300)
+    b = O.run(wl.p, wl.model, wl.fk, b, 1700, wl.stims, step0=300)
+    late = np.linalg.norm(b[0] - a[0]) / np.linalg.norm(a[0])
+    assert early < 1e-9
+    assert late > 1e-6
+
+
 # ---------------------------------------------------------------- SR pieces
 
 def test_bfecc_translates_a_gaussian_at_second_order():

@@ -137,12 +137,17 @@ class Fields(C.Structure):
     _fields_ = [("u", C.c_void_p), ("v", C.c_void_p), ("w", C.c_void_p)]
 
 
+class Fields64(C.Structure):
+    """yh_fields64: FP64 device pointers u, v, w."""
+    _fields_ = [("u", C.c_void_p), ("v", C.c_void_p), ("w", C.c_void_p)]
+
+
 class SymState(C.Structure):
     _fields_ = [("c", C.c_double * 3), ("phi", C.c_double * 3),
                 ("c_adv", C.c_double * 3), ("phi_adv", C.c_double * 3),
                 ("integrals", C.c_double * 12), ("centre", C.c_float * 2),
                 ("step", C.c_int), ("status", C.c_int), ("ntips", C.c_int),
-                ("pad_", C.c_int)]
+                ("nsingular", C.c_int)]
 
 
 class Stim(C.Structure):

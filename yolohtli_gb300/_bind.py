@@ -45,6 +45,12 @@ SIGNATURES = {
                                    _v, A.Fields, A.Fields, _v]),
     "yh_sym_advance": (_i, [_P(A.ParamVar), _v, _v]),
     "yh_stimulate_box": (_i, [_P(A.ParamVar), _v, _v, _i, _i, _i, _i, _f, _v]),
+    "yh_reaction_diffusion_f64": (_i, [_P(A.ParamVar), _i, _P(A.FKParams),
+                                       A.Fields64, A.Fields64, A.Fields64, _v,
+                                       _v]),
+    "yh_spiral_tip_f64": (_i, [_P(A.ParamVar), _v, _v, _d, _v, _v, _i, _v, _v]),
+    "yh_stimulate_box_f64": (_i, [_P(A.ParamVar), _v, _v, _i, _i, _i, _i, _d,
+                                  _v]),
     # solver handle
     "yh_create": (_i, [_P(A.ParamVar), _i, _P(A.FKParams), _v, _v, _P(_v)]),
     "yh_destroy": (_i, [_v]),
@@ -69,6 +75,8 @@ SIGNATURES = {
     "yh_check_finite": (_i, [_v, _P(C.c_longlong)]),
     "yh_save_checkpoint": (_i, [_v, C.c_char_p]),
     "yh_load_checkpoint": (_i, [_v, C.c_char_p]),
+    "yh_checkpoint_same_problem": (_i, [_P(A.ParamVar), _i, _P(A.FKParams),
+                                        _P(A.ParamVar), _i, _P(A.FKParams)]),
     # batched solver
     "yh_batch_create": (_i, [_i, _P(A.ParamVar), _P(A.FKParams), _P(_v), _v,
                              _P(_v)]),

@@ -120,15 +120,29 @@ class Batch:
 
     def save_checkpoint(self, directory):
         """One checkpoint file per instance (yolohtli_gb300.checkpoint), all
-        at the batch's step, in `directory` (created if missing)."""
+        at the batch's step, in `directory`. The files go to a fresh
+        directory `directory`.tmp first; only when all of them are written
+        does it replace `directory` (the old one is moved to `directory`.old
+        and removed after the swap). An interrupted save leaves the previous
+        checkpoint in `directory`, or, inside the swap, in `directory`.old,
+        which load_checkpoint falls back to."""
         import os
+        import shutil
         from . import checkpoint as ck
-        os.makedirs(str(directory), exist_ok=True)
+        d = os.path.normpath(str(directory))
+        tmp, old = d + ".tmp", d + ".old"
+        shutil.rmtree(tmp, ignore_errors=True)
+        os.makedirs(tmp)
         step = self.step_count()
         for k in range(self.count):
-            ck.write(self.checkpoint_path(directory, k), self.params[k],
+            ck.write(self.checkpoint_path(tmp, k), self.params[k],
                      A.YH_MODEL_FK3V, self.fks[k], step, *self.get_state(k),
                      mask=self._masks[k])
+        if os.path.exists(d):
+            shutil.rmtree(old, ignore_errors=True)
+            os.rename(d, old)
+        os.rename(tmp, d)
+        shutil.rmtree(old, ignore_errors=True)
 
     def load_checkpoint(self, directory):
         """Restores every instance's state and the step from the files of
@@ -136,14 +150,17 @@ class Batch:
         file raises YH_ECORRUPT, another problem (an instance's grid, step
         coefficients, FK3V parameters or mask) or files at different steps
         raise YH_EINVAL, and the batch is left as it was."""
+        import os
         from . import checkpoint as ck
-        got = [ck.read(self.checkpoint_path(directory, k))
-               for k in range(self.count)]
+        d = os.path.normpath(str(directory))
+        if not os.path.exists(d) and os.path.exists(d + ".old"):
+            d = d + ".old"  # a save interrupted inside its directory swap
+        got = [ck.read(self.checkpoint_path(d, k)) for k in range(self.count)]
         for k, c in enumerate(got):
             if not ck.same_problem(c, self.params[k], A.YH_MODEL_FK3V,
                                    self.fks[k], self._masks[k]):
                 check("yh_batch_load_checkpoint", A.YH_EINVAL)
-        if len({c.step for c in got}) != 1:
+        if len({c.step for c in got}) != 1 or not 0 <= got[0].step <= 2**31 - 1:
             check("yh_batch_load_checkpoint", A.YH_EINVAL)
         for k, c in enumerate(got):
             self.set_state(k, *c.fields)

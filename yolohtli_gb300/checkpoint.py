@@ -74,20 +74,15 @@ def read(path):
 
 # The parameters the step's coefficients are made of: the fields that
 # yh_load_checkpoint compares (make_step_coeffs in csrc/yh_api.cu).
-STEP_FIELDS = ("nx", "ny", "gateDiff", "rx", "ry", "rscale", "dt", "tc", "mu",
-               "alpha", "eps", "delta", "gamma", "beta", "theta")
-
-
 def same_problem(ckpt, p, model, fk, mask):
     """True when checkpoint `ckpt` belongs to the problem (p, model, fk,
-    mask): the rule of yh_load_checkpoint, restated for callers that keep
-    the parameters on the host (the batched solver)."""
-    if ckpt.model != model:
-        return False
-    if any(getattr(ckpt.p, f) != getattr(p, f) for f in STEP_FIELDS):
-        return False
-    if model == A.YH_MODEL_FK3V and any(
-            getattr(ckpt.fk, f) != getattr(fk, f) for f in A.FK_NAMES):
+    mask): yh_checkpoint_same_problem (the rule of yh_load_checkpoint) and
+    the same tissue cells, for callers that keep the parameters on the host
+    (the batched solver)."""
+    fk = fk if fk is not None else A.FKParams()
+    if not load().yh_checkpoint_same_problem(
+            C.byref(ckpt.p), int(ckpt.model), C.byref(ckpt.fk), C.byref(p),
+            int(model), C.byref(fk)):
         return False
     if (ckpt.mask is None) != (mask is None):
         return False

@@ -233,6 +233,7 @@ extern "C" size_t yh_sizeof(const char *type_name) {
   if (!strcmp(type_name, "yh_fk_params")) return sizeof(yh_fk_params);
   if (!strcmp(type_name, "yh_tip")) return sizeof(yh_tip);
   if (!strcmp(type_name, "yh_fields")) return sizeof(yh_fields);
+  if (!strcmp(type_name, "yh_fields64")) return sizeof(yh_fields64);
   if (!strcmp(type_name, "yh_sym_state")) return sizeof(yh_sym_state);
   if (!strcmp(type_name, "yh_stim")) return sizeof(yh_stim);
   if (!strcmp(type_name, "yh_batch_stim")) return sizeof(yh_batch_stim);
@@ -397,6 +398,58 @@ extern "C" int yh_stimulate_box(const yh_param_var *p, float *u,
                                 int j1, float value, void *stream) {
   if (!p || !u) return YH_EINVAL;
   return cuda_status(launch_stimulate<float>(
+      u, p->solidSwitch ? solid : nullptr, p->nx, p->ny, i0, j0, i1, j1, value,
+      (cudaStream_t)stream));
+}
+
+// FP64 instances of the operators above (the same kernel templates).
+static bool fields64_ok(const yh_fields64 &x, int model) {
+  return x.u && x.v && (model != YH_MODEL_FK3V || x.w);
+}
+
+extern "C" int yh_reaction_diffusion_f64(const yh_param_var *p, int model,
+                                         const yh_fk_params *fk,
+                                         yh_fields64 out, yh_fields64 in,
+                                         yh_fields64 vel_tan,
+                                         const uint8_t *solid, void *stream) {
+  int st = check_params(p, model, fk);
+  if (st) return st;
+  if (!fields64_ok(out, model) || !fields64_ok(in, model)) return YH_EINVAL;
+  if (vel_tan.u && !fields64_ok(vel_tan, model)) return YH_EINVAL;
+  if (p->solidSwitch && !solid) return YH_EINVAL;
+  const StepCoeffs<double> a = make_step_coeffs<double>(*p, model, fk);
+  return cuda_status(launch_rd_step<double>(
+      a, make_fld<double>(in.u, in.v, in.w),
+      make_fld<double>(out.u, out.v, out.w),
+      make_fld<double>(vel_tan.u, vel_tan.v, vel_tan.w),
+      p->solidSwitch ? solid : nullptr, (cudaStream_t)stream, nullptr));
+}
+
+extern "C" int yh_spiral_tip_f64(const yh_param_var *p, const double *g_past,
+                                 const double *g_present,
+                                 double physical_time, int *tip_count,
+                                 yh_tip *tip_vector, int capacity,
+                                 const uint8_t *solid, void *stream) {
+  if (!p || !g_past || !g_present || !tip_count || !tip_vector || capacity < 0)
+    return YH_EINVAL;
+  if (p->nx < 5 || p->ny < 5) return YH_EINVAL;
+  if (p->tipAlgorithm != 1 && p->tipAlgorithm != 2) return YH_EUNSUPPORTED;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(tip_count, 0, sizeof(int), s);
+  if (e != cudaSuccess) return cuda_status(e);
+  (void)solid;  // the hole branch uses a disc, not the mask
+  return cuda_status(launch_tips<double>(*p, g_past, g_present,
+                                         p->solidSwitch, physical_time,
+                                         tip_count, tip_vector, capacity,
+                                         nullptr, nullptr, s));
+}
+
+extern "C" int yh_stimulate_box_f64(const yh_param_var *p, double *u,
+                                    const uint8_t *solid, int i0, int j0,
+                                    int i1, int j1, double value,
+                                    void *stream) {
+  if (!p || !u) return YH_EINVAL;
+  return cuda_status(launch_stimulate<double>(
       u, p->solidSwitch ? solid : nullptr, p->nx, p->ny, i0, j0, i1, j1, value,
       (cudaStream_t)stream));
 }

@@ -19,6 +19,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #include <string>
 #include <vector>
@@ -510,12 +511,19 @@ extern "C" int yh_write_checkpoint(const char *path, const yh_param_var *p,
   h.hash = hash.h;
   uint8_t b[kHeaderBytes];
   pack(h, b);
-  FILE *o = fopen(path, "wb");
+  // Written to path.tmp, flushed to the disk, then renamed over path: an
+  // interrupted save (a crash, a kill, a full disk) leaves the previous
+  // checkpoint at `path` intact.
+  std::string tmp = std::string(path) + ".tmp";
+  FILE *o = fopen(tmp.c_str(), "wb");
   if (!o) return YH_EINVAL;
   bool ok = fwrite(b, 1, kHeaderBytes, o) == kHeaderBytes;
   for (const Part &q : parts)
     if (ok && q.bytes) ok = fwrite(q.data, 1, q.bytes, o) == q.bytes;
+  ok = ok && fflush(o) == 0 && fsync(fileno(o)) == 0;
   ok = (fclose(o) == 0) && ok;
+  ok = ok && rename(tmp.c_str(), path) == 0;
+  if (!ok) remove(tmp.c_str());
   return ok ? YH_OK : YH_EINVAL;
 }
 

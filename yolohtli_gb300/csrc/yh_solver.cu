@@ -59,6 +59,7 @@ struct yh_solver {
   float *adv_f = nullptr;
   int step = 0;
   int sr_step = 0;
+  int sr_nsingular = 0;  // the device state's nsingular at the last read
   int time_block = 1;
   bool sr_ready = false;
   bool frozen = false;
@@ -566,7 +567,15 @@ extern "C" int yh_run(yh_solver *h, int nsteps, const yh_stim *stims,
       ++k;
     }
     const int next = k < ev.size() ? ev[k].step : end;
-    int rc = run_plain(h, next - h->step);
+    int rc;
+    if (next == end && h->time_block > 1 && end - h->step >= 2) {
+      // the run's last step on its own: a launch of k steps leaves the u
+      // level k steps back in h->nxt, yh_track_tips needs the previous one
+      rc = run_plain(h, end - 1 - h->step);
+      if (!rc) rc = run_plain(h, 1);
+    } else {
+      rc = run_plain(h, next - h->step);
+    }
     if (rc) return rc;
   }
   return st(cudaGetLastError());
@@ -673,6 +682,7 @@ extern "C" int yh_sr_begin(yh_solver *h, int template_mode, const float *tu,
   if (e != cudaSuccess) return st(e);
   h->frozen = frozen;
   h->sr_step = 0;
+  h->sr_nsingular = 0;
   h->sr_ready = true;
   for (auto &g : h->sr) free_graph(g);
   return YH_OK;
@@ -744,7 +754,19 @@ extern "C" int yh_sr_step(yh_solver *h, int nsteps) {
     h->sr_step += 1;
     h->step += 1;
   }
-  return st(cudaGetLastError());
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && nsteps > 0) {
+    // the singular-solve count of the device state, read once per call
+    int ns = 0;
+    e = cudaMemcpyAsync(&ns, &h->sym->nsingular, sizeof(int),
+                        cudaMemcpyDeviceToHost, h->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+    if (e == cudaSuccess && ns != h->sr_nsingular) {
+      h->sr_nsingular = ns;
+      return YH_ESINGULAR;
+    }
+  }
+  return st(e);
 }
 
 extern "C" int yh_get_sym(yh_solver *h, yh_sym_state *out) {
@@ -840,6 +862,17 @@ static bool same_fk(const yh_fk_params &a, const yh_fk_params &b) {
          a.tau_v1_minus == b.tau_v1_minus && a.tau_v2_minus == b.tau_v2_minus &&
          a.tau_w_plus == b.tau_w_plus && a.tau_w_minus == b.tau_w_minus &&
          a.u_c == b.u_c && a.u_v == b.u_v && a.u_csi == b.u_csi && a.k == b.k;
+}
+
+extern "C" int yh_checkpoint_same_problem(const yh_param_var *a, int model_a,
+                                          const yh_fk_params *fk_a,
+                                          const yh_param_var *b, int model_b,
+                                          const yh_fk_params *fk_b) {
+  if (!a || !b) return 0;
+  if (model_a != model_b || !same_step(*a, *b)) return 0;
+  if (model_a == YH_MODEL_FK3V && (!fk_a || !fk_b || !same_fk(*fk_a, *fk_b)))
+    return 0;
+  return 1;
 }
 
 extern "C" int yh_load_checkpoint(yh_solver *h, const char *path) {

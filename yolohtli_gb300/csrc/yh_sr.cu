@@ -773,6 +773,7 @@ __global__ void __launch_bounds__(kPhaseBX *kPhaseBY)
     double c[3];
     const int stt = solve3_cofactor(I, s_cs, s_sn, c);
     sym->status = stt;
+    if (stt != YH_OK) sym->nsingular += 1;
     for (int kk = 0; kk < 3; ++kk) {
       const double ck = stt == YH_OK ? c[kk] : s_cold[kk];
       s_c[kk] = ck;

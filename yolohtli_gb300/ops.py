@@ -158,3 +158,36 @@ def sym_to_tensor(s, device="cuda"):
     import torch
     buf = (C.c_uint8 * C.sizeof(s)).from_buffer_copy(s)
     return torch.tensor(list(buf), dtype=torch.uint8, device=device)
+
+
+def fields64(ts):
+    """yh_fields64 from a list of 2 or 3 FP64 tensors (or None)."""
+    f = A.Fields64()
+    if ts is None:
+        return f
+    f.u = _p(ts[0])
+    f.v = _p(ts[1])
+    f.w = _p(ts[2]) if len(ts) > 2 else None
+    return f
+
+
+def reaction_diffusion_f64(p, model, fk, out, inp, vel_tan=None, solid=None):
+    """reaction_diffusion on FP64 tensors: the same kernel in double."""
+    return check("yh_reaction_diffusion_f64", load().yh_reaction_diffusion_f64(
+        C.byref(p), model, C.byref(fk) if fk is not None else None,
+        fields64(out), fields64(inp), fields64(vel_tan), _p(solid),
+        _stream()))
+
+
+def spiral_tip_f64(p, past_u, present_u, tip_count, tip_vec, capacity,
+                   physical_time=0.0, solid=None):
+    """spiral_tip on FP64 u levels (tips are FP32 yh_tip records)."""
+    return check("yh_spiral_tip_f64", load().yh_spiral_tip_f64(
+        C.byref(p), _p(past_u), _p(present_u), C.c_double(physical_time),
+        _p(tip_count), _p(tip_vec), capacity, _p(solid), _stream()))
+
+
+def stimulate_box_f64(p, u, i0, j0, i1, j1, value, solid=None):
+    return check("yh_stimulate_box_f64", load().yh_stimulate_box_f64(
+        C.byref(p), _p(u), _p(solid), i0, j0, i1, j1, C.c_double(value),
+        _stream()))
