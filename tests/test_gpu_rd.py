@@ -85,7 +85,9 @@ def test_handle_protocol_matches_oracle_and_is_deterministic():
     ref = O.run(wl.p, wl.model, wl.fk, wl.state0(), wl.nsteps, wl.stims)
     err = rel_l2(res[0][0], ref[0])
     print("FK3V 128^2 x 1500 steps: rel L2(u) FP32 vs FP64 oracle = %.3e" % err)
-    assert err < 1e-4
+    # measured 6.1e-6 (the wave has left the tissue; while fronts move the
+    # FK3V map amplifies FP32 rounding, tests/test_gpu_parity_configs.py)
+    assert err < 1e-5
 
 
 @pytest.mark.parametrize("nsteps", [1, 63, 64, 200])

@@ -193,3 +193,74 @@ def test_reference_bfecc_fixed_point_matches_product():
     torch.cuda.synchronize()
     assert max_abs(host(out[0]), outs[3]) < 2e-6
     assert max_abs(host(out[1]), host(gout[1])) < 2e-6
+
+
+def test_reference_long_run_and_tip_trajectory():
+    """REF2V, the reference's model, from its own cross-field initial
+    condition (main.cu:604-618) on 256^2 for 20,000 steps: the FP32 product
+    (solver handle) against the reference's own FP64 kernels run headless,
+    rel L2(u) after N steps, and the plain-mode tip sets every sampleIt =
+    40 steps (main.cu:156,961-964; the reference's spiralTip_kernel on its
+    own two u levels) within 0.1 cell."""
+    import torch
+    from scipy.optimize import linear_sum_assignment
+    n, nsteps, every = 256, 20000, 40
+    marks = (1000, 5000, 10000, 20000)
+    p = cross_params(n)
+    st = list(W.ref2v_cross(n, n))
+    a = [dev(x, torch.float64) for x in st]
+    b = [torch.zeros_like(a[0]) for _ in range(2)]
+    J = [torch.zeros_like(a[0]) for _ in range(2)]
+    vt = [torch.zeros_like(a[0]) for _ in range(2)]
+    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    vec = torch.zeros(5 * 4096, dtype=torch.float32, device="cuda")
+    plot = torch.zeros(n * n, dtype=torch.uint8, device="cuda")
+    m = Monodomain(p, A.YH_MODEL_REF2V, None)
+    m.set_state(*st)
+    R.set_params(p)
+    errs, tip_d, ntips, samples_ok, nsamples, matched, extra = {}, 0.0, 0, 0, 0, 0, 0
+    shown = 0
+    for step in range(every, nsteps + 1, every):
+        for _ in range(every):
+            R.rd(p, b, a, J, vt)
+            a, b = b, a
+        cnt.zero_()
+        R.tip(p, b[0], a[0], plot, cnt, vec, p.dt * step)
+        R.sync()
+        nr = int(cnt.item())
+        ref = host(vec)[: 5 * nr].reshape(nr, 5)
+        m.run(every)
+        m.track_tips()
+        got = m.get_tips()
+        nsamples += 1
+        ntips += nr
+        mk = 0
+        if nr and len(got):
+            d = np.hypot(got[:, None, 0] - ref[None, :, 0],
+                         got[:, None, 1] - ref[None, :, 1])
+            r, c = linear_sum_assignment(d)
+            mk = int((d[r, c] <= 0.1).sum())
+            tip_d = max(tip_d, float(d[r, c][d[r, c] <= 0.1].max(initial=0.0)))
+        matched += mk
+        extra += len(got) - mk
+        if mk == nr == len(got):
+            samples_ok += 1
+        elif shown < 4:
+            shown += 1
+            print("  N=%d product %s | reference %s" % (
+                step, np.round(got[:, :2], 3).tolist(),
+                np.round(ref[:, :2], 3).tolist()))
+        if step in marks:
+            errs[step] = rel_l2(m.get_state()[0], host(a[0]))
+    m.close()
+    print("REF2V 256^2 FP32 product vs the reference's FP64 kernels: rel L2(u)",
+          {k: "%.2e" % v for k, v in errs.items()},
+          "; tips: %d of %d samples with equal sets, %d of %d reference tips "
+          "matched within 0.1 cell (largest distance %.2e), %d extra" % (
+              samples_ok, nsamples, matched, ntips, tip_d, extra))
+    assert ntips > 0
+    # 1e-5 through 10,000 steps (measured 2e-7 .. 1.2e-6); 2.5e-5 at 20,000
+    for k in marks[:3]:
+        assert errs[k] < 1e-5, (k, errs[k])
+    assert errs[20000] < 1e-4
+    assert matched >= 0.95 * ntips

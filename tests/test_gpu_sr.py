@@ -247,9 +247,11 @@ def test_sr_sequence_matches_oracle():
     assert sg.step == nsr and r["step"] == nsr
     assert sg.status == A.YH_OK
     assert np.allclose(list(sg.centre), r["centre"], atol=1e-3)
-    assert np.allclose(list(sg.c), r["c"], rtol=1e-3, atol=1e-4 * np.abs(r["c"]).max())
-    assert np.allclose(list(sg.phi), r["phi"], rtol=1e-3, atol=1e-6)
-    assert rel_l2(got[0], r["state"][0]) < 1e-4
+    # measured: c and phi within 8e-5 relative (the smallest component),
+    # rel L2(u) 4.7e-7
+    assert np.allclose(list(sg.c), r["c"], rtol=3e-4, atol=1e-6 * np.abs(r["c"]).max())
+    assert np.allclose(list(sg.phi), r["phi"], rtol=3e-4, atol=1e-9)
+    assert rel_l2(got[0], r["state"][0]) < 2e-6
 
 
 def test_sr_frozen_template_runs_and_stays_finite():
@@ -267,3 +269,97 @@ def test_sr_frozen_template_runs_and_stays_finite():
     got = m.get_state()
     assert s.step == 37
     assert np.all(np.isfinite(got[0])) and np.all(np.isfinite(list(s.c)))
+
+
+def sr_spiral_case(n=128, L=3.0, radius=30):
+    """A REF2V spiral (ref2v_spiral) with the symmetry-reduction parameters:
+    dt halved as the reference does in SR mode (main.cu:148), a disc of
+    `radius` cells started at the spiral's tip."""
+    p, st = ref2v_spiral(n, L=L)
+    p.dt = 0.5 * p.dt
+    A.param_derive(p)
+    p.tipOffsetX = p.tipOffsetY = radius
+    m = Monodomain(p, A.YH_MODEL_REF2V, None)
+    m.set_state(*st)
+    m.run(1)
+    m.track_tips()
+    tips = m.get_tips()
+    m.close()
+    assert len(tips) >= 1
+    c = np.array([n / 2, n / 2])
+    k = int(np.argmin(np.hypot(tips[:, 0] - c[0], tips[:, 1] - c[1])))
+    p.tipx, p.tipy = float(tips[k, 0]), float(tips[k, 1])
+    return p, st
+
+
+def test_sr_frozen_template_trajectory_matches_oracle():
+    """BASELINE-style symmetry reduction (template frozen at the start
+    state) over 2,000 SR steps on 128^2: the FP32 product's c, phi and u
+    against the FP64 oracle's SR sequence (main.cu:894-954 with a fixed
+    template) at several step counts."""
+    p, st = sr_spiral_case()
+    m = Monodomain(p, A.YH_MODEL_REF2V, None)
+    m.set_state(*st)
+    m.sr_begin(A.YH_TEMPLATE_FROZEN, template=st)
+    st64 = [x.astype(np.float64) for x in st]
+    orc = O.SR(p, A.YH_MODEL_REF2V, None, st64,
+               template_mode=A.YH_TEMPLATE_FROZEN, template=st64)
+    done, rows = 0, []
+    for n in (250, 1000, 2000):
+        m.sr_step(n - done)
+        orc.step(n - done)
+        done = n
+        sg, r, got = m.get_sym(), orc.get(), m.get_state()
+        cs = np.abs(r["c"]).max()
+        rows.append((n, float(np.abs(np.array(sg.c) - r["c"]).max() / cs),
+                     float(np.abs(np.array(sg.phi) - r["phi"]).max()),
+                     rel_l2(got[0], r["state"][0]), sg.ntips, r["ntips"]))
+        assert sg.status == A.YH_OK and sg.nsingular == 0
+    print("frozen-template SR, FP32 vs FP64 oracle (N, max|dc|/max|c|, "
+          "max|dphi|, rel L2(u), tips gpu/oracle):", rows)
+    for n, dc, dphi, du, nt, nto in rows:
+        assert nt >= 1 and nto >= 1
+        assert dc <= 1e-3 and dphi <= 1e-3 and du <= 1e-4, (n, dc, dphi, du)
+
+
+def test_sr_tips_reconstruct_the_lab_frame_trajectory():
+    """The reconstruction of the reference's DATA/processSymmetry.m:80-115:
+    the symmetry-reduced tip mapped back to the lab frame through phi,
+    x = -phix + xt cos(-phit) - yt sin(-phit),
+    y = -phiy + xt sin(-phit) + yt cos(-phit)   (physical units, corner
+    origin), equals the plain-mode tip trajectory of the same start state
+    and time step up to a constant offset."""
+    p, st = sr_spiral_case()
+    every, nsamp = 100, 30
+    plain = Monodomain(p, A.YH_MODEL_REF2V, None)
+    plain.set_state(*st)
+    sr = Monodomain(p, A.YH_MODEL_REF2V, None)
+    sr.set_state(*st)
+    sr.sr_begin(A.YH_TEMPLATE_FROZEN, template=st)
+    lab, rec = [], []
+    prev = np.array([p.tipx, p.tipy])
+    for _ in range(nsamp):
+        plain.run(every)
+        plain.track_tips()
+        t = plain.get_tips()
+        assert len(t) >= 1
+        k = int(np.argmin(np.hypot(t[:, 0] - prev[0], t[:, 1] - prev[1])))
+        prev = t[k, :2].astype(np.float64)
+        lab.append(prev * p.hx)
+        sr.sr_step(every)
+        s = sr.get_sym()
+        xt, yt = s.centre[0] * p.hx, s.centre[1] * p.hy
+        ph = np.array(s.phi)
+        rec.append([-ph[0] + xt * np.cos(-ph[2]) - yt * np.sin(-ph[2]),
+                    -ph[1] + xt * np.sin(-ph[2]) + yt * np.cos(-ph[2])])
+    plain.close()
+    sr.close()
+    lab, rec = np.array(lab), np.array(rec)
+    off = (lab - rec).mean(axis=0)
+    dev_cells = np.hypot(*(lab - rec - off).T) / p.hx
+    span = np.hypot(*(lab - lab.mean(axis=0)).T).max() / p.hx
+    print("reconstruction: lab-frame tip path spans %.2f cells; reconstructed "
+          "path within %.3f cells (mean %.3f) after a constant offset" % (
+              span, dev_cells.max(), dev_cells.mean()))
+    assert span > 1.0
+    assert dev_cells.max() < 0.5
