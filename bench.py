@@ -461,13 +461,13 @@ def run_batch(args):
         dist.destroy_process_group()
 
 
-def sr_start():
-    """The re-entry that seeds the symmetry-reduced workload (fk_sr_512:
-    FK3V BR fit on 512^2, S1 at 0 ms, S2 on the lower-left quadrant at
-    430 ms, 20,000 steps of 0.05 ms). Returns (p, fk, state, tips)."""
+def sr_start(tau_d=0.25):
+    """The re-entry that seeds the symmetry-reduced workload
+    (fk_sr_512(tau_d): S1 at 0 ms, the tau_d's S2, 20,000 steps of 0.05 ms
+    on 512^2). Returns (p, fk, state, tips)."""
     from yolohtli_gb300 import workloads as W
     from yolohtli_gb300.solver import Monodomain
-    wl = W.fk_sr_512(seed=0)
+    wl = W.fk_sr_512(seed=0, tau_d=tau_d)
     n = wl.p.nx
     q = wl.p.copy()
     q.tipx = q.tipy = n / 2  # tips anywhere in the tissue
@@ -481,6 +481,11 @@ def sr_start():
     st = m.get_state()
     m.close()
     return wl.p, wl.fk, st, tips
+
+
+def nearest_tip(tips, n):
+    k = int(np.argmin(np.hypot(tips[:, 0] - n / 2, tips[:, 1] - n / 2)))
+    return float(tips[k, 0]), float(tips[k, 1])
 
 
 def sr_params(p, tip, radius=160):
@@ -511,105 +516,139 @@ def sr_roofline(rate, cells):
 
 def run_sr(args):
     """The symmetry-reduced spiral: FK3V FP32 on 512^2, every step RD, tips,
-    slices, the 12 phase-condition integrals in FP64, the FP64 3x3 solve,
-    the comoving field and BFECC, all on the device. Template: the spiral at
-    1000 ms (frozen); tau_d in {0.25, 0.35, 0.45}. `value` is SR steps/s
-    at tau_d = 0.25; the template retaken every step (the reference's
-    behaviour) and the REF2V FP64 drop-in of the reference's own symbols,
-    driven in its own sequence (main.cu:894-954), are reported beside it."""
+    slices, the 12 phase-condition integrals (float-float sums, FP64 from
+    the integrals on), the FP64 3x3 solve, the comoving field and BFECC,
+    all on the device; 40,000 SR steps of dt/2 = 0.025 ms (1000 ms).
+    Template re-taken every step (the reference's behaviour); a run that
+    ends with a singular solve or without a tip has no rate. tau_d = 0.25
+    (the value) and 0.30; 0.35 and 0.45 have no re-entry on 512^2
+    (workloads.SR_PROTOCOLS). The frozen template (the start state) is run
+    beside it and reported by where its phase conditions became singular.
+    The REF2V FP64 drop-in of the reference's own symbols, driven in its
+    own sequence (main.cu:894-954), is reported beside it."""
     import torch
     from yolohtli_gb300 import _abi as A
     from yolohtli_gb300 import workloads as W
     from yolohtli_gb300.compat import Compat, sr_driver
+    from yolohtli_gb300.ops import YolohtliError
     from yolohtli_gb300.solver import Monodomain
     nsr, K = args.nsteps, args.steps
-    p, fk, st, tips = sr_start()
-    n = p.nx
-    if not len(tips):
-        raise RuntimeError("the SR start has no spiral tip")
-    q = sr_params(p, (float(tips[0, 0]), float(tips[0, 1])))
+    starts = {td: sr_start(td) for td in sorted(W.SR_PROTOCOLS)}
+    n = 512
     N = n * n
 
-    def timed(m, k, profile=False):
+    def run(m, k, profile=False):
+        """k calls of nsr SR steps; (wall s, launches, ms per call,
+        calls that saw a singular solve)."""
         torch.cuda.synchronize()
         l0 = m.launch_count()
         if profile:  # the range `ncu --profile-from-start off` captures
             torch.cuda.profiler.start()
         t0 = time.perf_counter()
-        marks = []
+        marks, sing = [], 0
         for _ in range(k):
-            m.sr_step(nsr)
+            try:
+                m.sr_step(nsr)
+            except YolohtliError as e:
+                if e.status != A.YH_ESINGULAR:
+                    raise
+                sing += 1
             m.synchronize()
             marks.append(time.perf_counter())
         wall = time.perf_counter() - t0
         if profile:
             torch.cuda.profiler.stop()
         per = [1e3 * (b - a) for a, b in zip([t0] + marks[:-1], marks)]
-        return wall, m.launch_count() - l0, per
+        return wall, m.launch_count() - l0, per, sing
 
-    rates, status, launches, clk, step_ms = {}, {}, 0, None, []
-    for tau_d in (0.25, 0.35, 0.45):
-        f = A.FKParams.from_buffer_copy(fk)
-        f.tau_d = tau_d
-        m = Monodomain(q, A.YH_MODEL_FK3V, f)
+    def handle(td, mode, stream=None):
+        p, fk, st, tips = starts[td]
+        q = sr_params(p, nearest_tip(tips, n))
+        m = Monodomain(q, A.YH_MODEL_FK3V, fk, stream=stream)
         m.set_state(*st)
-        m.sr_begin(A.YH_TEMPLATE_FROZEN, template=st)
+        m.sr_begin(mode, template=st if mode == A.YH_TEMPLATE_FROZEN else None)
+        return m, q, st, fk
+
+    runs, launches, clk, step_ms = {}, 0, None, []
+    for td in sorted(starts):
+        # warm-up on a handle of its own (graph capture), then the timed run
+        # of the whole 40,000 steps from the start state
+        m, q, st, fk = handle(td, A.YH_TEMPLATE_CURRENT)
         for _ in range(args.warmup):
-            m.sr_step(nsr // 4)
-        m.synchronize()
-        if tau_d == 0.25:
+            try:
+                m.sr_step(nsr // 4)
+            except YolohtliError:
+                pass
+        m.close()
+        m, q, st, fk = handle(td, A.YH_TEMPLATE_CURRENT)
+        if td == 0.25:
             clocks = ClockSampler(env_int("LOCAL_RANK", 0))
             clocks.start()
-        wall, nl, per = timed(m, K, profile=tau_d == 0.25)
-        if tau_d == 0.25:
+        wall, nl, per, sing = run(m, K, profile=td == 0.25)
+        if td == 0.25:
             clk = clocks.stop()
             launches = nl
             step_ms = [round(x, 2) for x in per]
         sym = m.get_sym()
-        rates[tau_d] = K * nsr / wall
-        status[tau_d] = dict(status=sym.status, c=[round(x, 6) for x in sym.c],
-                             ntips=sym.ntips)
+        ok = sing == 0 and sym.nsingular == 0 and sym.ntips >= 1
+        runs[td] = dict(rate=K * nsr / wall, valid=ok, status=sym.status,
+                        nsingular=sym.nsingular, ntips_end=sym.ntips,
+                        c=[round(x, 6) for x in sym.c],
+                        phi=[round(x, 5) for x in sym.phi],
+                        start_tips=len(starts[td][3]))
         m.close()
-    # the three tau_d runs at once, one handle and stream each: one 512^2
-    # SR run leaves most of the GPU idle (latency-bound launches)
-    streams = [torch.cuda.Stream() for _ in range(3)]
-    runs = []
-    for tau_d, sm in zip((0.25, 0.35, 0.45), streams):
-        f = A.FKParams.from_buffer_copy(fk)
-        f.tau_d = tau_d
-        m = Monodomain(q, A.YH_MODEL_FK3V, f, stream=sm.cuda_stream)
-        m.set_state(*st)
-        m.sr_begin(A.YH_TEMPLATE_FROZEN, template=st)
+    # the frozen template: SR steps in segments of 1,000 until a solve is
+    # singular (the phase conditions lose rank once the pattern leaves the
+    # template's shape)
+    frozen = {}
+    for td in sorted(starts):
+        m, q, st, fk = handle(td, A.YH_TEMPLATE_FROZEN)
+        done, first = 0, None
+        while done < K * nsr:
+            try:
+                m.sr_step(1000)
+            except YolohtliError as e:
+                if e.status != A.YH_ESINGULAR:
+                    raise
+                first = done
+                break
+            done += 1000
+        s = m.get_sym()
+        frozen[str(td)] = {"singular_within_steps": None if first is None else
+                           [first, first + 1000], "ntips": s.ntips,
+                           "nsingular": s.nsingular}
+        m.close()
+    # the tau_d runs at once, one handle and stream each
+    streams = [torch.cuda.Stream() for _ in starts]
+    hs = [handle(td, A.YH_TEMPLATE_CURRENT, sm.cuda_stream)[0]
+          for td, sm in zip(sorted(starts), streams)]
+    for m in hs:
         m.sr_step(nsr // 4)
-        runs.append(m)
-    for m in runs:
         m.synchronize()
     t0 = time.perf_counter()
     for _ in range(K):
-        for m in runs:
-            m.sr_step(nsr)
-    for m in runs:
+        for m in hs:
+            try:
+                m.sr_step(nsr)
+            except YolohtliError:
+                pass
+    for m in hs:
         m.synchronize()
-    concurrent = 3 * K * nsr / (time.perf_counter() - t0)
-    for m in runs:
+    concurrent = len(hs) * K * nsr / (time.perf_counter() - t0)
+    for m in hs:
         m.close()
-    # the template retaken every step
-    m = Monodomain(q, A.YH_MODEL_FK3V, fk)
-    m.set_state(*st)
-    m.sr_begin(A.YH_TEMPLATE_CURRENT)
-    m.sr_step(nsr // 4)
-    m.synchronize()
-    wall, _, _ = timed(m, 1)
-    current = nsr / wall
-    # end to end: the state from pinned host memory each step, the state and
-    # the drift/rotation read back at its end
+    # end to end: the state from pinned host memory, the state and the
+    # drift/rotation read back, every nsr steps
+    m, q, st, fk = handle(0.25, A.YH_TEMPLATE_CURRENT)
     hst = [torch.from_numpy(np.ascontiguousarray(x, np.float32)).pin_memory()
            for x in st]
-    m.sr_begin(A.YH_TEMPLATE_FROZEN, template=st)
     t0 = time.perf_counter()
     for _ in range(K):
         m.set_state(*[x.numpy() for x in hst])
-        m.sr_step(nsr)
+        try:
+            m.sr_step(nsr)
+        except YolohtliError:
+            pass
         m.get_state()
         m.get_sym()
     e2e = K * nsr / (time.perf_counter() - t0)
@@ -633,47 +672,57 @@ def run_sr(args):
     cpu = None
     if not args.no_cpu_baseline:
         from oracle import oracle as O
-        m0 = O.SR(q, A.YH_MODEL_FK3V, fk, st, template_mode=A.YH_TEMPLATE_FROZEN,
-                  template=st)
+        p, fk, st, tips = starts[0.25]
+        q = sr_params(p, nearest_tip(tips, n))
+        m0 = O.SR(q, A.YH_MODEL_FK3V, fk, st)
         t0 = time.perf_counter()
         ks = 0
         while time.perf_counter() - t0 < 10.0:
             m0.step(5)
             ks += 5
         cpu = {"value": round(ks / (time.perf_counter() - t0), 3),
-               "unit": "SR steps/s", "cores": 1, "kind": "port",
+               "unit": "SR steps/s", "cores": os.cpu_count() or 1,
+               "kind": "port",
                "sample": "%d SR steps of the same 512^2 FK3V case in FP64 "
-                         "(oracle/oracle.c, one thread)" % ks}
-    v = rates[0.25]
+                         "(the oracle's SR sequence, OpenMP)" % ks}
+    head = runs[0.25]
+    v = head["rate"] if head["valid"] else None
     line = {
-        "metric": "SR steps/s", "value": round(v, 2), "unit": "SR steps/s",
-        "n_gpus": 1, "steps": K, "warmup": args.warmup,
-        "ms_per_step": round(1e3 * nsr / v, 3),
+        "metric": "SR steps/s", "value": None if v is None else round(v, 2),
+        "unit": "SR steps/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
+        "ms_per_step": None if v is None else round(1e3 * nsr / v, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 state, f64 integrals and solve", "data": "synthetic",
         "config": {"workload": "fk_sr_512", "grid": [n, n], "model": "FK3V",
                    "tau_d": 0.25, "sr_steps_per_step": nsr,
-                   "sr_steps_timed": K * nsr, "template": "frozen, the "
-                   "re-entry at 1000 ms (S2 at 430 ms: at 320 ms the "
-                   "tissue is still refractory)", "start_tips": len(tips),
-                   "disc_radius_cells": 160, "dt_ms": q.dt,
+                   "sr_steps_timed": K * nsr,
+                   "template": "re-taken every step (the reference's)",
+                   "start": "the state at 1000 ms of S1 + S2 on the lower "
+                            "half at 585 ms (tau_d 0.25), on the lower-left "
+                            "quadrant at 615 ms (tau_d 0.30)",
+                   "disc_radius_cells": 160,
+                   "dt_ms": sr_params(starts[0.25][0], (0, 0)).dt,
                    "l2": "state 3 MB: L2-resident (SR steps are latency-bound)",
                    "parallelism": "replicas x1"},
-        "gcell_steps_per_s": round(v * N / 1e9, 3),
+        "valid": head["valid"],
+        "gcell_steps_per_s": None if v is None else round(v * N / 1e9, 3),
         "step_ms": step_ms,
-        "tau_d_sweep": {str(k): round(x, 2) for k, x in rates.items()},
-        "sym": {str(k): x for k, x in status.items()},
-        "current_template": {"value": round(current, 2), "unit": "SR steps/s"},
-        "three_runs_concurrent": {"value": round(concurrent, 2),
-                                  "unit": "SR steps/s (sum of the 3 tau_d runs)",
-                                  "note": "one handle and stream per run"},
+        "tau_d_runs": {str(k): x for k, x in runs.items()},
+        "tau_d_without_reentry": {
+            "0.35": "no S2 time (180-705 ms, quadrant or half) sustains "
+                    "activity past 850 ms on 512^2",
+            "0.45": "as 0.35"},
+        "frozen_template": frozen,
+        "tau_d_concurrent": {"value": round(concurrent, 2),
+                             "unit": "SR steps/s (sum of the tau_d runs)",
+                             "note": "one handle and stream per run"},
         "compat_fp64_reference_sequence": {
             "value": round(compat_rate, 2), "unit": "SR steps/s",
             "model": "REF2V FP64",
             "sequence": "main.cu:894-954 through the drop-in symbols from "
                         "Python: 12 integral read-backs and a host solve "
                         "per step, as the reference"},
-        "roofline": sr_roofline(v, N),
+        "roofline": None if v is None else sr_roofline(v, N),
         "cpu_baseline": cpu,
         "e2e": {"value": round(e2e, 2), "unit": "SR steps/s",
                 "h2d_bytes_per_step": 3 * 4 * N,
@@ -687,9 +736,10 @@ def run_sr_reference(args):
     """--impl reference for the symmetry-reduced workload: the reference's
     SR step sequence (main.cu:894-954) as the CPU restatement runs it (the
     oracle port, FP64, OpenMP over the host cores) on this arm's case: the
-    fk_sr_512 start (built on the CPU too), the same disc, the frozen
-    template. The reference's own GPU kernels in their sequence (REF2V
-    FP64, the model it has) are reported beside it as reference_gpu."""
+    fk_sr_512 start at tau_d = 0.25 (built on the CPU too), the same disc,
+    the template re-taken every step. The reference's own GPU kernels in
+    their sequence (REF2V FP64, the model it has) are reported beside it
+    as reference_gpu."""
     if env_int("RANK", 0) != 0:
         return
     from oracle import oracle as O
@@ -706,11 +756,10 @@ def run_sr_reference(args):
     whole.tipx = whole.tipy = n / 2
     whole.tipOffsetX = whole.tipOffsetY = n // 2
     tips = O.tips(whole, pre[0], st[0])
-    tip = (float(tips[0, 0]), float(tips[0, 1])) if len(tips) else (n / 2, n / 2)
+    tip = nearest_tip(tips, n) if len(tips) else (n / 2, n / 2)
     q = sr_params(wl.p, tip)
     start_s = time.perf_counter() - t_start
-    sr = O.SR(q, A.YH_MODEL_FK3V, wl.fk, st,
-              template_mode=A.YH_TEMPLATE_FROZEN, template=st)
+    sr = O.SR(q, A.YH_MODEL_FK3V, wl.fk, st)
     sample = 25  # SR steps per bench step
     times = []
     for k in range(args.warmup + args.steps):
@@ -727,7 +776,8 @@ def run_sr_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
         "config": {"workload": "fk_sr_512", "grid": [n, n], "model": "FK3V",
-                   "tau_d": 0.25, "template": "frozen", "disc_radius_cells": 160,
+                   "tau_d": 0.25, "template": "re-taken every step (the reference's)",
+                   "disc_radius_cells": 160,
                    "dt_ms": q.dt, "start_tips": int(len(tips)),
                    "parallelism": "host cores"},
         "cpu_baseline": {

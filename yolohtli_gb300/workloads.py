@@ -6,6 +6,8 @@ fk_spiral_256      256x256, 10,000 steps, S1 columns 0-9 at t=0, S2 lower-left
 fk_holes_1024      1024x1024, 20,000 steps, 300 circular holes (r ~ U[2,6]
                    cells), 12 S2 patches of 40x40 at uniform positions and
                    times ~ U[200,400] ms: fibrillation-like.
+fk_sr_512          512x512 start of the symmetry-reduced workload: S1 at
+                   t = 0, S2 per tau_d (SR_PROTOCOLS), run to 1000 ms.
 fk_adjoint_case    512x512 parameter estimation: D(x, y) of 8 seeded Gaussian
                    bumps in [5e-4, 1.5e-3] cm^2/ms, a plane wave from the
                    left edge (the adjoint's workload).
@@ -79,10 +81,10 @@ def stim(step, i0, j0, i1, j1, value=1.0):
 
 def fk_spiral_256(seed=0, n=256, nsteps=10000, s2_ms=320.0):
     """S1 on columns 0-9 at t = 0, S2 on the lower-left quadrant at s2_ms.
-    With the BR-fit parameters the S1 back leaves the tissue refractory to
-    about 400 ms; on 256^2 (6.4 cm) no S2 time leaves activity past 600 ms,
-    on 512^2 (12.8 cm) an S2 at 400-550 ms gives re-entry that lasts past
-    1000 ms (fk_sr_512)."""
+    With the BR-fit parameters on 256^2 (6.4 cm) the S2 at 320 ms makes
+    tips for a few ms at the quadrant's corner and no S2 time leaves
+    activity past 600 ms: the wavelength does not fit; 512^2 re-entry is
+    in fk_sr_512."""
     rng = np.random.default_rng(seed)
     p = A.fk_tissue_params(n, n)
     u, v, w = _ic(n, n, rng)
@@ -92,11 +94,32 @@ def fk_spiral_256(seed=0, n=256, nsteps=10000, s2_ms=320.0):
                     u, v, w, None, [s2], nsteps)
 
 
-def fk_sr_512(seed=0):
-    """The start of the symmetry-reduced workload: fk_spiral_256's protocol
-    on 512^2 with S2 at 430 ms (inside the vulnerable window), run to
-    1000 ms, where two tips are in the tissue."""
-    return fk_spiral_256(seed=seed, n=512, nsteps=20000, s2_ms=430.0)
+# Start protocols of the symmetry-reduced workload on 512^2, per tau_d:
+# (S2 box, S2 time in ms). A sweep of S2 times 180-705 ms (every 15 ms) on
+# the lower-left quadrant and on the lower half, run to 3000 ms on the
+# GB300, found re-entry lasting past 3000 ms only for tau_d = 0.25 (lower
+# half, S2 at 540-585 ms) and tau_d = 0.30 (S2 at 615 ms); with
+# tau_d = 0.35, 0.40 and 0.45 every protocol's activity ends before
+# 850 ms: the tissue stays refractory too long (v recovers with
+# tau_v2- = 1000 ms below u_v) for a re-entrant path in 12.8 cm.
+SR_PROTOCOLS = {0.25: ((0, 0, 512, 256), 585.0),
+                0.30: ((0, 0, 256, 256), 615.0)}
+
+
+def fk_sr_512(seed=0, tau_d=0.25):
+    """The start of the symmetry-reduced workload: S1 on columns 0-9 at
+    t = 0 and the S2 of SR_PROTOCOLS[tau_d] on 512^2, run to 1000 ms (the
+    state there is the SR start and, frozen, its template). ValueError for
+    a tau_d without a protocol that sustains re-entry."""
+    if tau_d not in SR_PROTOCOLS:
+        raise ValueError("no re-entry lasts on 512^2 with tau_d = %g" % tau_d)
+    box, s2 = SR_PROTOCOLS[tau_d]
+    wl = fk_spiral_256(seed=seed, n=512, nsteps=20000, s2_ms=s2)
+    wl.fk.tau_d = tau_d
+    s = wl.stims[0]
+    s.i0, s.j0, s.i1, s.j1 = box
+    wl.name = "fk_sr_512_td%g" % tau_d
+    return wl
 
 
 def fk_holes_1024(seed=0, n=1024, nsteps=20000, nholes=300, npatch=12):
