@@ -201,7 +201,10 @@ def test_reference_long_run_and_tip_trajectory():
     (solver handle) against the reference's own FP64 kernels run headless,
     rel L2(u) after N steps, and the plain-mode tip sets every sampleIt =
     40 steps (main.cu:156,961-964; the reference's spiralTip_kernel on its
-    own two u levels) within 0.1 cell."""
+    own two u levels) within 0.1 cell. The reference kernel is also run on
+    the product's own two u levels (FP32 values, widened exactly): there
+    the tip sets must be equal, so any difference of the trajectories
+    comes from the states, not from the tip detection."""
     import torch
     from scipy.optimize import linear_sum_assignment
     n, nsteps, every = 256, 20000, 40
@@ -219,7 +222,16 @@ def test_reference_long_run_and_tip_trajectory():
     m.set_state(*st)
     R.set_params(p)
     errs, tip_d, ntips, samples_ok, nsamples, matched, extra = {}, 0.0, 0, 0, 0, 0, 0
+    same_in, same_tips, same_d = 0, 0, 0.0
     shown = 0
+
+    def match(x, y):
+        if not len(x) or not len(y):
+            return 0, 0.0
+        d = np.hypot(x[:, None, 0] - y[None, :, 0], x[:, None, 1] - y[None, :, 1])
+        r, c = linear_sum_assignment(d)
+        ok = d[r, c] <= 0.1
+        return int(ok.sum()), float(d[r, c][ok].max(initial=0.0))
     for step in range(every, nsteps + 1, every):
         for _ in range(every):
             R.rd(p, b, a, J, vt)
@@ -229,18 +241,26 @@ def test_reference_long_run_and_tip_trajectory():
         R.sync()
         nr = int(cnt.item())
         ref = host(vec)[: 5 * nr].reshape(nr, 5)
-        m.run(every)
+        m.run(every - 1)
+        prev = m.get_state()[0]
+        m.run(1)
         m.track_tips()
         got = m.get_tips()
+        # the reference's tip kernel on the product's own levels
+        cnt.zero_()
+        R.tip(p, dev(prev, torch.float64), dev(m.get_state()[0], torch.float64),
+              plot, cnt, vec, p.dt * step)
+        R.sync()
+        ns = int(cnt.item())
+        same = host(vec)[: 5 * ns].reshape(ns, 5)
+        ms_, ds_ = match(got, same)
+        same_in += ms_ == ns == len(got)
+        same_tips += ns
+        same_d = max(same_d, ds_)
         nsamples += 1
         ntips += nr
-        mk = 0
-        if nr and len(got):
-            d = np.hypot(got[:, None, 0] - ref[None, :, 0],
-                         got[:, None, 1] - ref[None, :, 1])
-            r, c = linear_sum_assignment(d)
-            mk = int((d[r, c] <= 0.1).sum())
-            tip_d = max(tip_d, float(d[r, c][d[r, c] <= 0.1].max(initial=0.0)))
+        mk, dd = match(got, ref)
+        tip_d = max(tip_d, dd)
         matched += mk
         extra += len(got) - mk
         if mk == nr == len(got):
@@ -256,11 +276,17 @@ def test_reference_long_run_and_tip_trajectory():
     print("REF2V 256^2 FP32 product vs the reference's FP64 kernels: rel L2(u)",
           {k: "%.2e" % v for k, v in errs.items()},
           "; tips: %d of %d samples with equal sets, %d of %d reference tips "
-          "matched within 0.1 cell (largest distance %.2e), %d extra" % (
-              samples_ok, nsamples, matched, ntips, tip_d, extra))
+          "matched within 0.1 cell (largest distance %.2e), %d extra; the "
+          "reference's tip kernel on the product's levels: %d of %d samples "
+          "equal (%d tips, largest distance %.2e)" % (
+              samples_ok, nsamples, matched, ntips, tip_d, extra, same_in,
+              nsamples, same_tips, same_d))
     assert ntips > 0
     # 1e-5 through 10,000 steps (measured 2e-7 .. 1.2e-6); 2.5e-5 at 20,000
     for k in marks[:3]:
         assert errs[k] < 1e-5, (k, errs[k])
     assert errs[20000] < 1e-4
-    assert matched >= 0.95 * ntips
+    # every product tip is one of the reference's, and on the same levels
+    # the two tip kernels agree
+    assert extra == 0
+    assert same_in >= 0.99 * nsamples

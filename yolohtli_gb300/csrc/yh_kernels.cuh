@@ -75,10 +75,6 @@ struct ResidentPlan {
   int nb, rq, rrem, rmax;  // blocks, rows per block (rq or rq+1), max rows
   int threads;             // compute threads per block (+ 64 or 128 receiving)
   size_t smem;             // dynamic shared memory per block
-  // register-resident form (FK3V, nx % 4 == 0): work items of 4 cells per
-  // compute thread (0: the shared-memory form), its threads and memory
-  int ni, reg_threads;
-  size_t reg_smem;
 };
 ResidentPlan resident_plan(const StepCoeffs<float> &a, int device);
 // bytes of the tagged boundary-row buffers of a plan

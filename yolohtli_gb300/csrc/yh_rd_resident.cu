@@ -46,7 +46,6 @@ constexpr int kResBatch = 16;                // halo words per comm thread and p
 constexpr int kResCells = YH_RES_CELLS;  // cells per work item, rows nx % 4 == 0
 constexpr unsigned long long kResWaitNs = 1000000000ull;  // 1 s
 
-
 struct ResArgs {
   StepCoeffs<float> a;
   Fld<float> io;                // state: read at the start, written at the end
@@ -455,220 +454,6 @@ __global__ void __launch_bounds__(kResThreads + NC, 1)
   }
 }
 
-// ---------------------------------------------------------------------------
-// Register-resident form (FK3V, nx % 4 == 0): every compute thread owns NI
-// work items of 4 cells for the whole launch and keeps their u, v, w and
-// hole codes in registers. v and w never diffuse, so they never leave the
-// thread; u goes to shared memory once per step (the double-buffered rows
-// the neighbours read), and the neighbour reads of an item are two float4
-// (rows j-1, j+1) and two scalars (columns i0-1, i0+4) at offsets computed
-// once per launch. The cell update is fk3v_cells4, as in every other
-// engine (same bits). Item k of thread t is virtual item t + k*T of the
-// block, in the order rows 0, R-1, 1 .. R-2 (the published rows first).
-// ---------------------------------------------------------------------------
-
-// The register-resident form runs NI = 4 items per compute thread in
-// blocks of at most 512 threads, which leaves 128 registers a thread
-// (65,536 per SM): the 4 x 12 state values, offsets, flags and hole codes
-// and the update's temporaries without spills. Fewer items a thread (more
-// threads, fewer registers each) spilled.
-constexpr int kResRegItems = 4;
-constexpr int kResRegThreads = 512;
-constexpr int kResRegComm = 64;  // receiving threads
-
-// Flags of a work item of the register-resident form (its local row in
-// bits 16-31).
-enum : uint32_t {
-  kItValid = 1u, kItPub = 2u, kItMirN = 4u, kItMirS = 8u, kItMirW = 16u,
-  kItMirE = 32u
-};
-
-template <bool HOLES, int NC, int NI>
-__global__ void __launch_bounds__(kResRegThreads, 1)
-    rd_resident_reg_kernel(const ResArgs A) {
-  extern __shared__ float4 sm4[];
-  const StepCoeffs<float> &a = A.a;
-  const int nx = a.nx, ny = a.ny, RM = A.rmax;
-  const int b = blockIdx.x, nb = A.nb;
-  const int r0 = b * A.rq + min(b, A.rrem);
-  const int R = A.rq + (b < A.rrem ? 1 : 0);
-  const bool bottom = b == 0, top = b == nb - 1;
-  float *U0 = reinterpret_cast<float *>(sm4);
-  float *U1 = U0 + (RM + 2) * nx;
-  const int t = threadIdx.x;
-  const int T = A.threads;
-  const bool comm = t >= T;
-  const int c = t - T;
-  const int nq = nx >> 2, items = R * nq;
-  const size_t par_stride = (size_t)A.nb * 2 * nx;
-  __shared__ int s_abort;
-  __shared__ int s_ev_step[kResMaxStims];
-  if (t == 0) s_abort = 0;
-  if (t < A.nstims) s_ev_step[t] = A.stims[t].step;
-
-  // the thread's items: buffer offset of the first cell and flags; state
-  // in registers
-  int off[NI];
-  uint32_t meta[NI], code[NI];
-  float u[NI][4], v[NI][4], w[NI][4];
-#pragma unroll
-  for (int k = 0; k < NI; ++k) {
-    const int vi = t + k * T;
-    const bool ok = !comm && vi < items;
-    const int vr = ok ? vi / nq : 0;
-    const int q = ok ? vi - vr * nq : 0;
-    const int lr = vr == 0 ? 0 : (vr == 1 ? R - 1 : vr - 1);
-    const int i0 = q << 2;
-    off[k] = (lr + 1) * nx + i0;
-    meta[k] = (ok ? kItValid : 0u) |
-              (ok && ((lr == 0 && !bottom) || (lr == R - 1 && !top)) ? kItPub : 0u) |
-              (top && lr == R - 1 ? kItMirN : 0u) |     // row ny -> ny - 2
-              (bottom && lr == 0 ? kItMirS : 0u) |      // row -1 -> 1
-              (i0 == 0 ? kItMirW : 0u) |                // column -1 -> 1
-              (i0 + 4 == nx ? kItMirE : 0u) |           // column nx -> nx - 2
-              ((uint32_t)lr << 16);
-    code[k] = 0x01010101u;
-#pragma unroll
-    for (int m = 0; m < 4; ++m) u[k][m] = v[k][m] = w[k][m] = 0.f;
-    if (ok) {
-      const int gy = r0 + lr;
-      const size_t g = (size_t)gy * nx + i0;
-      const float4 uu = *reinterpret_cast<const float4 *>(A.io.f[0] + g);
-      const float4 vv = *reinterpret_cast<const float4 *>(A.io.f[1] + g);
-      const float4 ww = *reinterpret_cast<const float4 *>(A.io.f[2] + g);
-      u[k][0] = uu.x; u[k][1] = uu.y; u[k][2] = uu.z; u[k][3] = uu.w;
-      v[k][0] = vv.x; v[k][1] = vv.y; v[k][2] = vv.z; v[k][3] = vv.w;
-      w[k][0] = ww.x; w[k][1] = ww.y; w[k][2] = ww.z; w[k][3] = ww.w;
-      *reinterpret_cast<float4 *>(U0 + off[k]) = uu;
-      if (HOLES) {
-        const uint8_t *S = A.solid;
-        uint32_t cw = 0;
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          const int i = i0 + m;
-          const bool sc = S[(size_t)gy * nx + i] != 0;
-          const bool sw = S[(size_t)gy * nx + mirror(i - 1, nx)] != 0;
-          const bool se = S[(size_t)gy * nx + mirror(i + 1, nx)] != 0;
-          const bool sn = S[(size_t)mirror(gy + 1, ny) * nx + i] != 0;
-          const bool ss = S[(size_t)mirror(gy - 1, ny) * nx + i] != 0;
-          cw |= ((sc ? 1u : 0u) | (hole_pattern(sw, sc, se) << 1) |
-                 (hole_pattern(sn, sc, ss) << 3)) << (8 * m);
-        }
-        code[k] = cw;
-      }
-      // the boundary rows of the state after 0 steps, tag 0, buffer 0
-      if ((meta[k] & kItPub) && b != A.mute)
-        st_tagged_vec<4>(A.halo + (size_t)b * 2 * nx + (lr == 0 ? 0 : nx) + i0,
-                         u[k], 0u);
-    }
-  }
-  __syncthreads();
-  int ev = 0;
-  {
-    int e0, e1;
-    stim_run(s_ev_step, A.nstims, ev, A.step0, e0, e1);
-    if (comm && !res_receive<4>(A, 0, e0, e1, b, r0, R, bottom, top, U0, c, NC))
-      s_abort = 1;
-  }
-  __syncthreads();
-  if (s_abort) return;
-
-  for (int s = 0; s < A.nsteps; ++s) {
-    const int gs = A.step0 + s;
-    float *cur = (s & 1) ? U1 : U0;
-    float *nxt = (s & 1) ? U0 : U1;
-    int e0, e1;
-    stim_run(s_ev_step, A.nstims, ev, gs, e0, e1);
-    if (e1 > e0) {
-      // stimulus events of this step on the thread's own cells (registers
-      // and the buffer the neighbours read); the halo rows got theirs when
-      // they were received
-#pragma unroll
-      for (int k = 0; k < NI; ++k) {
-        if (!(meta[k] & kItValid)) continue;
-        const int lr = (int)(meta[k] >> 16), gy = r0 + lr;
-        const int i0 = off[k] - (lr + 1) * nx;
-        bool hit = false;
-        for (int e = e0; e < e1; ++e) {
-          const yh_stim &E = A.stims[e];
-          if (gy < E.j0 || gy >= E.j1) continue;
-#pragma unroll
-          for (int m = 0; m < 4; ++m) {
-            const int i = i0 + m;
-            if (i >= E.i0 && i < E.i1 && (!HOLES || ((code[k] >> (8 * m)) & 1u))) {
-              u[k][m] = E.value;
-              hit = true;
-            }
-          }
-        }
-        if (hit)
-          *reinterpret_cast<float4 *>(cur + off[k]) =
-              make_float4(u[k][0], u[k][1], u[k][2], u[k][3]);
-      }
-      __syncthreads();
-    }
-    ev = e1;
-    if (!comm) {
-      unsigned long long *pb =
-          b == A.mute ? nullptr
-                      : A.halo + (size_t)((s + 1) & 1) * par_stride + (size_t)b * 2 * nx;
-#pragma unroll
-      for (int k = 0; k < NI; ++k) {
-        const uint32_t f = meta[k];
-        if (!(f & kItValid)) continue;
-        const float *pc = cur + off[k];
-        const float4 n4 = *reinterpret_cast<const float4 *>(pc + ((f & kItMirN) ? -nx : nx));
-        const float4 s4 = *reinterpret_cast<const float4 *>(pc + ((f & kItMirS) ? nx : -nx));
-        const float uw = pc[(f & kItMirW) ? 1 : -1];
-        const float ue = pc[(f & kItMirE) ? 2 : 4];
-        const float un_[4] = {n4.x, n4.y, n4.z, n4.w};
-        const float us_[4] = {s4.x, s4.y, s4.z, s4.w};
-        float ou[4], ov[4], ow[4];
-        fk3v_cells4(a, !HOLES || code[k] == 0x01010101u, code[k], u[k], uw,
-                    ue, un_, us_, v[k], w[k], ou, ov, ow);
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          u[k][m] = ou[m];
-          v[k][m] = ov[m];
-          w[k][m] = ow[m];
-        }
-        *reinterpret_cast<float4 *>(nxt + off[k]) =
-            make_float4(ou[0], ou[1], ou[2], ou[3]);
-        if ((f & kItPub) && pb) {
-          const int lr = (int)(f >> 16);
-          st_tagged_vec<4>(pb + (lr == 0 ? 0 : nx) + (off[k] - (lr + 1) * nx),
-                           ou, (unsigned)s + 1u);
-        }
-      }
-    } else if (s + 1 < A.nsteps) {
-      int n0, n1;
-      stim_run(s_ev_step, A.nstims, ev, gs + 1, n0, n1);
-      if (!res_receive<4>(A, s + 1, n0, n1, b, r0, R, bottom, top, nxt, c, NC))
-        s_abort = 1;
-    }
-    __syncthreads();
-    if (s_abort) return;
-  }
-
-  // the state back from registers; u of the level before the last step
-  const float *pre = (A.nsteps & 1) ? U0 : U1;
-#pragma unroll
-  for (int k = 0; k < NI; ++k) {
-    if (!(meta[k] & kItValid)) continue;
-    const int lr = (int)(meta[k] >> 16);
-    const size_t g = (size_t)(r0 + lr) * nx + (off[k] - (lr + 1) * nx);
-    *reinterpret_cast<float4 *>(A.io.f[0] + g) =
-        make_float4(u[k][0], u[k][1], u[k][2], u[k][3]);
-    *reinterpret_cast<float4 *>(A.io.f[1] + g) =
-        make_float4(v[k][0], v[k][1], v[k][2], v[k][3]);
-    *reinterpret_cast<float4 *>(A.io.f[2] + g) =
-        make_float4(w[k][0], w[k][1], w[k][2], w[k][3]);
-    if (A.prev_u)
-      *reinterpret_cast<float4 *>(A.prev_u + g) =
-          *reinterpret_cast<const float4 *>(pre + off[k]);
-  }
-}
-
 // Rows per block and shared memory of the resident solver on this device;
 // ok = false when the grid does not fit (or the model diffuses v).
 ResidentPlan resident_plan(const StepCoeffs<float> &a, int device) {
@@ -690,21 +475,6 @@ ResidentPlan resident_plan(const StepCoeffs<float> &a, int device) {
   pl.smem = (size_t)(2 * (pl.rmax + 2) + 2 * pl.rmax) * a.nx * sizeof(float) +
             (size_t)pl.rmax * a.nx + 64;
   pl.ok = pl.smem <= (size_t)smem_optin && pl.rq >= 2;
-  // register-resident form: two u buffers in shared memory, v, w and the
-  // hole codes in registers, when the block's items fit 4 a thread
-  pl.ni = 0;
-  pl.reg_threads = 0;
-  pl.reg_smem = (size_t)2 * (pl.rmax + 2) * a.nx * sizeof(float) + 64;
-  if (a.model == YH_MODEL_FK3V && a.nx % 4 == 0 && pl.rq >= 2 &&
-      pl.reg_smem <= (size_t)smem_optin) {
-    const int items = pl.rmax * (a.nx / 4);
-    const int T = ((items + kResRegItems - 1) / kResRegItems + 31) / 32 * 32;
-    if (T + kResRegComm <= kResRegThreads) {
-      pl.ni = kResRegItems;
-      pl.reg_threads = T;
-      pl.ok = true;
-    }
-  }
   // compute threads: the fewest rounds of work items at up to kResThreads
   // threads, then the fewest warps that keep that number of rounds (every
   // thread the same number of items where the rows allow it)
@@ -719,18 +489,6 @@ ResidentPlan resident_plan(const StepCoeffs<float> &a, int device) {
 
 size_t resident_halo_bytes(const ResidentPlan &pl, int nx) {
   return (size_t)2 * pl.nb * 2 * nx * sizeof(unsigned long long);
-}
-
-template <bool HOLES, int NC, int NI>
-static cudaError_t launch_res_reg(const ResArgs &A, size_t smem,
-                                  cudaStream_t s) {
-  auto fn = rd_resident_reg_kernel<HOLES, NC, NI>;
-  cudaError_t e =
-      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  void *args[] = {const_cast<ResArgs *>(&A)};
-  return cudaLaunchCooperativeKernel((const void *)fn, dim3(A.nb),
-                                     dim3(A.threads + NC), args, smem, s);
 }
 
 template <int MODEL, bool HOLES, int CW, int NC>
@@ -778,16 +536,6 @@ cudaError_t launch_rd_resident(const StepCoeffs<float> &a, const Fld<float> &io,
   if (e != cudaSuccess) return e;
   const bool vec = (a.nx % kResCells) == 0;
   const bool holes = solid != nullptr;
-  if (pl.ni && a.model == YH_MODEL_FK3V) {
-    A.threads = pl.reg_threads;
-#define YH_RES_REG(H, NI)                                                  \
-  if (holes == H && pl.ni == NI)                                           \
-    return launch_res_reg<H, kResRegComm, NI>(A, pl.reg_smem, s);
-    YH_RES_REG(true, kResRegItems)
-    YH_RES_REG(false, kResRegItems)
-#undef YH_RES_REG
-    return cudaErrorInvalidValue;
-  }
   A.threads = pl.threads;
   // Receiving threads: 128 take the halo in one pass of loads; with a hole
   // mask the compute warps are the critical path and 64 (two passes, fewer
