@@ -970,6 +970,36 @@ def adjoint_measure(nsteps, steps, warmup, dist, world, full=False):
                          "unit": "instance gradients/s", "checkpoint_steps": ck,
                          "note": "16 instances in one handle, one launch per step",
                          "roofline": adjoint_roofline(batch_rate, n * n, nsteps)}
+    # the batched fit: 16 instances (true D of seeds 0..15, the FK3V
+    # parameters shared), Adam on log D and log parameters from the true
+    # values + 10 %, 20 iterations, one batched gradient each
+    from yolohtli_gb300.adjoint import fit
+    af = Adjoint(p, fk0, nsteps, frame, spacing, ck, smooth=smooth, batch=B)
+    Dt = torch.cat([torch.tensor(W.fk_adjoint_case(n, seed=k)[0], device="cuda")
+                    for k in range(B)])
+    stf = [torch.tensor(x, device="cuda").repeat(B) for x in state0]
+    tgt = torch.empty(af.target_shape, dtype=torch.float32, device="cuda")
+    af.record(Dt, stf, tgt)
+    af.set_target(tgt)
+    Df = Dt * 1.1
+    e0 = float((Df - Dt).norm() / Dt.norm())
+    t4 = time.perf_counter()
+    th, losses = fit(af, Df, stf, fk_array(fk0) * 1.1, iters=20, lr=0.02)
+    fit_s = time.perf_counter() - t4
+    e1 = float((Df - Dt).norm() / Dt.norm())
+    th_true = fk_array(fk0)
+    out["fit"] = {
+        "instances": B, "iterations": 20, "optimizer": "Adam on log D and "
+        "log parameters, lr 0.02", "seconds": round(fit_s, 2),
+        "loss_total": [float(x) for x in losses.sum(axis=1)],
+        "loss_ratio_per_instance": [round(float(x), 4) for x in
+                                    losses[-1] / losses[0]],
+        "D_rel_error": [round(e0, 5), round(e1, 5)],
+        "fk_rel_error_max": [0.1, round(float(np.abs(th / th_true - 1).max()), 4)],
+        "note": "start: true D and FK parameters + 10 %; target: probes of the "
+                "run with the true values"}
+    del af, Dt, stf, tgt, Df
+    torch.cuda.empty_cache()
     # accuracy at the full size
     b64, st64, D64, _ = make(True, nsteps, ck)
     g64 = torch.empty_like(D64)
@@ -1049,7 +1079,7 @@ def run_adjoint(args):
             "loss": r["loss"], "forward_ratio": round(r["forward_ratio"], 3),
             "roofline": r["roofline"], "cpu_baseline": r.get("cpu_baseline"),
             "e2e": r["e2e"], "gpu_launches": None, "clocks": r["clocks"]}
-        for k in ("store_all_states", "batched_16", "fd_check",
+        for k in ("store_all_states", "batched_16", "fit", "fd_check",
                   "fp32_vs_fp64_gradient_rel_l2",
                   "fp32_vs_fp64_fk_gradient_rel_max", "fp64_gradients_per_s"):
             line[k] = r[k]

@@ -165,3 +165,52 @@ def probe_loss(D, adjoint, state0, fk=None):
     if _fn is None:
         _fn = _make_function()
     return _fn.apply(D, fk, adjoint, state0)
+
+
+def fit(adjoint, D, state0, fk, iters=20, lr=0.02, fit_fk=True,
+        betas=(0.9, 0.999), eps=1e-8):
+    """Parameter estimation with the adjoint's gradients: Adam on the
+    logarithm of the diffusion map D (every cell of every instance) and of
+    the 13 FK3V parameters, which the handle's instances share (their
+    gradients are summed). The D field's second moment is one number per
+    instance (the mean over its cells), so that a cell moves in proportion
+    to its gradient: cells the probes do not see keep their value, where a
+    per-cell second moment would move them as far as any other. One
+    iteration is one batched loss-and-gradient evaluation of all
+    instances. D: float32 CUDA tensor (batch x cells),
+    modified in place; fk: 13 values (yh_fk_params order). Returns
+    (fk as an array, losses): losses[i] is the per-instance loss before
+    iteration i, with one more row for the final estimate."""
+    import torch
+    b = adjoint.batch
+    th = np.asarray(fk, np.float64).copy()
+    logD = torch.log(D.double())
+    mD = torch.zeros_like(logD)
+    vD = torch.zeros(b, 1, dtype=torch.float64, device=D.device)
+    mt, vt = np.zeros(13), np.zeros(13)
+    g = torch.empty_like(D)
+    gfk = (A.FKParams * b)()
+    losses = []
+    for it in range(iters + 1):
+        adjoint.set_fk(fk_struct(th))
+        D.copy_(torch.exp(logD).float())
+        loss = adjoint.run(D, state0, g, gfk)
+        losses.append(np.atleast_1d(loss).astype(np.float64))
+        if it == iters:
+            break
+        # gradients with respect to the logarithms
+        gD = g.double() * D.double()
+        gt = sum(fk_array(gfk[k]) for k in range(b)) * th
+        k1 = it + 1
+        mD.mul_(betas[0]).add_(gD, alpha=1 - betas[0])
+        vD.mul_(betas[1]).add_((gD * gD).view(b, -1).mean(dim=1, keepdim=True),
+                               alpha=1 - betas[1])
+        step = (mD / (1 - betas[0] ** k1)).view(b, -1) / (
+            torch.sqrt(vD / (1 - betas[1] ** k1)) + eps)
+        logD -= lr * step.view(-1)
+        if fit_fk:
+            mt = betas[0] * mt + (1 - betas[0]) * gt
+            vt = betas[1] * vt + (1 - betas[1]) * gt * gt
+            th = th * np.exp(-lr * (mt / (1 - betas[0] ** k1)) / (
+                np.sqrt(vt / (1 - betas[1] ** k1)) + eps))
+    return th, np.array(losses)

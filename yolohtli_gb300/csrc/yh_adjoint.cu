@@ -66,25 +66,37 @@ __device__ __forceinline__ float ex2<float>(float x) { return exp2f(x); }
 template <>
 __device__ __forceinline__ double ex2<double>(double x) { return exp2(x); }
 
-template <typename Real>
-__device__ __forceinline__ Real th(Real x);
-template <>
-__device__ __forceinline__ float th<float>(float x) { return tanhf(x); }
-template <>
-__device__ __forceinline__ double th<double>(double x) { return tanh(x); }
-
 // The switch H(x) of the model (a step at 0) and its derivative: with a
-// smoothing width eps > 0, H = (1 + tanh(x / eps)) / 2.
+// smoothing width eps > 0, H = (1 + tanh(x / eps)) / 2, evaluated as the
+// logistic function 1 / (1 + 2^(-2 x / (eps ln 2))) (the same function),
+// dH = 2 H (1 - H) / eps.
 template <typename Real>
 __device__ __forceinline__ void heaviside(Real x, Real eps, Real &H, Real &dH) {
   if (eps > Real(0)) {
-    const Real t = th<Real>(x / eps);
-    H = Real(0.5) * (Real(1) + t);
-    dH = Real(0.5) * (Real(1) - t * t) / eps;
+    const Real e = ex2<Real>(Real(-2.8853900817779268147) * (x / eps));  // 2 / ln 2
+    H = Real(1) / (Real(1) + e);
+    dH = Real(2) * H * (Real(1) - H) / eps;
   } else {
     H = x >= Real(0) ? Real(1) : Real(0);
     dH = Real(0);
   }
+}
+
+// The switches and the sigmoid of one cell's u, shared by the update, its
+// derivatives and the parameter terms.
+template <typename Real>
+struct FkSwitch {
+  Real H1, dH1, H2, dH2, sig;
+};
+template <typename Real>
+__device__ __forceinline__ FkSwitch<Real> fk_switch(const AdjCoeffs<Real> &a,
+                                                    Real u) {
+  FkSwitch<Real> s;
+  heaviside(u - a.u_c, a.eps, s.H1, s.dH1);
+  heaviside(u - a.u_v, a.eps, s.H2, s.dH2);
+  const Real e = ex2<Real>(a.k2 * (u - a.u_csi));
+  s.sig = Real(1) / (Real(1) + e);
+  return s;
 }
 
 // The pointwise FK3V update and its partial derivatives.
@@ -100,14 +112,11 @@ struct FkLocal {
 // H2 = H(u - u_v): the FK3V update (fk3v_update) when eps = 0.
 template <typename Real>
 __device__ __forceinline__ FkLocal<Real> fk_local(const AdjCoeffs<Real> &a,
+                                                  const FkSwitch<Real> &S,
                                                   Real u, Real v, Real w,
                                                   Real du) {
   FkLocal<Real> r;
-  Real H1, dH1, H2, dH2;
-  heaviside(u - a.u_c, a.eps, H1, dH1);
-  heaviside(u - a.u_v, a.eps, H2, dH2);
-  const Real e = ex2<Real>(a.k2 * (u - a.u_csi));
-  const Real sig = Real(1) / (Real(1) + e);
+  const Real H1 = S.H1, dH1 = S.dH1, H2 = S.H2, dH2 = S.dH2, sig = S.sig;
   // d sig / du = -ln2 k2 e / (1 + e)^2 = -ln2 k2 sig (1 - sig)
   const Real dsig = -Real(0.69314718055994530942) * a.k2 * sig * (Real(1) - sig);
   const Real jp = a.s_tr - v * (Real(1) - u) * (u - a.u_c) * a.s_td;
@@ -145,14 +154,11 @@ constexpr int kNumFk = 13;
 // at one cell: (lu, lv, lw) is the adjoint of (un, vn, wn).
 template <typename Real>
 __device__ __forceinline__ void fk_param_terms(const AdjCoeffs<Real> &a,
+                                               const FkSwitch<Real> &S,
                                                Real u, Real v, Real w,
                                                Real lu, Real lv, Real lw,
                                                Real g[kNumFk]) {
-  Real H1, dH1, H2, dH2;
-  heaviside(u - a.u_c, a.eps, H1, dH1);
-  heaviside(u - a.u_v, a.eps, H2, dH2);
-  const Real e = ex2<Real>(a.k2 * (u - a.u_csi));
-  const Real sig = Real(1) / (Real(1) + e);
+  const Real H1 = S.H1, dH1 = S.dH1, H2 = S.H2, dH2 = S.dH2, sig = S.sig;
   const Real ln2 = Real(0.69314718055994530942);
   const Real ss = sig * (Real(1) - sig);
   const Real q = v * (Real(1) - u) * (u - a.u_c);  // jp = s_tr - q s_td
@@ -214,7 +220,9 @@ __global__ void adj_forward_kernel(const AdjCoeffs<Real> a,
   vo += off;
   wo += off;
   const int c = i + a.nx * j;
-  const FkLocal<Real> f = fk_local(a, u[c], v[c], w[c], diffusion(a, u, r, i, j));
+  const Real uc = u[c];
+  const FkLocal<Real> f = fk_local(a, fk_switch(a, uc), uc, v[c], w[c],
+                                   diffusion(a, u, r, i, j));
   uo[c] = f.un;
   vo[c] = f.vn;
   wo[c] = f.wn;
@@ -253,6 +261,18 @@ __global__ void __launch_bounds__(256)
     lw_o += off;
     gr += off;
   }
+  // the cell's state and switches, shared by the parameter terms and the
+  // update's derivatives
+  const bool in = i < nx && j < ny;
+  const int c = in ? i + nx * j : 0;
+  Real uc = Real(0), vc = Real(0), wc = Real(0);
+  FkSwitch<Real> S{};
+  if (in) {
+    uc = u[c];
+    vc = v[c];
+    wc = w[c];
+    S = fk_switch(a, uc);
+  }
   if (PARAMS) {
     // the block's 256 x 13 terms through shared memory, transposed: warp
     // q (0-7) sums rows q and q + 8 (8 values a lane, then a shuffle tree),
@@ -261,9 +281,8 @@ __global__ void __launch_bounds__(256)
     const int t = threadIdx.x + 32 * threadIdx.y;
     {
       Real g[kNumFk];
-      if (i < nx && j < ny) {
-        const int c = i + nx * j;
-        fk_param_terms(a, u[c], v[c], w[c], lu[c], lv[c], lw[c], g);
+      if (in) {
+        fk_param_terms(a, S, uc, vc, wc, lu[c], lv[c], lw[c], g);
       } else {
 #pragma unroll
         for (int k = 0; k < kNumFk; ++k) g[k] = Real(0);
@@ -286,11 +305,9 @@ __global__ void __launch_bounds__(256)
       if (lane == 0) gp[blk * 16 + q] += (double)sum;
     }
   }
-  if (i >= nx || j >= ny) return;
-  const int c = i + nx * j;
-  // pointwise part at c
-  const Real du = diffusion(a, u, r, i, j);
-  const FkLocal<Real> f = fk_local(a, u[c], v[c], w[c], du);
+  if (!in) return;
+  // pointwise part at c (the derivatives do not depend on du)
+  const FkLocal<Real> f = fk_local(a, S, uc, vc, wc, Real(0));
   const Real lun = lu[c];
   Real gu = lun * f.dun_du + lv[c] * f.dvn_du + lw[c] * f.dwn_du;
   const Real gv = lun * f.dun_dv + lv[c] * f.dvn_dv;
@@ -300,7 +317,7 @@ __global__ void __launch_bounds__(256)
   // j itself (-k_f per face, and r_j in every k_f), and as m(j, f) of the
   // cells j whose face f points (through the mirror) at c.
   const Real muc = a.tc * lun;
-  const Real uc = u[c], rc = r[c];
+  const Real rc = r[c];
   const int m[4] = {mirror(i - 1, nx) + nx * j, mirror(i + 1, nx) + nx * j,
                     i + nx * mirror(j - 1, ny), i + nx * mirror(j + 1, ny)};
   Real g = Real(0);
