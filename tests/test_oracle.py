@@ -379,3 +379,45 @@ def test_tangent_linear_model_matches_its_own_central_differences():
         assert L > 0
         fd = (Lp - Lm) / (2 * h)
         assert abs(fd - dL) <= 1e-5 * abs(dL), (eps, fd, dL)
+
+
+def _cable(tau_d, dx, dt, L_cm=8.0, t_ms=260.0):
+    """Planar wave along a cable of FK3V tissue (the oracle, FP64): speed
+    between 30 % and 60 % of the cable and the time u stays above 0.5 at
+    30 %."""
+    nx, ny = int(round(L_cm / dx)), 5
+    p = A.fk_tissue_params(nx, ny)
+    p.hx = p.hy = dx
+    p.dt = dt
+    p = A.param_derive(p)
+    fk = A.fk_defaults()
+    fk.tau_d = tau_d
+    u = np.zeros((ny, nx))
+    u[:, : int(round(0.25 / dx))] = 1.0
+    st = [u.ravel(), np.ones(nx * ny), np.ones(nx * ny)]
+    x1, x2 = int(nx * 0.3), int(nx * 0.6)
+    up, down = {}, None
+    every = max(1, int(round(0.5 / dt)))
+    step = 0
+    while step * dt < t_ms:
+        st = O.run(p, A.YH_MODEL_FK3V, fk, st, every, step0=step)
+        step += every
+        row = st[0].reshape(ny, nx)[2]
+        for x in (x1, x2):
+            if x not in up and row[x] > 0.5:
+                up[x] = step * dt
+        if x1 in up and down is None and row[x1] < 0.5 and step * dt > up[x1] + 5:
+            down = step * dt
+    cv = (x2 - x1) * dx / (up[x2] - up[x1]) * 10.0  # m/s
+    return cv, down - up[x1]
+
+
+def test_fk3v_planar_wave_speed_and_duration():
+    """Macroscopic observables of the BR-fit parameter set with tau_d =
+    0.25 at the benchmark's dx = 0.025 cm, dt = 0.05 ms, D = 0.001 cm^2/ms
+    (measured: 0.435 m/s, 135 ms above u = 0.5), converged within 5 % against
+    dx = 0.0125 cm, dt = 0.0125 ms (0.455 m/s, 135.5 ms)."""
+    cv, apd = _cable(0.25, 0.025, 0.05)
+    cv2, apd2 = _cable(0.25, 0.0125, 0.0125)
+    assert 0.40 < cv < 0.47 and 125.0 < apd < 145.0
+    assert abs(cv2 / cv - 1) < 0.06 and abs(apd2 / apd - 1) < 0.03
