@@ -829,8 +829,12 @@ def adjoint_roofline(grads_per_s, cells, nsteps, mode="sqrt_n"):
     peak, kind = measured_peaks()
     b = ADJ_BYTES[mode]
     achieved = grads_per_s * b * cells * nsteps / 1e9
+    trip = profiled_traffic("adjoint512_step_triplet") if cells == 512 * 512 else None
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+            "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "traffic": trip if mode == "sqrt_n" else None,
+            "traffic_note": "DRAM bytes of one forward + recompute + reverse "
+                            "step (ncu, cold L2)" if trip and mode == "sqrt_n" else None,
             "peak_kind": kind, "alg_bytes_per_cell_step": b,
             "note": "achieved = %d B x cells x steps per gradient x "
                     "gradients/s (forward %s + reverse)" % (
@@ -984,13 +988,14 @@ def adjoint_measure(nsteps, steps, warmup, dist, world, full=False):
     Df = Dt * 1.1
     e0 = float((Df - Dt).norm() / Dt.norm())
     t4 = time.perf_counter()
-    th, losses = fit(af, Df, stf, fk_array(fk0) * 1.1, iters=20, lr=0.02)
+    th, losses = fit(af, Df, stf, fk_array(fk0) * 1.1, iters=20, lr=0.01)
     fit_s = time.perf_counter() - t4
     e1 = float((Df - Dt).norm() / Dt.norm())
     th_true = fk_array(fk0)
     out["fit"] = {
         "instances": B, "iterations": 20, "optimizer": "Adam on log D and "
-        "log parameters, lr 0.02", "seconds": round(fit_s, 2),
+        "log parameters (second moments shared per instance's D and over "
+        "the 13 parameters), lr 0.01", "seconds": round(fit_s, 2),
         "loss_total": [float(x) for x in losses.sum(axis=1)],
         "loss_ratio_per_instance": [round(float(x), 4) for x in
                                     losses[-1] / losses[0]],

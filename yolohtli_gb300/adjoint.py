@@ -172,12 +172,13 @@ def fit(adjoint, D, state0, fk, iters=20, lr=0.02, fit_fk=True,
     """Parameter estimation with the adjoint's gradients: Adam on the
     logarithm of the diffusion map D (every cell of every instance) and of
     the 13 FK3V parameters, which the handle's instances share (their
-    gradients are summed). The D field's second moment is one number per
-    instance (the mean over its cells), so that a cell moves in proportion
-    to its gradient: cells the probes do not see keep their value, where a
-    per-cell second moment would move them as far as any other. One
-    iteration is one batched loss-and-gradient evaluation of all
-    instances. D: float32 CUDA tensor (batch x cells),
+    gradients are summed). The second moments are shared: one number per
+    instance for its D field (the mean over its cells) and one for the 13
+    parameters, so that a cell or a parameter moves in proportion to its
+    gradient; a per-value second moment would move the cells the probes do
+    not see, and the parameters the loss hardly depends on, as far as any
+    other, which made the loss climb again at 10,000 steps. One iteration
+    is one batched loss-and-gradient evaluation of all instances. D: float32 CUDA tensor (batch x cells),
     modified in place; fk: 13 values (yh_fk_params order). Returns
     (fk as an array, losses): losses[i] is the per-instance loss before
     iteration i, with one more row for the final estimate."""
@@ -187,7 +188,7 @@ def fit(adjoint, D, state0, fk, iters=20, lr=0.02, fit_fk=True,
     logD = torch.log(D.double())
     mD = torch.zeros_like(logD)
     vD = torch.zeros(b, 1, dtype=torch.float64, device=D.device)
-    mt, vt = np.zeros(13), np.zeros(13)
+    mt, vt = np.zeros(13), 0.0
     g = torch.empty_like(D)
     gfk = (A.FKParams * b)()
     losses = []
@@ -210,7 +211,7 @@ def fit(adjoint, D, state0, fk, iters=20, lr=0.02, fit_fk=True,
         logD -= lr * step.view(-1)
         if fit_fk:
             mt = betas[0] * mt + (1 - betas[0]) * gt
-            vt = betas[1] * vt + (1 - betas[1]) * gt * gt
+            vt = betas[1] * vt + (1 - betas[1]) * float(np.mean(gt * gt))
             th = th * np.exp(-lr * (mt / (1 - betas[0] ** k1)) / (
                 np.sqrt(vt / (1 - betas[1] ** k1)) + eps))
     return th, np.array(losses)
