@@ -314,7 +314,10 @@ int yh_phase_integrals(const yh_param_var *p, int model, yh_fields state,
  * a stream into a CUDA graph. All calls share the one array and it keeps
  * the last call's partial sums: calls that may overlap on the GPU (on
  * different streams) race and give wrong results; serialize them. Never
- * calls cudaMalloc or cudaFree. */
+ * calls cudaMalloc or cudaFree. The looked-up address is kept for the
+ * life of the process: after cudaDeviceReset (or anything else that tears
+ * down and recreates the device's context) the library must be reloaded
+ * before this entry point is called again. */
 int yh_phase_integrals_noalloc(const yh_param_var *p, int model,
                                yh_fields state, yh_fields vel_tan,
                                yh_fields templ_x, yh_fields templ_y,

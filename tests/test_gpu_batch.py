@@ -182,14 +182,41 @@ def test_invalid_batches_are_rejected():
     b.close()
 
 
-def test_config_sized_batch_runs_and_stays_finite():
-    bw = W.fk_batch_256(count=24, nsteps=64)
+def test_config_sized_batch_matches_the_oracle():
+    """The benchmark's batch (fk_batch_256, all 256 instances, per-instance
+    D, time constants, holes and S2 time), 400 steps under the autotuned
+    schedule: every instance equal bit for bit to its single-grid solver,
+    and 8 instances (the smallest, the largest and six between) within
+    1e-5 rel L2(u) of the FP64 oracle."""
+    bw = W.fk_batch_256(nsteps=400)
+    for w in bw.instances:
+        for s in w.stims:
+            s.step = s.step % 350  # the S2 inside the 400 steps
     b = Batch([w.p for w in bw.instances], [w.fk for w in bw.instances],
               [w.solid for w in bw.instances])
     for k, w in enumerate(bw.instances):
         b.set_state(k, *w.state0())
+    b.autotune(64)
+    for k, w in enumerate(bw.instances):
+        b.set_state(k, *w.state0())
     b.run(bw.nsteps, bw.stims())
-    for k in (0, len(bw.instances) - 1):
-        u = b.get_state(k)[0]
-        assert np.isfinite(u).all()
+    order = sorted(range(len(bw.instances)), key=lambda k: bw.instances[k].cells)
+    pick = [order[int(q)] for q in np.linspace(0, len(order) - 1, 8)]
+    worst = 0.0
+    for k in range(len(bw.instances)):
+        got = b.get_state(k)
+        if k in pick or k % 32 == 0:
+            ref = _single(bw.instances[k], [400])
+            for f in range(3):
+                assert np.array_equal(got[f], ref[f]), (k, f)
+        if k in pick:
+            w = bw.instances[k]
+            orc = O.run(w.p, w.model, w.fk, w.state0(), 400, w.stims,
+                        solid=w.solid)
+            m = np.ones(w.cells, bool) if w.solid is None else w.solid != 0
+            e = rel_l2(got[0][m], orc[0][m])
+            worst = max(worst, e)
+            assert e < 1e-5, (k, w.p.nx, e)
+    print("batch of 256, 400 steps: largest rel L2(u) against the FP64 oracle "
+          "over 8 instances %.2e" % worst)
     b.close()
