@@ -187,7 +187,11 @@ def test_config_sized_batch_matches_the_oracle():
     D, time constants, holes and S2 time), 400 steps under the autotuned
     schedule: every instance equal bit for bit to its single-grid solver,
     and 8 instances (the smallest, the largest and six between) within
-    1e-5 rel L2(u) of the FP64 oracle."""
+    1e-5 rel L2(u) of the FP64 oracle, or, where an S2 upstroke is under
+    way at step 400, within twice what the oracle's own FP32 transcription
+    of the step reaches against the FP64 oracle (the FK3V switches turn
+    FP32 rounding into 1e-5 .. 4e-5 there: measured 1.4e-5 at 288^2, 3.4e-5
+    at 704^2 with the S2 at steps 333 and 340)."""
     bw = W.fk_batch_256(nsteps=400)
     for w in bw.instances:
         for s in w.stims:
@@ -213,10 +217,15 @@ def test_config_sized_batch_matches_the_oracle():
             w = bw.instances[k]
             orc = O.run(w.p, w.model, w.fk, w.state0(), 400, w.stims,
                         solid=w.solid)
+            o32 = O.run(w.p, w.model, w.fk, w.state0(), 400, w.stims,
+                        solid=w.solid, dtype=np.float32)
             m = np.ones(w.cells, bool) if w.solid is None else w.solid != 0
             e = rel_l2(got[0][m], orc[0][m])
+            e32 = rel_l2(o32[0][m], orc[0][m])
+            print("instance %d (%d^2): rel L2(u) against the FP64 oracle %.2e "
+                  "(FP32 transcription %.2e)" % (k, w.p.nx, e, e32))
             worst = max(worst, e)
-            assert e < 1e-5, (k, w.p.nx, e)
+            assert e < max(1e-5, 2.0 * e32), (k, w.p.nx, e, e32)
     print("batch of 256, 400 steps: largest rel L2(u) against the FP64 oracle "
           "over 8 instances %.2e" % worst)
     b.close()
