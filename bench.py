@@ -247,6 +247,51 @@ def reference_gpu(n=1024, steps=200, warmup=20):
                       "%d launches after %d warm-up" % (steps, warmup)}
 
 
+def dropin_gpu(n=1024, steps=200, warmup=20):
+    """This library's FP64 drop-in of reactionDiffusion_wrapper (the
+    reference's C++ symbol, include/yolohtli_compat.h) on the case and loop
+    of reference_gpu: REF2V FP64, n x n cells, one call per step, host-timed.
+    None without a GPU."""
+    try:
+        import torch
+        from yolohtli_gb300 import _abi as A
+        from yolohtli_gb300 import workloads as W
+        from yolohtli_gb300.compat import B2, G2, Compat, Int2, sv
+    except Exception:
+        return None
+    if not torch.cuda.is_available():
+        return None
+    p = A.param_defaults(n, n)
+    p.Lx = p.Ly = 3.0
+    p.hx = p.hy = 3.0 / (n - 1)
+    p = A.param_derive(p)
+    cp = Compat()
+    cp.set_params(p)
+    st = W.ref2v_cross(n, n)
+    a = [torch.tensor(np.asarray(x, np.float64), device="cuda") for x in st]
+    b = [torch.zeros_like(a[0]) for _ in range(2)]
+    J = [torch.zeros_like(a[0]) for _ in range(2)]
+    vt = [torch.zeros_like(a[0]) for _ in range(2)]
+    rd = cp.f["rd"]
+    for k in range(warmup + steps):
+        if k == warmup:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+        rd(0, G2, B2, sv(*b), sv(*a), sv(*J), sv(*vt), False, None, False,
+           None, False, Int2(0, 0))
+        a, b = b, a
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    if cp.err() != 0:
+        return {"unavailable": "drop-in returned status %d" % cp.err()}
+    return {"value": round(n * n * steps / dt / 1e9, 3), "unit": METRIC,
+            "kernel": "rd_step_scalar<REF2V, double> through the drop-in "
+                      "reactionDiffusion_wrapper",
+            "model": "REF2V FP64", "grid": [n, n], "steps": steps,
+            "launch": "one call per step, host-timed over %d calls after %d "
+                      "warm-up (as reference_gpu)" % (steps, warmup)}
+
+
 def run_reference(args, wl):
     rank = env_int("RANK", 0)
     if rank != 0:
@@ -1411,6 +1456,9 @@ def main():
         extras["batched"] = batch_summary(batch_measure(5000, 2, 1, dist, world))
         extras["adjoint"] = adjoint_summary(
             adjoint_measure(10000, 2, 1, dist, world), 10000)
+        # like for like with the reference's own kernel (reference_gpu of
+        # the reference arm's line): REF2V FP64, 1024^2, through the drop-in
+        extras["fp64_dropin"] = dropin_gpu()
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": METRIC,

@@ -26,10 +26,14 @@
 // the state x^n it forms lambda^n = (dF/dx^n)^T lambda^{n+1} + dL/dx^n and
 // adds (dF/dr)^T lambda^{n+1} to the gradient with respect to r. The
 // forward states of a segment are recomputed from a checkpoint (every
-// `ck` steps) before the segment's reverse sweep: memory is the
-// checkpoints plus one segment of states. The whole sequence (~3 nsteps
-// launches and the checkpoint copies) is captured once per handle as a
-// CUDA graph and replayed.
+// `ck` steps) before the segment's reverse sweep, on a second stream, one
+// segment ahead of the sweep (the recompute of segment k - 1 runs beside
+// the reverse sweep of segment k; at one 512^2 instance both are bound by
+// launch latency, not by the SMs); the forward pass writes the last
+// segment's states where the sweep reads them. Memory: the checkpoints
+// plus two segments of states. The whole sequence (~3 nsteps launches and
+// the checkpoint copies) is captured once per handle as a CUDA graph and
+// replayed.
 #include <math.h>
 #include <string.h>
 
@@ -234,8 +238,11 @@ __global__ void adj_forward_kernel(const AdjCoeffs<Real> a,
 // With PARAMS the block also adds its cells' fk_param_terms to its own
 // accumulators gp[block][0..12] (FP64; one slot per block, so the sum over
 // steps keeps a fixed order).
+// FP32: 32 registers, 8 blocks of 256 per SM, so a 512^2 step (1024
+// blocks) is one wave of the GPU's 152 SMs (at the default 40 registers it
+// was 1.1 waves, and 19 % slower a gradient).
 template <typename Real, bool PARAMS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 8 : 4)
     adj_reverse_kernel(const AdjCoeffs<Real> a, const Real *__restrict__ r,
                        const Real *__restrict__ u, const Real *__restrict__ v,
                        const Real *__restrict__ w, const Real *__restrict__ lu,
@@ -448,11 +455,17 @@ struct yh_adjoint {
   double rscale = 0;  // r = rscale * D
   cudaStream_t s = nullptr;
   bool own_stream = false;
+  // the recompute stream and its events (fork, segment ready per buffer,
+  // segment consumed per buffer, join)
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   AdjCoeffs<float> af{};
   AdjCoeffs<double> ad{};
   // Every state is [field][instance][cell].
   void *ckpt = nullptr;   // checkpoints: (nsteps - 1) / ck + 1 states
-  void *seg = nullptr;    // one segment of states: ck + 1 states
+  void *seg = nullptr;    // two segments of ck + 1 states (one if ck == 1)
+  size_t seg_states = 0;  // states per segment buffer
   void *lam = nullptr;    // two adjoint states (ping-pong)
   void *r = nullptr;      // r = dt D / h^2, [instance][cell]
   void *gr = nullptr;     // gradient with respect to r
@@ -491,10 +504,15 @@ const AdjCoeffs<double> &coeffs<double>(const yh_adjoint *h) { return h->ad; }
 
 template <typename Real>
 cudaError_t fwd(const yh_adjoint *h, const Real *r, const Real *const *x,
-                Real *const *y) {
+                Real *const *y, cudaStream_t s) {
   const dim3 b(32, 8), g((h->nx + 31) / 32, (h->ny + 7) / 8, h->batch);
-  return launch_pdl(adj_forward_kernel<Real>, g, b, 0, h->s, coeffs<Real>(h),
+  return launch_pdl(adj_forward_kernel<Real>, g, b, 0, s, coeffs<Real>(h),
                     r, x[0], x[1], x[2], y[0], y[1], y[2]);
+}
+template <typename Real>
+cudaError_t fwd(const yh_adjoint *h, const Real *r, const Real *const *x,
+                Real *const *y) {
+  return fwd<Real>(h, r, x, y, h->s);
 }
 
 // Loss of frame f (1-based step / frame) from u, and with lu its adjoint.
@@ -524,17 +542,25 @@ cudaError_t rev(const yh_adjoint *h, const Real *r, const Real *const *x,
 // on the handle's buffers only: r and checkpoint 0 hold the inputs. Its
 // launches are captured into a CUDA graph by run_t. With ck == 1 every
 // state is kept (no recompute): the checkpoints are states 0 .. T-1 and
-// the forward pass writes them in place.
+// the forward pass writes them in place. Otherwise segment k (states
+// k ck .. min((k + 1) ck, T)) lives in segment buffer k % 2: the forward
+// pass fills the last segment's buffer itself, and the recompute stream
+// refills buffer k % 2 with segment k - 2 once the sweep of segment k is
+// done with it.
 template <typename Real>
 cudaError_t run_body(yh_adjoint *h, bool grad, bool params) {
   const size_t n = (size_t)h->n * h->batch;
   const int T = h->nsteps, ck = h->ck;
   const bool all = ck == 1;
   const View<Real> C{(Real *)h->ckpt, n}, S{(Real *)h->seg, n}, L{(Real *)h->lam, n};
+  auto buf = [&](int k) {
+    return View<Real>{(Real *)h->seg + (size_t)(k & 1) * h->seg_states * 3 * n, n};
+  };
   Real *r = (Real *)h->r, *gr = (Real *)h->gr;
   auto st3 = [](const View<Real> &V, int k, Real **out) {
     for (int q = 0; q < 3; ++q) out[q] = V.f(k, q);
   };
+  const int K = (T - 1) / ck + 1, sl = (K - 1) * ck;  // segments; last start
   cudaError_t e = cudaMemsetAsync(h->loss, 0, h->batch * sizeof(double), h->s);
   // forward: checkpoints every ck steps, the loss at every frame
   if (all) {
@@ -547,22 +573,36 @@ cudaError_t run_body(yh_adjoint *h, bool grad, bool params) {
         e = probe<Real>(h, (t + 1) / h->frame, y[0], h->loss, nullptr);
     }
   } else {
+    // states before sl ping-pong in the other buffer's first two slots;
+    // states sl .. T go to the last segment's buffer
+    const View<Real> BL = buf(K - 1), BO = buf(K);
     Real *cur[3], *nxt[3];
-    st3(S, 0, cur);
-    st3(S, 1, nxt);
+    st3(sl == 0 ? BL : BO, 0, cur);
+    st3(BO, 1, nxt);
     for (int q = 0; q < 3 && e == cudaSuccess; ++q)
       e = cudaMemcpyAsync(cur[q], C.f(0, q), n * sizeof(Real),
                           cudaMemcpyDeviceToDevice, h->s);
     for (int t = 0; t < T && e == cudaSuccess; ++t) {
-      e = fwd<Real>(h, r, cur, nxt);
-      for (int q = 0; q < 3; ++q) std::swap(cur[q], nxt[q]);
       const int step = t + 1;
+      if (step >= sl) {
+        Real *y[3];
+        st3(BL, step - sl, y);
+        e = fwd<Real>(h, r, cur, y);
+        for (int q = 0; q < 3; ++q) cur[q] = y[q];
+      } else {
+        e = fwd<Real>(h, r, cur, nxt);
+        for (int q = 0; q < 3; ++q) std::swap(cur[q], nxt[q]);
+      }
       if (e == cudaSuccess && step % h->frame == 0)
         e = probe<Real>(h, step / h->frame, cur[0], h->loss, nullptr);
-      if (e == cudaSuccess && step % ck == 0 && step < T)
+      if (e == cudaSuccess && step % ck == 0 && step < sl)
         for (int q = 0; q < 3 && e == cudaSuccess; ++q)
           e = cudaMemcpyAsync(C.f(step / ck, q), cur[q], n * sizeof(Real),
                               cudaMemcpyDeviceToDevice, h->s);
+      // the forward pass is done with the other buffer: the recompute of
+      // segment K - 2 may start beside the last segment's steps
+      if (e == cudaSuccess && step == sl && grad)
+        e = cudaEventRecord(h->ev_fork, h->s);
     }
   }
   if (e != cudaSuccess || !grad) return e;
@@ -594,22 +634,48 @@ cudaError_t run_body(yh_adjoint *h, bool grad, bool params) {
       e = back(t, t == T ? S.f(0, 0) : C.f(t, 0), xp);
     }
   } else {
-    for (int s0 = ((T - 1) / ck) * ck; s0 >= 0 && e == cudaSuccess; s0 -= ck) {
-      const int s1 = std::min(s0 + ck, T);  // states s0 .. s1
-      for (int q = 0; q < 3 && e == cudaSuccess; ++q)
-        e = cudaMemcpyAsync(S.f(0, q), C.f(s0 / ck, q), n * sizeof(Real),
-                            cudaMemcpyDeviceToDevice, h->s);
-      for (int t = s0; t < s1 && e == cudaSuccess; ++t) {
+    cudaStream_t s2 = h->s2;
+    // segment k (k <= K - 2) from its checkpoint into buffer k % 2, on s2
+    auto recompute = [&](int k) {
+      const View<Real> B = buf(k);
+      const int s0 = k * ck, s1 = s0 + ck;
+      cudaError_t er = cudaSuccess;
+      for (int q = 0; q < 3 && er == cudaSuccess; ++q)
+        er = cudaMemcpyAsync(B.f(0, q), C.f(k, q), n * sizeof(Real),
+                             cudaMemcpyDeviceToDevice, s2);
+      for (int t = s0; t < s1 && er == cudaSuccess; ++t) {
         Real *x[3], *y[3];
-        st3(S, t - s0, x);
-        st3(S, t - s0 + 1, y);
-        e = fwd<Real>(h, r, x, y);
+        st3(B, t - s0, x);
+        st3(B, t - s0 + 1, y);
+        er = fwd<Real>(h, r, x, y, s2);
       }
+      if (er == cudaSuccess) er = cudaEventRecord(h->ev_ready[k & 1], s2);
+      return er;
+    };
+    const bool forked = K >= 2;
+    if (forked) {
+      e = cudaStreamWaitEvent(s2, h->ev_fork, 0);
+      if (e == cudaSuccess) e = recompute(K - 2);
+    }
+    for (int k = K - 1; k >= 0 && e == cudaSuccess; --k) {
+      const View<Real> B = buf(k);
+      const int s0 = k * ck, s1 = std::min(s0 + ck, T);  // states s0 .. s1
+      if (k <= K - 2) e = cudaStreamWaitEvent(h->s, h->ev_ready[k & 1], 0);
       for (int t = s1; t > s0 && e == cudaSuccess; --t) {
         Real *xp[3];
-        st3(S, t - 1 - s0, xp);
-        e = back(t, S.f(t - s0, 0), xp);
+        st3(B, t - 1 - s0, xp);
+        e = back(t, B.f(t - s0, 0), xp);
       }
+      if (e == cudaSuccess && k >= 2) {
+        e = cudaEventRecord(h->ev_free[k & 1], h->s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, h->ev_free[k & 1], 0);
+        if (e == cudaSuccess) e = recompute(k - 2);
+      }
+    }
+    if (forked) {  // join s2 back (also after an error, so the capture ends)
+      const cudaError_t ej = cudaEventRecord(h->ev_join, s2);
+      const cudaError_t ew = cudaStreamWaitEvent(h->s, h->ev_join, 0);
+      if (e == cudaSuccess) e = ej != cudaSuccess ? ej : ew;
     }
   }
   if (e == cudaSuccess && params) {
@@ -750,6 +816,10 @@ extern "C" int yh_adjoint_destroy(yh_adjoint *h) {
   cudaFree(h->loss);
   cudaFree(h->gp);
   cudaFree(h->gfk);
+  if (h->s2) cudaStreamDestroy(h->s2);
+  for (cudaEvent_t ev : {h->ev_fork, h->ev_join, h->ev_ready[0], h->ev_ready[1],
+                         h->ev_free[0], h->ev_free[1]})
+    if (ev) cudaEventDestroy(ev);
   if (h->own_stream && h->s) cudaStreamDestroy(h->s);
   delete h;
   return YH_OK;
@@ -793,7 +863,7 @@ extern "C" int yh_adjoint_create_batch(const yh_param_var *p,
   const size_t cells = (size_t)h->n * batch;
   const size_t state = 3 * cells * es;
   const size_t nck = (size_t)(nsteps - 1) / checkpoint_steps + 1;
-  const size_t nseg = checkpoint_steps == 1 ? 1 : (size_t)checkpoint_steps + 1;
+  h->seg_states = checkpoint_steps == 1 ? 2 : (size_t)checkpoint_steps + 1;
   const size_t tgt = (size_t)std::max(1, h->frames) * h->npx * h->npy * batch;
   cudaError_t e = cudaSuccess;
   h->s = (cudaStream_t)stream;
@@ -802,7 +872,12 @@ extern "C" int yh_adjoint_create_batch(const yh_param_var *p,
     h->own_stream = e == cudaSuccess;
   }
   if (e == cudaSuccess) e = cudaMalloc(&h->ckpt, nck * state);
-  if (e == cudaSuccess) e = cudaMalloc(&h->seg, std::max<size_t>(nseg, 2) * state);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&h->seg, (checkpoint_steps == 1 ? 1 : 2) * h->seg_states * state);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->s2, cudaStreamNonBlocking);
+  for (cudaEvent_t *ev : {&h->ev_fork, &h->ev_join, &h->ev_ready[0], &h->ev_ready[1],
+                          &h->ev_free[0], &h->ev_free[1]})
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&h->lam, 2 * state);
   if (e == cudaSuccess) e = cudaMalloc(&h->r, cells * es);
   if (e == cudaSuccess) e = cudaMalloc(&h->gr, cells * es);

@@ -35,6 +35,24 @@ StepCoeffs<Real> make_step_coeffs(const yh_param_var &p, int model,
   a.gamma = (Real)p.gamma;
   a.beta = (Real)p.beta;
   a.theta = (Real)p.theta;
+  {
+    // -dt I_sum = dt u (mu (1 - u)(u - alpha) - v) with
+    // mu (1 - u)(u - alpha) = -mu u^2 + mu (1 + alpha) u - mu alpha;
+    // -dt I_v = dt eps (delta (u - gamma)(beta - u) - v - theta) with
+    // delta (u - gamma)(beta - u) = -delta u^2 + delta (beta + gamma) u
+    // - delta beta gamma
+    const double K = p.dt, Ke = K * p.eps;
+    a.pu2 = (Real)(-K * p.mu);
+    a.pu1 = (Real)(K * p.mu * (1.0 + p.alpha));
+    a.pu0 = (Real)(-K * p.mu * p.alpha);
+    a.puv = (Real)(-K);
+    a.pv2 = (Real)(-Ke * p.delta);
+    a.pv1 = (Real)(Ke * p.delta * (p.beta + p.gamma));
+    a.pv0 = (Real)(-Ke * (p.delta * p.beta * p.gamma + p.theta));
+    a.pvv = (Real)(-Ke);
+    a.rxs = (Real)(p.rx * p.rscale);
+    a.rys = (Real)(p.ry * p.rscale);
+  }
   if (fk) {
     a.u_c = (Real)fk->u_c;
     a.u_v = (Real)fk->u_v;

@@ -55,6 +55,10 @@ struct StepCoeffs {
   Real inv_twp, inv_twm;
   // the same rates pre-multiplied by tc*dt (FP32 update, fk3v_update)
   Real s_td, s_tr, s_to, s_tsi, s_tvp, s_tv1m, s_tv2m, s_twp, s_twm;
+  // the REF2V reaction terms as polynomials in u with dt folded in
+  // (ref2v_rhs_poly), and the gate's diffusion coefficients rx*rscale,
+  // ry*rscale
+  Real pu2, pu1, pu0, puv, pv2, pv1, pv0, pvv, rxs, rys;
 };
 
 // Hole coefficients along one axis (reactionDiffusion.cu:162-169):
@@ -78,6 +82,22 @@ __device__ __forceinline__ void ref2v_currents(const StepCoeffs<Real> &a,
                                                Real &I_v) {
   I_sum = -(a.mu * u * (Real(1) - u) * (u - a.alpha) - u * v);
   I_v = -(a.eps * (a.delta * (u - a.gamma) * (a.beta - u) - v - a.theta));
+}
+
+// The REF2V right-hand sides r0 = du - dt I_sum, r1 = dv - dt I_v
+// (reactionDiffusion.cu:131-141,498-499) with the currents expanded into
+// polynomials of u and dt folded into their coefficients
+// (make_step_coeffs):
+//   r0 = du + u (pu2 u^2 + pu1 u + pu0 + puv v)
+//   r1 = dv + pv2 u^2 + pv1 u + pv0 + pvv v
+// in Horner form: 8 FP64 operations against the reference order's 15; the
+// two orders round differently (about 1e-16 relative a step).
+template <typename Real>
+__device__ __forceinline__ void ref2v_rhs_poly(const StepCoeffs<Real> &a,
+                                               Real u, Real v, Real du,
+                                               Real dv, Real &r0, Real &r1) {
+  r0 = fma(u, fma(a.puv, v, fma(fma(a.pu2, u, a.pu1), u, a.pu0)), du);
+  r1 = fma(a.pvv, v, fma(fma(a.pv2, u, a.pv1), u, a.pv0)) + dv;
 }
 
 // Programmatic dependent launch (PTX griddepcontrol, sm_90+). A kernel

@@ -2,7 +2,9 @@
 // reactionDiffusion_kernel, reactionDiffusion.cu:26-566, on its Euler /
 // Neumann / 5-point path) and the stimulus box.
 //
-// rd_step_scalar: one cell per thread, any nx; also the FP64 instance.
+// rd_step_scalar: one cell per thread, any nx; also the FP64 instance (the
+//                 REF2V FP64 step with its currents in the polynomial form
+//                 of ref2v_rhs_poly and velTan as rhs * (1/dt)).
 // rd_step_vec4:   FP32, four cells per thread with float4 loads/stores of
 //                 the centre row and of the rows above and below (nx % 4 == 0).
 // Both read the inputs through the read-only path and write every output
@@ -32,11 +34,11 @@ __device__ __forceinline__ void reaction(const StepCoeffs<Real> &a, Real u,
   }
 }
 
-// velTan = rhs/dt (reactionDiffusion.cu:529-530): a division in FP64 as the
-// reference does it, a multiplication by 1/dt in FP32.
+// velTan = rhs/dt (reactionDiffusion.cu:529-530) as rhs * (1/dt): one
+// multiplication in place of a division (within an ulp of it).
 __device__ __forceinline__ double tangent(const StepCoeffs<double> &a,
                                           double r) {
-  return r / a.dt;
+  return r * a.inv_dt;
 }
 __device__ __forceinline__ float tangent(const StepCoeffs<float> &a, float r) {
   return r * a.inv_dt;
@@ -88,6 +90,37 @@ __global__ void __launch_bounds__(256)
   bool sc = true;
   Real du, dv = Real(0);
   constexpr bool F32 = std::is_same<Real, float>::value;
+  if constexpr (MODEL == YH_MODEL_REF2V && !F32) {
+    if (HOLES) {
+      sc = solid[C] != 0;
+      Real cxw, cxc, cxe, cyn, cyc, cys;
+      hole_coeffs(solid[W] != 0, sc, solid[E] != 0, cxw, cxc, cxe);
+      hole_coeffs(solid[N] != 0, sc, solid[S] != 0, cyn, cyc, cys);
+      du = (cxw * __ldg(U + W) - cxc * u + cxe * __ldg(U + E)) * a.rx +
+           (cyn * __ldg(U + N) - cyc * u + cys * __ldg(U + S)) * a.ry;
+      if (a.gate_diff)
+        dv = (cxw * __ldg(V + W) - cxc * v + cxe * __ldg(V + E)) * a.rxs +
+             (cyn * __ldg(V + N) - cyc * v + cys * __ldg(V + S)) * a.rys;
+    } else {
+      const Real hx = fma(Real(-2), u, __ldg(U + W) + __ldg(U + E));
+      const Real hy = fma(Real(-2), u, __ldg(U + N) + __ldg(U + S));
+      du = fma(hx, a.rx, hy * a.ry);
+      if (a.gate_diff) {
+        const Real gx = fma(Real(-2), v, __ldg(V + W) + __ldg(V + E));
+        const Real gy = fma(Real(-2), v, __ldg(V + N) + __ldg(V + S));
+        dv = fma(gx, a.rxs, gy * a.rys);
+      }
+    }
+    Real r0, r1;
+    ref2v_rhs_poly(a, u, v, du, dv, r0, r1);
+    out.f[0][C] = sc ? fma(a.tc, r0, u) : Real(0);
+    out.f[1][C] = sc ? fma(a.tc, r1, v) : Real(0);
+    if (TAN) {
+      tan.f[0][C] = sc ? r0 * a.inv_dt : Real(0);
+      tan.f[1][C] = sc ? r1 * a.inv_dt : Real(0);
+    }
+    return;
+  }
   if (HOLES) {
     sc = solid[C] != 0;
     Real cxw, cxc, cxe, cyn, cyc, cys;
