@@ -869,8 +869,9 @@ def adjoint_roofline(grads_per_s, cells, nsteps, mode="sqrt_n"):
     reads D, u, v, w and writes u, v, w (28 B); the reverse step reads D,
     u, v, w, the adjoint state lu, lv, lw, writes lu, lv, lw and updates
     the D gradient (48 B). sqrt(N) checkpoints run every forward step twice
-    (the pass that records the checkpoints, the segment recompute):
-    2 x 28 + 48 = 104 B; with every state kept, 28 + 48 = 76 B."""
+    (the pass that records the checkpoints, the segment recompute; the
+    last segment's once): 2 x 28 + 48 = 104 B; with every state kept,
+    28 + 48 = 76 B."""
     peak, kind = measured_peaks()
     b = ADJ_BYTES[mode]
     achieved = grads_per_s * b * cells * nsteps / 1e9

@@ -598,7 +598,9 @@ int yh_batch_get_launch_count(yh_batch *b, long long *n);
  * the cell centres of the lattice squares) on the states after every
  * frame_steps steps. One run takes nsteps forward steps keeping a
  * checkpoint every checkpoint_steps, then recomputes each segment and
- * sweeps it backwards: memory is the checkpoints plus one segment. fp64
+ * sweeps it backwards (the recompute of the next segment runs on a second
+ * stream of the handle beside the sweep; the forward pass keeps the last
+ * segment): memory is the checkpoints plus two segments. fp64
  * runs the same in FP64 (for gradient checks). hx must equal hy. smooth:
  * 0 keeps FK3V's switches H(u - u_c), H(u - u_v) as steps (the model of
  * the other engines; its derivative exists almost everywhere but grows with
