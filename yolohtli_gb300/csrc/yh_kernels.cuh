@@ -39,12 +39,15 @@ inline bool aligned16(const Fld<Real> &x, int model) {
 
 // yh_rd.cu
 // codes: optional per-cell hole codes of `solid` (launch_hole_codes), used
-// by the FP32 float4 kernel; the scalar kernels read `solid`.
+// by the FP32 float4 kernel; the scalar kernels read `solid`. reset:
+// optional counter the launch sets to 0 (the symmetry-reduced step's tip
+// count, so no memset node sits between its kernels).
 template <typename Real>
 cudaError_t launch_rd_step(const StepCoeffs<Real> &a, const Fld<Real> &in,
                            const Fld<Real> &out, const Fld<Real> &tan,
                            const uint8_t *solid, cudaStream_t s,
-                           const uint8_t *codes = nullptr);
+                           const uint8_t *codes = nullptr,
+                           int *reset = nullptr);
 cudaError_t launch_hole_codes(const uint8_t *solid, int nx, int ny,
                               uint8_t *codes, cudaStream_t s);
 template <typename Real>

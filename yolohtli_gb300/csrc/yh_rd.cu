@@ -72,10 +72,11 @@ template <int MODEL, typename Real, bool HOLES, bool TAN>
 __global__ void __launch_bounds__(256)
     rd_step_scalar(const StepCoeffs<Real> a, const Fld<Real> in,
                    const Fld<Real> out, const Fld<Real> tan,
-                   const uint8_t *__restrict__ solid) {
+                   const uint8_t *__restrict__ solid, int *reset) {
   constexpr int NF = MODEL == YH_MODEL_FK3V ? 3 : 2;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (reset && i == 0 && j == 0) *reset = 0;
   const int nx = a.nx, ny = a.ny;
   if (i >= nx || j >= ny) return;
   const int C = i + nx * j;
@@ -197,7 +198,7 @@ template <int MODEL, bool HOLES, bool TAN, bool CODES>
 __global__ void __launch_bounds__(256)
     rd_step_vec4(const StepCoeffs<float> a, const Fld<float> in,
                  const Fld<float> out, const Fld<float> tan,
-                 const uint8_t *__restrict__ solid) {
+                 const uint8_t *__restrict__ solid, int *reset) {
   constexpr int NF = MODEL == YH_MODEL_FK3V ? 3 : 2;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;  // float4 column
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -210,6 +211,7 @@ __global__ void __launch_bounds__(256)
   const int iw = mirror(i0 - 1, nx), ie = mirror(i0 + 4, nx);
   grid_dep_wait();
   grid_dep_launch();
+  if (reset && q == 0 && j == 0) *reset = 0;
   const float *__restrict__ U = in.f[0];
   const float4 uc = __ldg(reinterpret_cast<const float4 *>(U + row + i0));
   const float4 un = __ldg(reinterpret_cast<const float4 *>(U + rowN + i0));
@@ -370,7 +372,7 @@ template <int MODEL, typename Real, bool HOLES, bool TAN>
 static cudaError_t launch_rd_t(const StepCoeffs<Real> &a, const Fld<Real> &in,
                                const Fld<Real> &out, const Fld<Real> &tan,
                                const uint8_t *solid, const uint8_t *codes,
-                               cudaStream_t s) {
+                               cudaStream_t s, int *reset) {
   if constexpr (std::is_same<Real, float>::value) {
     const uint8_t *m = HOLES && codes ? codes : solid;
     if ((a.nx % 4) == 0 && aligned16(in, MODEL) && aligned16(out, MODEL) &&
@@ -392,16 +394,16 @@ static cudaError_t launch_rd_t(const StepCoeffs<Real> &a, const Fld<Real> &in,
       cfg.numAttrs = 1;
       if (HOLES && codes)
         return cudaLaunchKernelEx(&cfg, rd_step_vec4<MODEL, HOLES, TAN, true>,
-                                  a, in, out, tan, codes);
+                                  a, in, out, tan, codes, reset);
       return cudaLaunchKernelEx(&cfg, rd_step_vec4<MODEL, HOLES, TAN, false>,
-                                a, in, out, tan, solid);
+                                a, in, out, tan, solid, reset);
     }
   }
   {
     const dim3 block(32, 8);
     const dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8);
     rd_step_scalar<MODEL, Real, HOLES, TAN>
-        <<<grid, block, 0, s>>>(a, in, out, tan, solid);
+        <<<grid, block, 0, s>>>(a, in, out, tan, solid, reset);
   }
   return cudaGetLastError();
 }
@@ -410,12 +412,12 @@ template <typename Real>
 cudaError_t launch_rd_step(const StepCoeffs<Real> &a, const Fld<Real> &in,
                            const Fld<Real> &out, const Fld<Real> &tan,
                            const uint8_t *solid, cudaStream_t s,
-                           const uint8_t *codes) {
+                           const uint8_t *codes, int *reset) {
   const bool holes = solid != nullptr;
   const bool t = tan.f[0] != nullptr;
 #define YH_RD_CASE(M, H, T)                                             \
   if (a.model == M && holes == H && t == T)                             \
-    return launch_rd_t<M, Real, H, T>(a, in, out, tan, solid, codes, s);
+    return launch_rd_t<M, Real, H, T>(a, in, out, tan, solid, codes, s, reset);
   YH_RD_CASE(YH_MODEL_REF2V, false, false)
   YH_RD_CASE(YH_MODEL_REF2V, false, true)
   YH_RD_CASE(YH_MODEL_REF2V, true, false)
@@ -449,13 +451,13 @@ template cudaError_t launch_rd_step<float>(const StepCoeffs<float> &,
                                            const Fld<float> &,
                                            const Fld<float> &,
                                            const uint8_t *, cudaStream_t,
-                                           const uint8_t *);
+                                           const uint8_t *, int *);
 template cudaError_t launch_rd_step<double>(const StepCoeffs<double> &,
                                             const Fld<double> &,
                                             const Fld<double> &,
                                             const Fld<double> &,
                                             const uint8_t *, cudaStream_t,
-                                            const uint8_t *);
+                                            const uint8_t *, int *);
 template cudaError_t launch_stimulate<float>(float *, const uint8_t *, int,
                                              int, int, int, int, int, float,
                                              cudaStream_t);

@@ -696,10 +696,9 @@ static cudaError_t enqueue_sr_step(yh_solver *h, bool first) {
   const Fld<float> ty = h->frozen ? h->ty : none;
   const Fld<float> tt = h->frozen ? h->tt : none;
   float *advf_rows = h->adv_f, *advf_cols = h->adv_f + h->p.ny;
-  cudaError_t e = cudaMemsetAsync(h->tip_count, 0, sizeof(int), h->s);
-  if (e == cudaSuccess)  // 1. RD with tangent: cur -> nxt
-    e = launch_rd_step<float>(a, h->cur, h->nxt, h->tan, h->solid, h->s,
-                              h->codes);
+  // 1. RD with tangent: cur -> nxt; it also zeroes the tip count
+  cudaError_t e = launch_rd_step<float>(a, h->cur, h->nxt, h->tan, h->solid,
+                                        h->s, h->codes, h->tip_count);
   if (e == cudaSuccess)  // 2. tips x = pre-RD u, y = post-RD u; centre
     e = launch_tips<float>(h->p, h->nxt.f[0], h->cur.f[0], h->p.solidSwitch, 0.0,
                            h->tip_count, h->tips, kTipCapacity, h->sym,
