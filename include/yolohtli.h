@@ -573,12 +573,33 @@ int yh_batch_set_schedule(yh_batch *b, long long group_cells, int streams);
  * TMA bulk tensor copies, the same bits; YH_EUNSUPPORTED unless every
  * instance's rows allow it: nx % 16 == 0 for instances with holes). */
 int yh_batch_set_depth(yh_batch *b, int depth);
+/* The wavefront engine: one persistent launch per run segment (a run is one
+ * segment unless an instance has more than 4 events in it). Each instance
+ * goes to a cluster of `cluster` CTAs (1, 2 or 4; one CTA per SM, the
+ * instance's columns split into that many bands), which advances it up to K
+ * steps per pass with its rows in shared-memory rings: level k of a pass
+ * computes step k on row p - 2k at wavefront position p, neighbouring bands
+ * exchange their edge columns through distributed shared memory. K is as
+ * large as the rings allow (at most (R - 3) / 2 for R ring rows, R <= 128),
+ * capped at max_levels when max_levels > 0. Instances go to the clusters
+ * longest first, each to the least loaded. The same bits as one launch per
+ * step; the state is updated in place. YH_EUNSUPPORTED where an instance
+ * has fewer quads (nx / 4) than `cluster` or its rings would hold fewer
+ * than 8 rows (nx / cluster above ~1,690 cells). cluster 0 returns to the
+ * grouped launches; yh_batch_set_depth and yh_batch_set_schedule do too. */
+int yh_batch_set_wave(yh_batch *b, int cluster, int max_levels);
+/* The wavefront engine's shape (*cluster 0: grouped launches) and the
+ * clusters of its launch. */
+int yh_batch_get_wave(yh_batch *b, int *cluster, int *max_levels,
+                      int *clusters);
 /* The schedule autotuner: times probe_steps steps (rounded up to even, no
  * events) of every schedule of groups of 256 K, 512 K, 1 M or 2 M cells
- * on 2, 3 or 4 streams at depth 1 and (where supported) 2 on the current
+ * on 2, 3 or 4 streams at depth 1 and (where supported) 2, and of the
+ * wavefront engine with 1, 2 and 4 CTAs per instance, on the current
  * state, keeps the fastest and restores the state and the step count. The
  * choice is returned in *group_cells, *streams and *depth (any may be
- * NULL). */
+ * NULL); the wavefront engine reports *depth 0, *streams = CTAs per
+ * instance and *group_cells 0. */
 int yh_batch_autotune(yh_batch *b, int probe_steps, long long *group_cells,
                       int *streams, int *depth);
 int yh_batch_get_step(yh_batch *b, int *step);

@@ -110,6 +110,124 @@ def test_every_schedule_gives_the_same_bits(schedule, depth):
     b.close()
 
 
+def _ragged_instances(seed=7):
+    """Widths that split unevenly into bands of quads (nx / 4 = 9, 25, 11,
+    13) and are no multiple of 16, heights from 5 rows up, holes in two,
+    events on both runs (one on the first step of a run, two on one step)."""
+    rng = np.random.default_rng(seed)
+    shapes = [(36, 40), (100, 52), (44, 70), (52, 5), (100, 130)]
+    out = []
+    for k, (nx, ny) in enumerate(shapes):
+        p = A.fk_tissue_params(nx, ny, D=float(rng.uniform(5e-4, 1.5e-3)))
+        fk = A.fk_defaults()
+        u, v, w = W._ic(nx, ny, rng)
+        solid = None
+        if k in (1, 4):
+            solid = W.hole_mask(nx, ny, 4 + k, 2.0, 5.0, rng)
+            p.solidSwitch = True
+            for f in (u, v, w):
+                f[solid == 0] = 0.0
+        stims = [W.stim(13 + 29 * k, 0, 0, nx // 2, max(ny // 2, 1)),
+                 W.stim(130, nx // 3, 0, nx // 3 + 9, ny, 0.7)]
+        if k == 2:
+            stims.append(W.stim(211, 2, 2, 30, 30, 1.0))
+            stims.append(W.stim(211, 10, 10, 40, 60, 0.4))
+        out.append(W.Workload("r%d" % k, p, fk, A.YH_MODEL_FK3V, u, v, w,
+                              solid, stims, 0))
+    return out
+
+
+@pytest.mark.parametrize("cluster,levels", [(1, 0), (2, 0), (4, 0), (1, 1),
+                                            (2, 2), (4, 3), (2, 5), (1, 7)])
+@pytest.mark.parametrize("which", ["mixed", "ragged"])
+def test_wavefront_engine_gives_the_same_bits(cluster, levels, which):
+    # one persistent launch per run: 1, 2 or 4 CTAs per instance (bands of
+    # unequal width, neighbour columns through distributed shared memory),
+    # passes of 1-7 steps or as many as the rings allow (a short last pass),
+    # events on any level of a pass, mirror edges and holes
+    insts = _instances() if which == "mixed" else _ragged_instances()
+    runs = [130, 170]
+    b = Batch([w.p for w in insts], [w.fk for w in insts],
+              [w.solid for w in insts])
+    b.set_wave(cluster, levels)
+    cl, kcap, nclusters = b.wave()
+    assert cl == cluster and kcap == levels and nclusters >= 1
+    for k, w in enumerate(insts):
+        b.set_state(k, *w.state0())
+    ev = [(k, st) for k, w in enumerate(insts) for st in w.stims]
+    for n in runs:
+        b.run(n, ev)
+    b.synchronize()
+    assert b.launch_count() == len(runs)  # one launch per run
+    assert b.step_count() == sum(runs)
+    for k, wl in enumerate(insts):
+        got = b.get_state(k)
+        ref = _single(wl, runs)
+        for f in range(3):
+            assert np.array_equal(got[f], ref[f]), (cluster, levels, k, f)
+    b.close()
+
+
+def test_wavefront_engine_segments_and_switches_back():
+    # 7 events of one instance split the run into segments (a launch each);
+    # the grouped launches and the wavefront engine continue each other's
+    # state
+    wl = _instances()[3]
+    wl.stims = [W.stim(10 + 9 * q, q, q, q + 10, q + 12, 1.0 - 0.1 * q)
+                for q in range(7)]
+    b = Batch([wl.p], [wl.fk], [wl.solid])
+    b.set_wave(2)
+    b.set_state(0, *wl.state0())
+    b.run(60, [(0, s) for s in wl.stims])
+    b.set_depth(1)
+    assert b.wave()[0] == 0
+    b.run(41, [(0, s) for s in wl.stims])
+    b.set_wave(4, 6)
+    b.run(33, [(0, s) for s in wl.stims])
+    b.synchronize()
+    got = b.get_state(0)
+    ref = _single(wl, [60, 41, 33])
+    for f in range(3):
+        assert np.array_equal(got[f], ref[f]), f
+    with pytest.raises(YolohtliError) as e:
+        b.set_wave(3)
+    assert e.value.status == A.YH_EINVAL
+    b.close()
+    narrow = A.fk_tissue_params(12, 16)  # 3 quads: no band for a 4th CTA
+    b = Batch([narrow], [A.fk_defaults()])
+    with pytest.raises(YolohtliError) as e:
+        b.set_wave(4)
+    assert e.value.status == A.YH_EUNSUPPORTED
+    b.set_wave(2)
+    b.close()
+
+
+def test_wavefront_engine_on_the_benchmark_batch():
+    """fk_batch_256 (all 256 instances, holes, per-instance D and time
+    constants, the S2 moved inside the run) for 300 steps with the wavefront
+    engine at 2 CTAs per instance: every 16th instance and the largest ones
+    equal bit for bit to their single-grid solvers."""
+    bw = W.fk_batch_256(nsteps=300)
+    for w in bw.instances:
+        for s in w.stims:
+            s.step = 37 + s.step % 250
+    b = Batch([w.p for w in bw.instances], [w.fk for w in bw.instances],
+              [w.solid for w in bw.instances])
+    b.set_wave(2)
+    for k, w in enumerate(bw.instances):
+        b.set_state(k, *w.state0())
+    b.run(bw.nsteps, bw.stims())
+    b.synchronize()
+    assert b.launch_count() == 1
+    big = sorted(range(len(bw.instances)), key=lambda k: -bw.instances[k].cells)[:3]
+    for k in sorted(set(range(0, len(bw.instances), 16)) | set(big)):
+        got = b.get_state(k)
+        ref = _single(bw.instances[k], [bw.nsteps])
+        for f in range(3):
+            assert np.array_equal(got[f], ref[f]), (k, f)
+    b.close()
+
+
 def test_autotune_restores_the_state_and_keeps_the_bits():
     insts = _instances(seed=5)
     b = Batch([w.p for w in insts], [w.fk for w in insts],
@@ -122,8 +240,11 @@ def test_autotune_restores_the_state_and_keeps_the_bits():
     before = [b.get_state(k) for k in range(len(insts))]
     launches = b.launch_count()
     g, q, d = b.autotune(64)
-    assert g in (1 << 18, 1 << 19, 1 << 20, 1 << 21) and q in (2, 3, 4)
-    assert d in (1, 2)
+    if d == 0:  # the wavefront engine, q CTAs per instance
+        assert g == 0 and q in (1, 2, 4) and b.wave()[0] == q
+    else:
+        assert g in (1 << 18, 1 << 19, 1 << 20, 1 << 21) and q in (2, 3, 4)
+        assert d in (1, 2) and b.wave()[0] == 0
     assert b.step_count() == 100 and b.launch_count() == launches
     for k in range(len(insts)):
         now = b.get_state(k)

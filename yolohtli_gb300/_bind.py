@@ -89,6 +89,8 @@ SIGNATURES = {
     "yh_batch_set_schedule": (_i, [_v, C.c_longlong, _i]),
     "yh_batch_autotune": (_i, [_v, _i, _P(C.c_longlong), _P(_i), _P(_i)]),
     "yh_batch_set_depth": (_i, [_v, _i]),
+    "yh_batch_set_wave": (_i, [_v, _i, _i]),
+    "yh_batch_get_wave": (_i, [_v, _P(_i), _P(_i), _P(_i)]),
     "yh_batch_get_step": (_i, [_v, _P(_i)]),
     "yh_batch_set_step": (_i, [_v, _i]),
     "yh_batch_get_launch_count": (_i, [_v, _P(C.c_longlong)]),

@@ -2,7 +2,8 @@
 
 Many independent FK3V grids, each with its own size, parameters, hole mask
 and stimulus events, advanced together: one kernel launch per step for each
-group of instances that fits in the L2, the groups on several streams. Host
+group of instances that fits in the L2, the groups on several streams, or
+one persistent launch per run (the wavefront engine, set_wave). Host
 arrays are numpy FP32, flat nx*ny, row-major.
 """
 import ctypes as C
@@ -92,7 +93,8 @@ class Batch:
 
     def autotune(self, probe_steps=256):
         """Times the schedules on the current state (restored), keeps the
-        fastest; returns (group_cells, streams, steps per launch)."""
+        fastest; returns (group_cells, streams, steps per launch), or
+        (0, CTAs per instance, 0) for the wavefront engine."""
         g, q, d = C.c_longlong(), C.c_int(), C.c_int()
         check("yh_batch_autotune", self.lib.yh_batch_autotune(
             self.h, int(probe_steps), C.byref(g), C.byref(q), C.byref(d)))
@@ -101,6 +103,20 @@ class Batch:
     def set_depth(self, depth):
         """Steps per launch: 1, or 2 (TMA-staged 64 x 16 tiles)."""
         check("yh_batch_set_depth", self.lib.yh_batch_set_depth(self.h, int(depth)))
+
+    def set_wave(self, cluster, max_levels=0):
+        """The wavefront engine (one persistent launch per run segment) with
+        `cluster` CTAs per instance (1, 2 or 4; 0: grouped launches) and at
+        most max_levels steps per pass (0: as many as the rings allow)."""
+        check("yh_batch_set_wave", self.lib.yh_batch_set_wave(
+            self.h, int(cluster), int(max_levels)))
+
+    def wave(self):
+        """(CTAs per instance or 0, levels cap, clusters of the launch)."""
+        c, k, n = C.c_int(), C.c_int(), C.c_int()
+        check("yh_batch_get_wave", self.lib.yh_batch_get_wave(
+            self.h, C.byref(c), C.byref(k), C.byref(n)))
+        return c.value, k.value, n.value
 
     def synchronize(self):
         check("yh_batch_synchronize", self.lib.yh_batch_synchronize(self.h))

@@ -283,6 +283,293 @@ __global__ void __launch_bounds__(tile2s::kThreads)
                      ww, code4, rr, rc, ring_ok, rv, rw, rcode, hook);
 }
 
+// ---------------------------------------------------------------------------
+// The wavefront engine: one persistent launch runs a whole run segment of
+// every instance. Each instance goes to one cluster of CL CTAs (one CTA per
+// SM, the instance's columns split into CL bands of whole quads), which
+// advances it K steps per pass with the state in shared memory:
+//
+//   level k (0 <= k < L, L = min(K, steps left)) computes step s0 + k;
+//   at wavefront position p it computes row p - 2k of its band.
+//
+// Row r + 1 of level k's input is level k - 1's output of position p - 1,
+// so one barrier per position orders every dependency. Level 0 reads the
+// state of step s0 (rows staged from global memory by cp.async kAhead
+// positions ahead), level L - 1 writes step s0 + L back in place, and the
+// levels between exchange rows in shared-memory rings of R rows (a power of
+// two, R >= 2K + kAhead, so that no ring slot is overwritten while it is
+// read):
+// u by step parity (level k reads ring k & 1 and writes ring (k + 1) & 1),
+// v, w and the hole codes in one ring each, updated in place. A band's
+// west and east neighbour columns come from the neighbouring CTAs: level 0
+// stages them with its rows, and every other level's writer of a band's
+// first or last quad stores its value into the neighbour's ring
+// (distributed shared memory). Those stores are read two positions later;
+// a split cluster barrier (wait for the previous position, arrive for this
+// one) orders them. Every cell update is fk3v_cells4 on the values the
+// single-step kernel reads (events applied to the read values), so the
+// engine gives the same bits as one launch per step. State traffic per
+// pass: 25 bytes a cell for L steps.
+namespace wave {
+
+#ifndef YH_WAVE_THREADS
+#define YH_WAVE_THREADS 512
+#endif
+#ifndef YH_WAVE_AHEAD
+#define YH_WAVE_AHEAD 3
+#endif
+constexpr int kThreads = YH_WAVE_THREADS;
+constexpr int kMaxRing = 128;
+// Rows staged ahead of level 0 (>= 3): row x is requested at position
+// x - kAhead and must have landed by position x - 1.
+constexpr int kAhead = YH_WAVE_AHEAD;
+static_assert(kAhead >= 3 && kAhead <= 10, "kAhead out of range");
+
+__device__ __forceinline__ uint32_t sptr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void cp16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sptr(dst)),
+               "l"(__cvta_generic_to_global(src))
+               : "memory");
+}
+__device__ __forceinline__ void cp4(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sptr(dst)),
+               "l"(__cvta_generic_to_global(src))
+               : "memory");
+}
+__device__ __forceinline__ void cp_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+// Waits until at most the kAhead - 2 most recent groups are in flight.
+__device__ __forceinline__ void cp_wait_staged() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(kAhead - 2) : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_arrive() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// Stores v at the address of `local` in CTA `rank` of this cluster.
+__device__ __forceinline__ void st_peer(const float *local, uint32_t rank,
+                                        float v) {
+  uint32_t ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+               : "=r"(ra)
+               : "r"(sptr(local)), "r"(rank));
+  asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(ra), "f"(v)
+               : "memory");
+}
+
+// Band of CTA `rank`: quads [band_first, band_first + band_quads) of nq.
+__host__ __device__ inline int band_quads(int nq, int cl, int rank) {
+  return nq / cl + (rank < nq % cl ? 1 : 0);
+}
+__host__ __device__ inline int band_first(int nq, int cl, int rank) {
+  return rank * (nq / cl) + (rank < nq % cl ? rank : nq % cl);
+}
+// Bytes of one ring row for bands of at most nqm quads: u in two parities
+// (4 nqm + 8 floats: the west neighbour at 3, the band at 4.., the east
+// neighbour after it), v, w (4 nqm floats) and the hole codes (4 nqm bytes).
+__host__ __device__ inline int ring_row_bytes(int nqm) {
+  return 8 * (4 * nqm + 8) + 32 * nqm + 4 * nqm;
+}
+// Ring rows that fit `smem` bytes (a power of two, 8 .. kMaxRing), or 0.
+__host__ __device__ inline int ring_rows(int nqm, int smem) {
+  int R = kMaxRing;
+  while (R > 8 && R * ring_row_bytes(nqm) > smem) R >>= 1;
+  return R * ring_row_bytes(nqm) <= smem ? R : 0;
+}
+// Levels per pass for R ring rows (R >= 2K + kAhead), at most kcap (0: no
+// cap).
+__host__ __device__ inline int levels(int R, int kcap) {
+  const int k = (R - kAhead) / 2;
+  return kcap > 0 && kcap < k ? kcap : k;
+}
+
+__device__ __forceinline__ float4 lds4(const float *p) {
+  return *reinterpret_cast<const float4 *>(p);
+}
+__device__ __forceinline__ void sts4(float *p, const float (&x)[4]) {
+  *reinterpret_cast<float4 *>(p) = make_float4(x[0], x[1], x[2], x[3]);
+}
+
+template <int CL>
+__global__ void __launch_bounds__(kThreads, 1)
+    rd_batch_wave_kernel(const BatchInst *__restrict__ insts,
+                         const int *__restrict__ list,
+                         const int *__restrict__ beg, Fld<float> st,
+                         const uint8_t *__restrict__ codes, int base, int len,
+                         int smem, int kcap) {
+  extern __shared__ __align__(16) float ring[];
+  __shared__ BatchInst I;
+  const int t = threadIdx.x;
+  const int rank = CL > 1 ? (int)cluster_rank() : 0;
+  const int cl = blockIdx.x / CL;
+  for (int li = beg[cl]; li < beg[cl + 1]; ++li) {
+    // every CTA of the cluster is done with the previous instance's rings
+    if (CL > 1) {
+      cluster_arrive();
+      cluster_wait();
+    } else {
+      __syncthreads();
+    }
+    {
+      const int *src = reinterpret_cast<const int *>(insts + list[li]);
+      int *dst = reinterpret_cast<int *>(&I);
+      for (int k = t; k < (int)(sizeof(BatchInst) / 4); k += kThreads)
+        dst[k] = __ldg(src + k);
+    }
+    __syncthreads();
+    const StepCoeffs<float> &a = I.a;
+    const FkPairs fc(a);  // in registers for the whole instance
+    const int nx = a.nx, ny = a.ny, nq = nx >> 2;
+    const int nqb = band_quads(nq, CL, rank), q0 = band_first(nq, CL, rank);
+    const int nqm = (nq + CL - 1) / CL;
+    const int nqw = CL > 1 && rank > 0 ? band_quads(nq, CL, rank - 1) : 0;
+    const int su = 4 * nqm + 8, sv = 4 * nqm;
+    const int R = ring_rows(nqm, smem), K = levels(R, kcap);
+    float *U0 = ring, *U1 = ring + R * su;
+    float *Vr = ring + 2 * R * su, *Wr = Vr + R * sv;
+    uint8_t *Cr = reinterpret_cast<uint8_t *>(Wr + R * sv);
+    const bool holes = I.holes != 0;
+    const int hq = holes ? nqb : 0;
+    const int nops = 3 * nqb + hq + 2;
+    const size_t off = (size_t)I.off;
+    float *const gu = st.f[0] + off, *const gv = st.f[1] + off,
+                 *const gw = st.f[2] + off;
+    const uint8_t *const gc = codes + off;
+    const int dq = kThreads % nqb, dk = kThreads / nqb;
+    // stages row x of the pass's first state (band, its neighbour columns,
+    // v, w, hole codes) into ring slot x & (R - 1)
+    auto stage = [&](int x) {
+      if (x >= ny) return;
+      const int sx = x & (R - 1);
+      const size_t g = (size_t)nx * x + 4 * q0;
+      for (int o = t; o < nops; o += kThreads) {
+        if (o < nqb) {
+          cp16(U0 + sx * su + 4 + 4 * o, gu + g + 4 * o);
+        } else if (o < 2 * nqb) {
+          cp16(Vr + sx * sv + 4 * (o - nqb), gv + g + 4 * (o - nqb));
+        } else if (o < 3 * nqb) {
+          cp16(Wr + sx * sv + 4 * (o - 2 * nqb), gw + g + 4 * (o - 2 * nqb));
+        } else if (o < 3 * nqb + hq) {
+          cp4(Cr + sx * sv + 4 * (o - 3 * nqb), gc + g + 4 * (o - 3 * nqb));
+        } else if (o == 3 * nqb + hq) {
+          if (rank > 0) cp4(U0 + sx * su + 3, gu + g - 1);
+        } else if (rank < CL - 1) {
+          cp4(U0 + sx * su + 4 + 4 * nqb, gu + g + 4 * nqb);
+        }
+      }
+    };
+    for (int done = 0; done < len;) {
+      const int L = min(K, len - done), s0 = base + done;
+      const int npos = ny + 2 * (L - 1);
+      for (int x = 0; x < kAhead; ++x) {
+        stage(x);
+        cp_commit();
+      }
+      cp_wait_staged();  // rows 0 and 1
+      __syncthreads();
+      if (CL > 1) cluster_arrive();
+      for (int p = 0; p < npos; ++p) {
+        stage(p + kAhead);
+        cp_commit();
+        const int klo = p >= ny ? (p - ny + 2) >> 1 : 0;
+        const int khi = min(L - 1, p >> 1);
+        const int nit = (khi - klo + 1) * nqb;
+        int k = klo + t / nqb, q = t % nqb;
+        for (int it = t; it < nit; it += kThreads) {
+          const int r = p - 2 * k;
+          const int jN = mirror(r + 1, ny), jS = mirror(r - 1, ny);
+          const float *Ui = (k & 1) ? U1 : U0;
+          const int s = r & (R - 1);
+          const float *c0 = Ui + s * su + 4 + 4 * q;
+          const float4 uc = lds4(c0);
+          const float4 unq = lds4(Ui + (jN & (R - 1)) * su + 4 + 4 * q);
+          const float4 usq = lds4(Ui + (jS & (R - 1)) * su + 4 + 4 * q);
+          const int i0 = 4 * (q0 + q);
+          float uw = i0 == 0 ? uc.y : c0[-1];       // x = -1 mirrors x = 1
+          float ue = i0 + 4 == nx ? uc.z : c0[4];   // x = nx mirrors nx - 2
+          float u[4] = {uc.x, uc.y, uc.z, uc.w};
+          float uN[4] = {unq.x, unq.y, unq.z, unq.w};
+          float uS[4] = {usq.x, usq.y, usq.z, usq.w};
+          const float4 v4 = lds4(Vr + s * sv + 4 * q);
+          const float4 w4 = lds4(Wr + s * sv + 4 * q);
+          const uint32_t code4 =
+              holes ? *reinterpret_cast<const uint32_t *>(Cr + s * sv + 4 * q)
+                    : 0x01010101u;
+          if (I.nev) {
+            const int gs = s0 + k;
+            const int iw = mirror(i0 - 1, nx), ie = mirror(i0 + 4, nx);
+            for (int e = 0; e < I.nev; ++e) {
+              const yh_stim &ev = I.ev[e];
+              if (ev.step != gs) continue;
+#pragma unroll
+              for (int c = 0; c < 4; ++c) {
+                if (in_box(ev, i0 + c, r)) u[c] = ev.value;
+                if (in_box(ev, i0 + c, jN)) uN[c] = ev.value;
+                if (in_box(ev, i0 + c, jS)) uS[c] = ev.value;
+              }
+              if (in_box(ev, iw, r)) uw = ev.value;
+              if (in_box(ev, ie, r)) ue = ev.value;
+            }
+          }
+          const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+          const float ww[4] = {w4.x, w4.y, w4.z, w4.w};
+          float ou[4], ov[4], ow[4];
+          fk3v_cells4(a, fc, code4 == 0x01010101u, code4, u, uw, ue, uN, uS,
+                      vv, ww, ou, ov, ow);
+          if (k == L - 1) {
+            const size_t g = (size_t)nx * r + i0;
+            *reinterpret_cast<float4 *>(gu + g) = make_float4(ou[0], ou[1], ou[2], ou[3]);
+            *reinterpret_cast<float4 *>(gv + g) = make_float4(ov[0], ov[1], ov[2], ov[3]);
+            *reinterpret_cast<float4 *>(gw + g) = make_float4(ow[0], ow[1], ow[2], ow[3]);
+          } else {
+            float *Uo = ((k & 1) ? U0 : U1) + s * su;
+            sts4(Uo + 4 + 4 * q, ou);
+            sts4(Vr + s * sv + 4 * q, ov);
+            sts4(Wr + s * sv + 4 * q, ow);
+            if (CL > 1) {
+              if (q == 0 && rank > 0)
+                st_peer(Uo + 4 + 4 * nqw, (uint32_t)(rank - 1), ou[0]);
+              if (q == nqb - 1 && rank < CL - 1)
+                st_peer(Uo + 3, (uint32_t)(rank + 1), ou[3]);
+            }
+          }
+          q += dq;
+          k += dk;
+          if (q >= nqb) {
+            q -= nqb;
+            ++k;
+          }
+        }
+        cp_wait_staged();  // row p + 2, read from position p + 1 on
+        __syncthreads();
+        if (CL > 1) {
+          cluster_wait();
+          cluster_arrive();
+        }
+      }
+      if (CL > 1) cluster_wait();
+      done += L;
+    }
+  }
+  // a CTA's shared memory must outlive its peers' stores into it
+  if (CL > 1) {
+    cluster_arrive();
+    cluster_wait();
+  }
+}
+
+}  // namespace wave
+
 __global__ void batch_set_base(int *base, int value) { *base = value; }
 
 inline int st(cudaError_t e) {
@@ -328,6 +615,13 @@ struct yh_batch {
   std::vector<int> ubeg2, uend2;
   std::vector<cudaGraphExec_t> graphs2;  // [group][starting level]
   int *d_err = nullptr;          // set when a TMA wait gave up
+  // the wavefront engine (0: off; else CTAs per instance) and its plan:
+  // instances by cluster (d_wlist[d_wbeg[c] .. d_wbeg[c + 1]))
+  int wave = 0;
+  int wave_kcap = 0;             // levels per pass at most (0: no cap)
+  int wave_smem = 0;             // dynamic shared memory per CTA
+  int wave_clusters = 0;
+  int *d_wlist = nullptr, *d_wbeg = nullptr;
 };
 
 namespace {
@@ -429,7 +723,10 @@ int graph_for2(yh_batch *b, int g, int lvl, cudaStream_t s,
 // `len` steps of every group from b->step with the events currently in the
 // records; groups run on the internal streams, forked from and joined to
 // the caller's stream.
+int run_segment_wave(yh_batch *b, int len);
+
 int run_segment(yh_batch *b, int len) {
+  if (b->wave) return run_segment_wave(b, len);
   cudaError_t e = cudaEventRecord(b->fork, b->s);
   for (int q = 0; q < b->nstreams && e == cudaSuccess; ++q)
     e = cudaStreamWaitEvent(b->streams[q], b->fork, 0);
@@ -593,6 +890,131 @@ int plan_schedule(yh_batch *b, long long group_cells, int nstreams) {
   return st(e);
 }
 
+template <int CL>
+cudaError_t wave_attrs(int smem) {
+  return cudaFuncSetAttribute(wave::rd_batch_wave_kernel<CL>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+cudaLaunchConfig_t wave_config(int cl, int clusters, int smem, cudaStream_t s,
+                               cudaLaunchAttribute *attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cl * clusters);
+  cfg.blockDim = dim3(wave::kThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
+// The wavefront engine's plan for `cl` CTAs per instance: the shared
+// memory per CTA (the most the device allows beside the kernel's static
+// record), the clusters that fit on the device at once (one CTA per SM),
+// and the instances' assignment to clusters: longest first, each to the
+// cluster with the least work so far (work ~ rows x (ny + 2K) / K per step,
+// the positions a pass takes per step). YH_EUNSUPPORTED where an
+// instance's band is narrower than a quad or its rings hold fewer than 8
+// rows.
+int plan_wave(yh_batch *b, int cl, int kcap) {
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa = {};
+  if (e == cudaSuccess)
+    e = cl == 1 ? cudaFuncGetAttributes(&fa, wave::rd_batch_wave_kernel<1>)
+                : cl == 2 ? cudaFuncGetAttributes(&fa, wave::rd_batch_wave_kernel<2>)
+                          : cudaFuncGetAttributes(&fa, wave::rd_batch_wave_kernel<4>);
+  if (e != cudaSuccess) return st(e);
+  const int smem = ((optin - (int)fa.sharedSizeBytes - 1024) / 1024) * 1024;
+  std::vector<double> work(b->count);
+  for (int k = 0; k < b->count; ++k) {
+    const int nq = b->inst[k].a.nx / 4, ny = b->inst[k].a.ny;
+    if (nq < cl) return YH_EUNSUPPORTED;
+    const int nqm = (nq + cl - 1) / cl;
+    const int R = wave::ring_rows(nqm, smem);
+    if (R < 8) return YH_EUNSUPPORTED;
+    const int K = wave::levels(R, kcap);
+    work[k] = (double)nqm * (ny + 2 * K + 4) / K;
+  }
+  e = cl == 1 ? wave_attrs<1>(smem) : cl == 2 ? wave_attrs<2>(smem) : wave_attrs<4>(smem);
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = wave_config(cl, 1, smem, b->s, attr);
+  int clusters = 0;
+  if (e == cudaSuccess)
+    e = cl == 1 ? cudaOccupancyMaxActiveClusters(&clusters, wave::rd_batch_wave_kernel<1>, &cfg)
+        : cl == 2 ? cudaOccupancyMaxActiveClusters(&clusters, wave::rd_batch_wave_kernel<2>, &cfg)
+                  : cudaOccupancyMaxActiveClusters(&clusters, wave::rd_batch_wave_kernel<4>, &cfg);
+  if (e != cudaSuccess) return st(e);
+  if (clusters < 1) return YH_EUNSUPPORTED;
+  std::vector<int> order(b->count);
+  for (int k = 0; k < b->count; ++k) order[k] = k;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return work[x] > work[y]; });
+  std::vector<std::vector<int>> per(clusters);
+  std::vector<double> load(clusters, 0.0);
+  for (int k : order) {
+    const int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    per[c].push_back(k);
+    load[c] += work[k];
+  }
+  std::vector<int> list, beg(1, 0);
+  for (const auto &v : per) {
+    list.insert(list.end(), v.begin(), v.end());
+    beg.push_back((int)list.size());
+  }
+  e = cudaStreamSynchronize(b->s);  // no launch reads the old plan
+  if (e != cudaSuccess) return st(e);
+  cudaFree(b->d_wlist);
+  cudaFree(b->d_wbeg);
+  b->d_wlist = b->d_wbeg = nullptr;
+  e = cudaMalloc(&b->d_wlist, list.size() * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_wbeg, beg.size() * sizeof(int));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_wlist, list.data(), list.size() * sizeof(int),
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_wbeg, beg.data(), beg.size() * sizeof(int),
+                   cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return st(e);
+  b->wave = cl;
+  b->wave_kcap = kcap;
+  b->wave_smem = smem;
+  b->wave_clusters = clusters;
+  return YH_OK;
+}
+
+// `len` steps of every instance in one launch of the wavefront engine, the
+// state updated in place.
+int run_segment_wave(yh_batch *b, int len) {
+  cudaLaunchAttribute attr[1];
+  const cudaLaunchConfig_t cfg =
+      wave_config(b->wave, b->wave_clusters, b->wave_smem, b->s, attr);
+  const Fld<float> f = level(b, b->cur);
+  const BatchInst *ins = b->d_inst;
+  const int *wl = b->d_wlist, *wb = b->d_wbeg;
+  const uint8_t *codes = b->codes;
+  cudaError_t e;
+  if (b->wave == 1)
+    e = cudaLaunchKernelEx(&cfg, wave::rd_batch_wave_kernel<1>, ins, wl, wb, f,
+                           codes, b->step, len, b->wave_smem, b->wave_kcap);
+  else if (b->wave == 2)
+    e = cudaLaunchKernelEx(&cfg, wave::rd_batch_wave_kernel<2>, ins, wl, wb, f,
+                           codes, b->step, len, b->wave_smem, b->wave_kcap);
+  else
+    e = cudaLaunchKernelEx(&cfg, wave::rd_batch_wave_kernel<4>, ins, wl, wb, f,
+                           codes, b->step, len, b->wave_smem, b->wave_kcap);
+  if (e != cudaSuccess) return st(e);
+  b->launches += 1;
+  b->step += len;
+  return YH_OK;
+}
+
 // Copies the records (with this segment's events) to the device.
 int upload_records(yh_batch *b) {
   cudaError_t e = cudaStreamSynchronize(b->s);  // the staging copy is free
@@ -643,6 +1065,8 @@ extern "C" int yh_batch_destroy(yh_batch *b) {
   cudaFree(b->d_maps);
   cudaFree(b->d_err);
   cudaFree(b->d_base);
+  cudaFree(b->d_wlist);
+  cudaFree(b->d_wbeg);
   if (b->own_stream && b->s) cudaStreamDestroy(b->s);
   delete b;
   return YH_OK;
@@ -775,6 +1199,29 @@ extern "C" int yh_batch_set_depth(yh_batch *b, int depth) {
   const cudaError_t e = cudaStreamSynchronize(b->s);
   if (e != cudaSuccess) return st(e);
   b->depth = depth;
+  b->wave = 0;
+  return YH_OK;
+}
+
+extern "C" int yh_batch_set_wave(yh_batch *b, int cluster, int max_levels) {
+  if (!b || max_levels < 0 ||
+      (cluster != 0 && cluster != 1 && cluster != 2 && cluster != 4))
+    return YH_EINVAL;
+  if (cluster == 0) {
+    const cudaError_t e = cudaStreamSynchronize(b->s);
+    if (e != cudaSuccess) return st(e);
+    b->wave = 0;
+    return YH_OK;
+  }
+  return plan_wave(b, cluster, max_levels);
+}
+
+extern "C" int yh_batch_get_wave(yh_batch *b, int *cluster, int *max_levels,
+                                 int *clusters) {
+  if (!b) return YH_EINVAL;
+  if (cluster) *cluster = b->wave;
+  if (max_levels) *max_levels = b->wave_kcap;
+  if (clusters) *clusters = b->wave ? b->wave_clusters : 0;
   return YH_OK;
 }
 
@@ -896,24 +1343,29 @@ extern "C" int yh_batch_autotune(yh_batch *b, int probe_steps,
   const long long sizes[] = {1 << 18, 1 << 19, 1 << 20, 1 << 21};
   const int counts[] = {2, 3, 4};
   long long best_g = kBatchGroupCells;
-  int best_s = kBatchStreams, best_d = 1, rc = st(e);
+  int best_s = kBatchStreams, best_d = 1, best_w = 0, rc = st(e);
   float best_ms = 3.4e38f;
+  // the first run captures the groups' graphs; the second is timed
+  auto probe = [&](float *ms) {
+    int r = yh_batch_run(b, probe_steps, nullptr, 0);
+    if (!r) r = st(restore());
+    if (!r) r = st(cudaEventRecord(t0, b->s));
+    if (!r) r = yh_batch_run(b, probe_steps, nullptr, 0);
+    if (!r) r = st(cudaEventRecord(t1, b->s));
+    if (!r) r = st(cudaEventSynchronize(t1));
+    if (!r) r = st(cudaEventElapsedTime(ms, t0, t1));
+    if (!r) r = st(restore());
+    return r;
+  };
   for (int d = 1; d <= (b->tma2 ? 2 : 1); ++d)
   for (long long g : sizes)
     for (int q : counts) {
       if (rc) break;
       b->depth = d;
+      b->wave = 0;
       rc = plan_schedule(b, g, q);
-      // the first run captures the groups' graphs; the second is timed
-      if (!rc) rc = yh_batch_run(b, probe_steps, nullptr, 0);
-      if (!rc) rc = st(restore());
-      if (!rc) rc = st(cudaEventRecord(t0, b->s));
-      if (!rc) rc = yh_batch_run(b, probe_steps, nullptr, 0);
-      if (!rc) rc = st(cudaEventRecord(t1, b->s));
-      if (!rc) rc = st(cudaEventSynchronize(t1));
       float ms = 0.f;
-      if (!rc) rc = st(cudaEventElapsedTime(&ms, t0, t1));
-      if (!rc) rc = st(restore());
+      if (!rc) rc = probe(&ms);
       if (!rc && ms < best_ms) {
         best_ms = ms;
         best_g = g;
@@ -921,8 +1373,23 @@ extern "C" int yh_batch_autotune(yh_batch *b, int probe_steps,
         best_d = d;
       }
     }
+  // the wavefront engine with 1, 2 or 4 CTAs per instance
+  for (int cl : {1, 2, 4}) {
+    if (rc) break;
+    const int pr = plan_wave(b, cl, 0);
+    if (pr == YH_EUNSUPPORTED) continue;
+    rc = pr;
+    float ms = 0.f;
+    if (!rc) rc = probe(&ms);
+    if (!rc && ms < best_ms) {
+      best_ms = ms;
+      best_w = cl;
+    }
+  }
+  b->wave = 0;
   b->depth = best_d;
   if (!rc) rc = plan_schedule(b, best_g, best_s);
+  if (!rc && best_w) rc = plan_wave(b, best_w, 0);
   if (!rc) rc = st(restore());
   if (!rc) rc = st(cudaStreamSynchronize(b->s));
   b->launches = launches0;
@@ -930,15 +1397,16 @@ extern "C" int yh_batch_autotune(yh_batch *b, int probe_steps,
   if (t1) cudaEventDestroy(t1);
   cudaFree(snap);
   if (rc) return rc;
-  if (group_cells) *group_cells = best_g;
-  if (streams) *streams = best_s;
-  if (depth) *depth = best_d;
+  if (group_cells) *group_cells = best_w ? 0 : best_g;
+  if (streams) *streams = best_w ? best_w : best_s;
+  if (depth) *depth = best_w ? 0 : best_d;
   return YH_OK;
 }
 
 extern "C" int yh_batch_set_schedule(yh_batch *b, long long group_cells,
                                      int streams) {
   if (!b || group_cells <= 0 || streams <= 0 || streams > 64) return YH_EINVAL;
+  b->wave = 0;
   return plan_schedule(b, group_cells, streams);
 }
 

@@ -222,36 +222,116 @@ __device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
   return d;
 }
 
+// Coefficients of the packed FK3V update as f32x2 lane pairs (each value
+// in both lanes) and the scalars of its lane selects, read through one
+// interface from two sources: FkPairsAt builds each pair where it is used
+// (from the coefficients in a kernel parameter or shared memory), FkPairs
+// holds them built once, for a kernel that updates many cells per thread
+// and keeps them in registers. Both give the same values.
+struct FkPairsAt {
+  const StepCoeffs<float> &a;
+  __device__ __forceinline__ F2 one() const { return f2(1.f); }
+  __device__ __forceinline__ F2 m2() const { return f2(-2.f); }
+  __device__ __forceinline__ F2 u_csi() const { return f2(a.u_csi); }
+  __device__ __forceinline__ F2 k_exp2() const { return f2(a.k_exp2); }
+  __device__ __forceinline__ F2 u_c() const { return f2(a.u_c); }
+  __device__ __forceinline__ F2 m_s_td() const { return f2(-a.s_td); }
+  __device__ __forceinline__ F2 s_tr() const { return f2(a.s_tr); }
+  __device__ __forceinline__ F2 s_to() const { return f2(a.s_to); }
+  __device__ __forceinline__ F2 m_s_tsi() const { return f2(-a.s_tsi); }
+  __device__ __forceinline__ F2 tc() const { return f2(a.tc); }
+  __device__ __forceinline__ F2 m_s_tvp() const { return f2(-a.s_tvp); }
+  __device__ __forceinline__ F2 m_s_twp() const { return f2(-a.s_twp); }
+  __device__ __forceinline__ F2 s_twm() const { return f2(a.s_twm); }
+  __device__ __forceinline__ F2 rx() const { return f2(a.rx); }
+  __device__ __forceinline__ F2 ry() const { return f2(a.ry); }
+  __device__ __forceinline__ float u_c1() const { return a.u_c; }
+  __device__ __forceinline__ float u_v1() const { return a.u_v; }
+  __device__ __forceinline__ float s_tv1m() const { return a.s_tv1m; }
+  __device__ __forceinline__ float s_tv2m() const { return a.s_tv2m; }
+};
+struct FkPairs {
+  F2 p_one, p_m2, p_u_csi, p_k_exp2, p_u_c, p_m_s_td, p_s_tr, p_s_to,
+      p_m_s_tsi, p_tc, p_m_s_tvp, p_m_s_twp, p_s_twm, p_rx, p_ry;
+  float p_u_c1, p_u_v1, p_s_tv1m, p_s_tv2m;
+  __device__ __forceinline__ explicit FkPairs(const StepCoeffs<float> &a) {
+    const FkPairsAt c{a};
+    p_one = c.one();
+    p_m2 = c.m2();
+    p_u_csi = c.u_csi();
+    p_k_exp2 = c.k_exp2();
+    p_u_c = c.u_c();
+    p_m_s_td = c.m_s_td();
+    p_s_tr = c.s_tr();
+    p_s_to = c.s_to();
+    p_m_s_tsi = c.m_s_tsi();
+    p_tc = c.tc();
+    p_m_s_tvp = c.m_s_tvp();
+    p_m_s_twp = c.m_s_twp();
+    p_s_twm = c.s_twm();
+    p_rx = c.rx();
+    p_ry = c.ry();
+    p_u_c1 = c.u_c1();
+    p_u_v1 = c.u_v1();
+    p_s_tv1m = c.s_tv1m();
+    p_s_tv2m = c.s_tv2m();
+  }
+  __device__ __forceinline__ F2 one() const { return p_one; }
+  __device__ __forceinline__ F2 m2() const { return p_m2; }
+  __device__ __forceinline__ F2 u_csi() const { return p_u_csi; }
+  __device__ __forceinline__ F2 k_exp2() const { return p_k_exp2; }
+  __device__ __forceinline__ F2 u_c() const { return p_u_c; }
+  __device__ __forceinline__ F2 m_s_td() const { return p_m_s_td; }
+  __device__ __forceinline__ F2 s_tr() const { return p_s_tr; }
+  __device__ __forceinline__ F2 s_to() const { return p_s_to; }
+  __device__ __forceinline__ F2 m_s_tsi() const { return p_m_s_tsi; }
+  __device__ __forceinline__ F2 tc() const { return p_tc; }
+  __device__ __forceinline__ F2 m_s_tvp() const { return p_m_s_tvp; }
+  __device__ __forceinline__ F2 m_s_twp() const { return p_m_s_twp; }
+  __device__ __forceinline__ F2 s_twm() const { return p_s_twm; }
+  __device__ __forceinline__ F2 rx() const { return p_rx; }
+  __device__ __forceinline__ F2 ry() const { return p_ry; }
+  __device__ __forceinline__ float u_c1() const { return p_u_c1; }
+  __device__ __forceinline__ float u_v1() const { return p_u_v1; }
+  __device__ __forceinline__ float s_tv1m() const { return p_s_tv1m; }
+  __device__ __forceinline__ float s_tv2m() const { return p_s_tv2m; }
+};
+
 // fk3v_update of two cells, the same operations lane by lane in f32x2.
+template <class CP>
+__device__ __forceinline__ void fk3v_update2(const CP &c, F2 U, F2 V, F2 W,
+                                             F2 D, F2 &UN, F2 &VN, F2 &WN) {
+  float u0, u1;
+  f2_split(U, u0, u1);
+  const bool p0 = u0 >= c.u_c1(), p1 = u1 >= c.u_c1();
+  const bool q0 = u0 >= c.u_v1(), q1 = u1 >= c.u_v1();
+  const F2 x = mul2(sub2(U, c.u_csi()), c.k_exp2());
+  float x0, x1, e0, e1;
+  f2_split(x, x0, x1);
+  f2_split(add2(f2(ex2_approx(x0), ex2_approx(x1)), c.one()), e0, e1);
+  const F2 sig = f2(rcp_approx(e0), rcp_approx(e1));
+  const F2 a4 = mul2(V, mul2(sub2(c.one(), U), sub2(U, c.u_c())));
+  float jp0, jp1, jn0, jn1;
+  f2_split(fma2(a4, c.m_s_td(), c.s_tr()), jp0, jp1);
+  f2_split(mul2(U, c.s_to()), jn0, jn1);
+  const F2 Jd = fma2(mul2(W, sig), c.m_s_tsi(),
+                     f2(p0 ? jp0 : jn0, p1 ? jp1 : jn1));
+  UN = sub2(fma2(D, c.tc(), U), Jd);
+  float vp0, vp1, vm0, vm1, wp0, wp1, wm0, wm1;
+  f2_split(fma2(V, c.m_s_tvp(), V), vp0, vp1);
+  f2_split(fma2(sub2(c.one(), V),
+                f2(q0 ? c.s_tv1m() : c.s_tv2m(), q1 ? c.s_tv1m() : c.s_tv2m()),
+                V),
+           vm0, vm1);
+  VN = f2(p0 ? vp0 : vm0, p1 ? vp1 : vm1);
+  f2_split(fma2(W, c.m_s_twp(), W), wp0, wp1);
+  f2_split(fma2(sub2(c.one(), W), c.s_twm(), W), wm0, wm1);
+  WN = f2(p0 ? wp0 : wm0, p1 ? wp1 : wm1);
+}
 __device__ __forceinline__ void fk3v_update2(const StepCoeffs<float> &a, F2 U,
                                              F2 V, F2 W, F2 D, F2 &UN, F2 &VN,
                                              F2 &WN) {
-  float u0, u1, v0, v1, w0, w1;
-  f2_split(U, u0, u1);
-  const bool p0 = u0 >= a.u_c, p1 = u1 >= a.u_c;
-  const bool q0 = u0 >= a.u_v, q1 = u1 >= a.u_v;
-  const F2 one = f2(1.f);
-  const F2 x = mul2(sub2(U, f2(a.u_csi)), f2(a.k_exp2));
-  float x0, x1, e0, e1;
-  f2_split(x, x0, x1);
-  f2_split(add2(f2(ex2_approx(x0), ex2_approx(x1)), one), e0, e1);
-  const F2 sig = f2(rcp_approx(e0), rcp_approx(e1));
-  const F2 a4 = mul2(V, mul2(sub2(one, U), sub2(U, f2(a.u_c))));
-  float jp0, jp1, jn0, jn1;
-  f2_split(fma2(a4, f2(-a.s_td), f2(a.s_tr)), jp0, jp1);
-  f2_split(mul2(U, f2(a.s_to)), jn0, jn1);
-  const F2 Jd = fma2(mul2(W, sig), f2(-a.s_tsi), f2(p0 ? jp0 : jn0, p1 ? jp1 : jn1));
-  UN = sub2(fma2(D, f2(a.tc), U), Jd);
-  float vp0, vp1, vm0, vm1, wp0, wp1, wm0, wm1;
-  f2_split(fma2(V, f2(-a.s_tvp), V), vp0, vp1);
-  f2_split(fma2(sub2(one, V),
-                f2(q0 ? a.s_tv1m : a.s_tv2m, q1 ? a.s_tv1m : a.s_tv2m), V),
-           vm0, vm1);
-  VN = f2(p0 ? vp0 : vm0, p1 ? vp1 : vm1);
-  f2_split(fma2(W, f2(-a.s_twp), W), wp0, wp1);
-  f2_split(fma2(sub2(one, W), f2(a.s_twm), W), wm0, wm1);
-  WN = f2(p0 ? wp0 : wm0, p1 ? wp1 : wm1);
-  (void)v0; (void)v1; (void)w0; (void)w1;
+  fk3v_update2(FkPairsAt{a}, U, V, W, D, UN, VN, WN);
 }
 
 // Scaled 5-point Laplacian rx (lo - 2c + hi)_x + ry (lo - 2c + hi)_y with
@@ -269,28 +349,14 @@ __device__ __forceinline__ float lap5(const StepCoeffs<float> &a, float hx,
                                       float hy) {
   return __fmaf_rn(hx, a.rx, __fmul_rn(hy, a.ry));
 }
-__device__ __forceinline__ F2 lap5_2(const StepCoeffs<float> &a, F2 W, F2 C,
-                                     F2 E, F2 N, F2 S) {
-  const F2 m2 = f2(-2.f);
-  const F2 hx = add2(fma2(m2, C, W), E);
-  const F2 hy = add2(fma2(m2, C, N), S);
-  return fma2(hx, f2(a.rx), mul2(hy, f2(a.ry)));
+template <class CP>
+__device__ __forceinline__ F2 lap5_2(const CP &c, F2 W, F2 C, F2 E, F2 N,
+                                     F2 S) {
+  const F2 hx = add2(fma2(c.m2(), C, W), E);
+  const F2 hy = add2(fma2(c.m2(), C, N), S);
+  return fma2(hx, c.rx(), mul2(hy, c.ry()));
 }
 
-// FK3V update of 4 consecutive cells (u[k], with west/east neighbours uw,
-// ue and the rows above/below un, us). plain: all four cells tissue with
-// tissue neighbours; else `code` holds the four hole codes (byte k: bit 0
-// tissue, bits 1-2 x pattern, bits 3-4 y pattern) and cells outside tissue
-// are set to 0.
-__device__ __forceinline__ void fk3v_cells4(const StepCoeffs<float> &a,
-                                            bool plain, uint32_t code,
-                                            const float (&u)[4], float uw,
-                                            float ue, const float (&un)[4],
-                                            const float (&us)[4],
-                                            const float (&v)[4],
-                                            const float (&w)[4],
-                                            float (&ou)[4], float (&ov)[4],
-                                            float (&ow)[4]);
 
 // Hole pattern of one axis as 2 bits: 0 (1,2,1), 1 (2,2,0), 2 (0,2,2),
 // 3 (0,0,0) — the coefficient triples of reactionDiffusion.cu:162-169.
@@ -305,10 +371,17 @@ __device__ __forceinline__ void pattern_weights(uint32_t pat, float &wlo,
   wc = pat == 3u ? 0.f : 2.f;
 }
 
+// FK3V update of 4 consecutive cells (u[k], with west/east neighbours uw,
+// ue and the rows above/below un, us). plain: all four cells tissue with
+// tissue neighbours; else `code` holds the four hole codes (byte k: bit 0
+// tissue, bits 1-2 x pattern, bits 3-4 y pattern) and cells outside tissue
+// are set to 0. c: a's coefficients as lane pairs (FkPairsAt or FkPairs).
+template <class CP>
 __device__ __forceinline__ void fk3v_cells4(const StepCoeffs<float> &a,
-                                            bool plain, uint32_t code,
-                                            const float (&u)[4], float uw,
-                                            float ue, const float (&un)[4],
+                                            const CP &c, bool plain,
+                                            uint32_t code, const float (&u)[4],
+                                            float uw, float ue,
+                                            const float (&un)[4],
                                             const float (&us)[4],
                                             const float (&v)[4],
                                             const float (&w)[4],
@@ -316,9 +389,9 @@ __device__ __forceinline__ void fk3v_cells4(const StepCoeffs<float> &a,
                                             float (&ow)[4]) {
   F2 D01, D23;
   if (plain) {
-    D01 = lap5_2(a, f2(uw, u[0]), f2(u[0], u[1]), f2(u[1], u[2]),
+    D01 = lap5_2(c, f2(uw, u[0]), f2(u[0], u[1]), f2(u[1], u[2]),
                  f2(un[0], un[1]), f2(us[0], us[1]));
-    D23 = lap5_2(a, f2(u[1], u[2]), f2(u[2], u[3]), f2(u[3], ue),
+    D23 = lap5_2(c, f2(u[1], u[2]), f2(u[2], u[3]), f2(u[3], ue),
                  f2(un[2], un[3]), f2(us[2], us[3]));
   } else {
     float du[4];
@@ -337,12 +410,12 @@ __device__ __forceinline__ void fk3v_cells4(const StepCoeffs<float> &a,
     D23 = f2(du[2], du[3]);
   }
   F2 un2, vn2, wn2;
-  fk3v_update2(a, f2(u[0], u[1]), f2(v[0], v[1]), f2(w[0], w[1]), D01, un2,
+  fk3v_update2(c, f2(u[0], u[1]), f2(v[0], v[1]), f2(w[0], w[1]), D01, un2,
                vn2, wn2);
   f2_split(un2, ou[0], ou[1]);
   f2_split(vn2, ov[0], ov[1]);
   f2_split(wn2, ow[0], ow[1]);
-  fk3v_update2(a, f2(u[2], u[3]), f2(v[2], v[3]), f2(w[2], w[3]), D23, un2,
+  fk3v_update2(c, f2(u[2], u[3]), f2(v[2], v[3]), f2(w[2], w[3]), D23, un2,
                vn2, wn2);
   f2_split(un2, ou[2], ou[3]);
   f2_split(vn2, ov[2], ov[3]);
@@ -352,6 +425,18 @@ __device__ __forceinline__ void fk3v_cells4(const StepCoeffs<float> &a,
     for (int k = 0; k < 4; ++k)
       if (((code >> (8 * k)) & 1u) == 0u) ou[k] = ov[k] = ow[k] = 0.f;
   }
+}
+__device__ __forceinline__ void fk3v_cells4(const StepCoeffs<float> &a,
+                                            bool plain, uint32_t code,
+                                            const float (&u)[4], float uw,
+                                            float ue, const float (&un)[4],
+                                            const float (&us)[4],
+                                            const float (&v)[4],
+                                            const float (&w)[4],
+                                            float (&ou)[4], float (&ov)[4],
+                                            float (&ow)[4]) {
+  fk3v_cells4(a, FkPairsAt{a}, plain, code, u, uw, ue, un, us, v, w, ou, ov,
+              ow);
 }
 
 // New u, v, w of one cell from its scaled Laplacian du: the FP32 FK3V
