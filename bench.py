@@ -338,7 +338,8 @@ def run_reference(args, wl):
     print(json.dumps(line), flush=True)
 
 
-def batch_measure(nsteps, solves, warmup, dist, world, loops=True):
+def batch_measure(nsteps, solves, warmup, dist, world, loops=True,
+                  engine="auto"):
     """The batched workload (fk_batch_256: 256 FK3V grids of 128^2 .. 768^2,
     `nsteps` steps): the batched solver (schedule autotuned on the initial
     state), then, with `loops`, a loop of single-grid solvers on one shared
@@ -367,7 +368,11 @@ def batch_measure(nsteps, solves, warmup, dist, world, loops=True):
         b.synchronize()
 
     restore()
-    tuned = b.autotune(256)
+    if engine == "auto":
+        tuned = b.autotune(256)
+    else:  # the wavefront engine with that many CTAs per instance
+        b.set_wave(int(engine[4:]))
+        tuned = (0, int(engine[4:]), 0)
     for _ in range(warmup):
         restore()
         b.run(bw.nsteps, events())
@@ -409,6 +414,24 @@ def batch_measure(nsteps, solves, warmup, dist, world, loops=True):
     e2e = {"value": round(job_value(bw.cells, bw.nsteps, solves, world, e2e_s), 3),
            "unit": METRIC, "h2d_bytes_per_step": 12 * bw.cells,
            "d2h_bytes_per_step": 4 * bw.cells}
+    # the wavefront engine (one persistent launch per solve) beside the
+    # autotuner's pick: a warm-up solve, then a timed one, per cluster size
+    wave = {}
+    if engine == "auto" and loops:
+        for cl in (1, 2):
+            b.set_wave(cl)
+            restore()
+            b.run(bw.nsteps, events())
+            restore()
+            ev = events()
+            l0 = b.launch_count()
+            t0 = time.perf_counter()
+            b.run(bw.nsteps, ev)
+            b.synchronize()
+            dt = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
+            wave["cta_per_instance_%d" % cl] = {
+                "value": round(job_value(bw.cells, bw.nsteps, 1, world, dt), 3),
+                "gpu_launches_per_solve": b.launch_count() - l0}
     b.close()
     del dev0, hst, outs
     torch.cuda.empty_cache()
@@ -442,16 +465,25 @@ def batch_measure(nsteps, solves, warmup, dist, world, loops=True):
                                        max_over_ranks(sec_l, dist, "cuda")), 3)
     return {"bw": bw, "value": value, "sec": sec, "solves": solves,
             "tuned": tuned, "launches": launches, "clocks": clk, "e2e": e2e,
-            "loops": lp}
+            "loops": lp, "wave": wave}
 
 
 def batch_config(bw, tuned, world):
+    if tuned[2] == 0:
+        sched = ("wavefront engine: one persistent launch per solve, %d CTA(s) "
+                 "per instance" % tuned[1])
+    else:
+        sched = ("autotuned: groups of ~%d cells on %d streams, %d steps per "
+                 "launch" % tuned[:3])
     return {"workload": bw.name, "instances": len(bw.instances),
             "cells": bw.cells, "steps_per_solve": bw.nsteps,
             "sizes": "n ~ U{128,160,...,768}, square",
-            "schedule": "autotuned: groups of ~%d cells on %d streams, %d "
-                        "steps per launch" % tuned[:3],
-            "parallelism": "replicas x%d" % world}
+            "schedule": sched, "parallelism": "replicas x%d" % world}
+
+
+WAVE_NOTE = ("the wavefront engine (rd_batch_wave_kernel): every instance "
+             "on a cluster of CTAs, K steps per pass in shared memory, one "
+             "launch per solve; timed beside the autotuner's pick")
 
 
 def batch_summary(r):
@@ -462,6 +494,8 @@ def batch_summary(r):
            "solves_timed": r["solves"], "e2e": r["e2e"],
            "gpu_launches_per_solve": round(r["launches"] / r["solves"], 1),
            "loop_baselines": dict(lp, unit=METRIC)}
+    if r["wave"]:
+        out["wave_engine"] = dict(r["wave"], unit=METRIC, note=WAVE_NOTE)
     for k, v in lp.items():
         out["x_vs_" + k] = round(r["value"] / v, 3) if v else None
     return out
@@ -477,7 +511,8 @@ def run_batch(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device(
             "cuda", env_int("LOCAL_RANK", 0)))
-    r = batch_measure(args.nsteps, args.steps, args.warmup, dist, world)
+    r = batch_measure(args.nsteps, args.steps, args.warmup, dist, world,
+                      engine=args.batch_engine)
     if rank == 0:
         peak, peak_kind = measured_peaks()
         value = r["value"]
@@ -501,6 +536,8 @@ def run_batch(args):
                                         "(step engine, graphs)"),
             "gpu_launches": int(r["launches"]), "clocks": r["clocks"],
         }
+        if r["wave"]:
+            line["wave_engine"] = dict(r["wave"], unit=METRIC, note=WAVE_NOTE)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -1257,6 +1294,11 @@ def main():
     ap.add_argument("--grid", type=int, default=1024,
                     help="grid side (1024 = the benchmark; larger sides are "
                          "for profiling beyond the L2, holes scaled by area)")
+    ap.add_argument("--batch-engine", default="auto",
+                    choices=["auto", "wave1", "wave2", "wave4"],
+                    help="batch256: the autotuner's pick (and the wavefront "
+                         "engine timed beside it), or the wavefront engine "
+                         "with 1, 2 or 4 CTAs per instance alone")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--out", default=None,
                     help="spiral256: directory for the final state and the "

@@ -60,6 +60,28 @@ def test_resident_equals_step_engine(nx, ny, holes):
         assert d <= 1e-6, (f, d)
 
 
+@pytest.mark.parametrize("nx,ny,nholes", [(1024, 1024, 300), (256, 304, 400), (128, 300, 60)])
+def test_resident_split_passes_are_bitwise_the_step_engine(nx, ny, nholes):
+    # FK3V with holes runs the plain quads and the hole quads in separate
+    # passes (the hole quads listed per block, rows 0 and R-1 first): the
+    # same bits as the step engine, with holes on the blocks' boundary rows,
+    # dense hole masks and stimulus events inside the run
+    rng = np.random.default_rng(nholes)
+    p, fk = A.fk_tissue_params(nx, ny), A.fk_defaults()
+    u, v, w = W._ic(nx, ny, rng)
+    solid = W.hole_mask(nx, ny, nholes, 2.0, 7.0, rng)
+    p.solidSwitch = True
+    for f in (u, v, w):
+        f[solid == 0] = 0.0
+    stims = [W.stim(17, 0, 0, nx // 2, ny // 2), W.stim(60, nx // 3, 5, nx, ny // 3, 0.6)]
+    st = [u, v, w]
+    a, _, _ = run(p, fk, A.YH_MODEL_FK3V, st, solid, 150, A.YH_ENGINE_STEP, stims)
+    b, _, nl = run(p, fk, A.YH_MODEL_FK3V, st, solid, 150, A.YH_ENGINE_RESIDENT, stims)
+    assert nl == 1
+    for f in range(3):
+        assert np.array_equal(a[f], b[f]), f
+
+
 def test_resident_ref2v_without_gate_diffusion():
     p, fk, st, solid = case(160, 130, True, model=A.YH_MODEL_REF2V)
     a, _, _ = run(p, fk, A.YH_MODEL_REF2V, st, solid, 200, A.YH_ENGINE_STEP)
