@@ -472,6 +472,10 @@ def batch_config(bw, tuned, world):
     if tuned[2] == 0:
         sched = ("wavefront engine: one persistent launch per solve, %d CTA(s) "
                  "per instance" % tuned[1])
+    elif tuned[0] == 0:
+        sched = ("autotuned: every instance its own sequence of single-grid "
+                 "launches (64-step graphs, %d step(s) per launch), on %d "
+                 "streams" % (tuned[2], tuned[1]))
     else:
         sched = ("autotuned: groups of ~%d cells on %d streams, %d steps per "
                  "launch" % tuned[:3])

@@ -567,7 +567,11 @@ int yh_batch_run(yh_batch *b, int nsteps, const yh_batch_stim *stims,
                  int nstims);
 /* Schedule of later runs: groups of about group_cells cells (largest
  * instances first) on `streams` internal streams (1-64). The default is
- * 1,048,576 cells on 2 streams. */
+ * 1,048,576 cells on 2 streams. group_cells 0: every instance runs its own
+ * sequence of single-grid launches (the step engine's kernels, one or, at
+ * depth 2, two steps per launch, the instance's coefficients in the kernel
+ * parameters, 64-step graphs per instance), the instances spread over the
+ * streams so that large and small ones run together. */
 int yh_batch_set_schedule(yh_batch *b, long long group_cells, int streams);
 /* Steps per launch: 1 (the default) or 2 (64 x 16 tiles, inputs staged by
  * TMA bulk tensor copies, the same bits; YH_EUNSUPPORTED unless every
@@ -594,12 +598,15 @@ int yh_batch_get_wave(yh_batch *b, int *cluster, int *max_levels,
                       int *clusters);
 /* The schedule autotuner: times probe_steps steps (rounded up to even, no
  * events) of every schedule of groups of 256 K, 512 K, 1 M or 2 M cells
- * on 2, 3 or 4 streams at depth 1 and (where supported) 2, and of the
- * wavefront engine with 1, 2 and 4 CTAs per instance, on the current
- * state, keeps the fastest and restores the state and the step count. The
- * choice is returned in *group_cells, *streams and *depth (any may be
- * NULL); the wavefront engine reports *depth 0, *streams = CTAs per
- * instance and *group_cells 0. */
+ * on 2, 3 or 4 streams at depth 1 and (where supported) 2, of one launch
+ * sequence per instance on 6, 8 or 12 streams at depth 1 and 2, and of the
+ * wavefront engine
+ * with 1, 2 and 4 CTAs per instance, on the current state, keeps the
+ * fastest and restores the state and the step count. The choice is
+ * returned in *group_cells, *streams and *depth (any may be NULL): one
+ * sequence per instance reports *group_cells 0 and *depth 1 or 2, the
+ * wavefront engine *depth 0, *streams = CTAs per instance and *group_cells
+ * 0. */
 int yh_batch_autotune(yh_batch *b, int probe_steps, long long *group_cells,
                       int *streams, int *depth);
 int yh_batch_get_step(yh_batch *b, int *step);

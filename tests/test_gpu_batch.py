@@ -84,12 +84,14 @@ def test_batch_equals_the_single_grid_solver_bitwise():
 
 
 @pytest.mark.parametrize("depth", [1, 2])
-@pytest.mark.parametrize("schedule", [(1 << 12, 3), (1, 4), (1 << 30, 1)])
+@pytest.mark.parametrize("schedule", [(1 << 12, 3), (1, 4), (1 << 30, 1),
+                                      (0, 3), (0, 8)])
 def test_every_schedule_gives_the_same_bits(schedule, depth):
     # groups of one instance up to one group for all, on 1-4 streams, one or
     # two steps per launch (depth 2: TMA-staged 64 x 16 tiles; runs of odd
     # length and events on either step of a launch, including two events
-    # on one step)
+    # on one step); group_cells 0: every instance its own sequence of
+    # single-grid step launches (events by the stimulus kernel)
     insts = _instances()
     runs = [130, 170]
     b = Batch([w.p for w in insts], [w.fk for w in insts],
@@ -110,12 +112,12 @@ def test_every_schedule_gives_the_same_bits(schedule, depth):
     b.close()
 
 
-def _ragged_instances(seed=7):
+def _ragged_instances(seed=7, shapes=((36, 40), (100, 52), (44, 70), (52, 5),
+                                      (100, 130))):
     """Widths that split unevenly into bands of quads (nx / 4 = 9, 25, 11,
     13) and are no multiple of 16, heights from 5 rows up, holes in two,
     events on both runs (one on the first step of a run, two on one step)."""
     rng = np.random.default_rng(seed)
-    shapes = [(36, 40), (100, 52), (44, 70), (52, 5), (100, 130)]
     out = []
     for k, (nx, ny) in enumerate(shapes):
         p = A.fk_tissue_params(nx, ny, D=float(rng.uniform(5e-4, 1.5e-3)))
@@ -165,6 +167,34 @@ def test_wavefront_engine_gives_the_same_bits(cluster, levels, which):
         ref = _single(wl, runs)
         for f in range(3):
             assert np.array_equal(got[f], ref[f]), (cluster, levels, k, f)
+    b.close()
+
+
+@pytest.mark.parametrize("depth", [1, 2])
+def test_per_instance_schedule_on_ragged_grids(depth):
+    # every instance its own launch sequence (depth 2: the two-step
+    # kernel; widths with and without 16-byte rows of hole codes), events
+    # cutting the runs at odd and even steps: the same bits as single grids
+    # (depth 2 needs 16-byte rows of hole codes: the grids with holes are
+    # 96 and 112 wide there)
+    insts = _ragged_instances() if depth == 1 else _ragged_instances(
+        shapes=((36, 40), (96, 52), (44, 70), (52, 5), (112, 130)))
+    runs = [131, 70, 99]
+    b = Batch([w.p for w in insts], [w.fk for w in insts],
+              [w.solid for w in insts])
+    b.set_schedule(0, 3)
+    b.set_depth(depth)
+    for k, w in enumerate(insts):
+        b.set_state(k, *w.state0())
+    ev = [(k, st) for k, w in enumerate(insts) for st in w.stims]
+    for n in runs:
+        b.run(n, ev)
+    b.synchronize()
+    for k, wl in enumerate(insts):
+        got = b.get_state(k)
+        ref = _single(wl, runs)
+        for f in range(3):
+            assert np.array_equal(got[f], ref[f]), (depth, k, f)
     b.close()
 
 
@@ -242,6 +272,8 @@ def test_autotune_restores_the_state_and_keeps_the_bits():
     g, q, d = b.autotune(64)
     if d == 0:  # the wavefront engine, q CTAs per instance
         assert g == 0 and q in (1, 2, 4) and b.wave()[0] == q
+    elif g == 0:  # one launch sequence per instance on q streams
+        assert q in (6, 8, 12) and d in (1, 2) and b.wave()[0] == 0
     else:
         assert g in (1 << 18, 1 << 19, 1 << 20, 1 << 21) and q in (2, 3, 4)
         assert d in (1, 2) and b.wave()[0] == 0

@@ -87,14 +87,17 @@ class Batch:
             self.h, int(nsteps), arr, len(stims)))
 
     def set_schedule(self, group_cells, streams):
-        """Groups of about group_cells cells on `streams` internal streams."""
+        """Groups of about group_cells cells on `streams` internal streams
+        (group_cells 0: every instance its own sequence of single-grid step
+        launches, the instances spread over the streams)."""
         check("yh_batch_set_schedule", self.lib.yh_batch_set_schedule(
             self.h, int(group_cells), int(streams)))
 
     def autotune(self, probe_steps=256):
         """Times the schedules on the current state (restored), keeps the
-        fastest; returns (group_cells, streams, steps per launch), or
-        (0, CTAs per instance, 0) for the wavefront engine."""
+        fastest; returns (group_cells, streams, steps per launch):
+        (0, streams, 1) for one launch sequence per instance, (0, CTAs per
+        instance, 0) for the wavefront engine."""
         g, q, d = C.c_longlong(), C.c_int(), C.c_int()
         check("yh_batch_autotune", self.lib.yh_batch_autotune(
             self.h, int(probe_steps), C.byref(g), C.byref(q), C.byref(d)))
