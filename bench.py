@@ -370,6 +370,10 @@ def batch_measure(nsteps, solves, warmup, dist, world, loops=True,
     restore()
     if engine == "auto":
         tuned = b.autotune(256)
+    elif engine == "instance":  # one two-step launch sequence per instance
+        b.set_schedule(0, 8)
+        b.set_depth(2)
+        tuned = (0, 8, 2)
     else:  # the wavefront engine with that many CTAs per instance
         b.set_wave(int(engine[4:]))
         tuned = (0, int(engine[4:]), 0)
@@ -1299,10 +1303,11 @@ def main():
                     help="grid side (1024 = the benchmark; larger sides are "
                          "for profiling beyond the L2, holes scaled by area)")
     ap.add_argument("--batch-engine", default="auto",
-                    choices=["auto", "wave1", "wave2", "wave4"],
+                    choices=["auto", "instance", "wave1", "wave2", "wave4"],
                     help="batch256: the autotuner's pick (and the wavefront "
-                         "engine timed beside it), or the wavefront engine "
-                         "with 1, 2 or 4 CTAs per instance alone")
+                         "engine timed beside it), one two-step launch "
+                         "sequence per instance on 8 streams, or the "
+                         "wavefront engine with 1, 2 or 4 CTAs per instance")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--out", default=None,
                     help="spiral256: directory for the final state and the "
