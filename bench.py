@@ -403,17 +403,16 @@ def batch_measure(nsteps, solves, warmup, dist, world, loops=True,
     sec = max_over_ranks(sec, dist, "cuda")
     value = job_value(bw.cells, bw.nsteps, solves, world, sec)
 
-    # end to end: host buffers in, u of every grid out, every solve
+    # end to end: host buffers in, u of every grid out, every solve, through
+    # yh_batch_run_host (each instance's copies on its own stream under the
+    # per-instance schedule)
     hst = [[torch.tensor(x).pin_memory() for x in w.state0()] for w in insts]
-    outs = [torch.empty(w.cells, dtype=torch.float32).pin_memory() for w in insts]
+    outs = [(torch.empty(w.cells, dtype=torch.float32).pin_memory(), None, None)
+            for w in insts]
     b.synchronize()
     t0 = time.perf_counter()
     for _ in range(solves):
-        for k in range(len(insts)):
-            lib.yh_batch_set_state(b.h, k, *[C.c_void_p(x.data_ptr()) for x in hst[k]])
-        b.run(bw.nsteps, events())
-        for k in range(len(insts)):
-            lib.yh_batch_get_state(b.h, k, C.c_void_p(outs[k].data_ptr()), None, None)
+        b.run_host(bw.nsteps, hst, outs, events())
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
     e2e = {"value": round(job_value(bw.cells, bw.nsteps, solves, world, e2e_s), 3),
            "unit": METRIC, "h2d_bytes_per_step": 12 * bw.cells,

@@ -565,6 +565,20 @@ int yh_batch_state_device(yh_batch *b, int k, yh_fields *cur);
  * order given. */
 int yh_batch_run(yh_batch *b, int nsteps, const yh_batch_stim *stims,
                  int nstims);
+/* yh_batch_run with the states in host memory: instance k's state is
+ * copied in from u_in[k], v_in[k], w_in[k] before its first step and its
+ * result out to u_out[k], v_out[k], w_out[k] after its last (any of the six
+ * arrays, or any entry, may be NULL: that field is not copied), and the
+ * call returns when the outputs are written. Under the per-instance
+ * schedule (yh_batch_set_schedule with group_cells 0) every instance's
+ * copies run on its own stream beside the other instances' steps (pinned
+ * host memory lets them overlap); the other schedules copy on the caller's
+ * stream before and after the run. */
+int yh_batch_run_host(yh_batch *b, int nsteps, const yh_batch_stim *stims,
+                      int nstims, const float *const *u_in,
+                      const float *const *v_in, const float *const *w_in,
+                      float *const *u_out, float *const *v_out,
+                      float *const *w_out);
 /* Schedule of later runs: groups of about group_cells cells (largest
  * instances first) on `streams` internal streams (1-64). The default is
  * 1,048,576 cells on 2 streams. group_cells 0: every instance runs its own

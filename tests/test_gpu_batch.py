@@ -198,6 +198,46 @@ def test_per_instance_schedule_on_ragged_grids(depth):
     b.close()
 
 
+@pytest.mark.parametrize("schedule", ["instance", "grouped", "wave"])
+def test_run_host_copies_in_and_out(schedule):
+    # states from host memory in, results out, one call: under every
+    # schedule the same bits as set_state + run + get_state; five events of
+    # one instance inside the run make two segments (copies in before the
+    # first, out after the last)
+    insts = _instances()
+    insts[3].stims = [W.stim(10 + 9 * q, q, q, q + 10, q + 12, 1.0 - 0.1 * q)
+                      for q in range(7)]
+    ev = [(k, st) for k, w in enumerate(insts) for st in w.stims]
+    b = Batch([w.p for w in insts], [w.fk for w in insts],
+              [w.solid for w in insts])
+    if schedule == "instance":
+        b.set_schedule(0, 3)
+        b.set_depth(2)
+    elif schedule == "wave":
+        b.set_wave(2, 5)
+    b.run(20, ev)  # some other state in the batch first
+    states = [tuple(np.ascontiguousarray(x) for x in w.state0()) for w in insts]
+    outs = [tuple(np.empty(w.cells, np.float32) for _ in range(3)) for w in insts]
+    outs[2] = (outs[2][0], None, outs[2][2])  # a field not copied out
+    step0 = b.step_count()
+    b.run_host(101, states, outs, ev)
+    assert b.step_count() == step0 + 101
+    for k, wl in enumerate(insts):
+        m = Monodomain(wl.p, wl.model, wl.fk, solid=wl.solid)
+        m.set_engine(A.YH_ENGINE_STEP, 1)
+        m.set_state(*wl.state0())
+        m.set_step(step0)
+        m.run(101, wl.stims)
+        ref = m.get_state()
+        m.close()
+        got = b.get_state(k)
+        for f in range(3):
+            assert np.array_equal(got[f], ref[f]), (schedule, k, f)
+            if outs[k][f] is not None:
+                assert np.array_equal(outs[k][f], ref[f]), (schedule, k, f)
+    b.close()
+
+
 def test_wavefront_engine_segments_and_switches_back():
     # 7 events of one instance split the run into segments (a launch each);
     # the grouped launches and the wavefront engine continue each other's

@@ -86,6 +86,8 @@ SIGNATURES = {
     "yh_batch_get_state": (_i, [_v, _i, _v, _v, _v]),
     "yh_batch_state_device": (_i, [_v, _i, _P(A.Fields)]),
     "yh_batch_run": (_i, [_v, _i, _P(A.BatchStim), _i]),
+    "yh_batch_run_host": (_i, [_v, _i, _P(A.BatchStim), _i, _P(_v), _P(_v),
+                               _P(_v), _P(_v), _P(_v), _P(_v)]),
     "yh_batch_set_schedule": (_i, [_v, C.c_longlong, _i]),
     "yh_batch_autotune": (_i, [_v, _i, _P(C.c_longlong), _P(_i), _P(_i)]),
     "yh_batch_set_depth": (_i, [_v, _i]),

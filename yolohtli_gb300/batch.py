@@ -86,6 +86,33 @@ class Batch:
         check("yh_batch_run", self.lib.yh_batch_run(
             self.h, int(nsteps), arr, len(stims)))
 
+    def run_host(self, nsteps, states_in=None, states_out=None, stims=()):
+        """run() with the states in host memory: states_in[k] = (u, v, w)
+        arrays (or None) copied into instance k before its first step,
+        states_out[k] = (u, v, w) float32 arrays (or None) filled with its
+        result; under the per-instance schedule every instance's copies run
+        on its own stream beside the others' steps (pinned arrays, e.g.
+        torch's pin_memory(), let them overlap). Returns when the outputs
+        are written."""
+        n = self.count
+        arr = (A.BatchStim * max(1, len(stims)))()
+        for q, (k, s) in enumerate(stims):
+            arr[q].instance = k
+            arr[q].s = s
+
+        def table(states, f):
+            t = (C.c_void_p * n)()
+            if states is not None:
+                for k in range(n):
+                    if states[k] is not None and states[k][f] is not None:
+                        x = states[k][f]
+                        t[k] = x.data_ptr() if hasattr(x, "data_ptr") else x.ctypes.data
+            return t
+        ins = [table(states_in, f) for f in range(3)]
+        outs = [table(states_out, f) for f in range(3)]
+        check("yh_batch_run_host", self.lib.yh_batch_run_host(
+            self.h, int(nsteps), arr, len(stims), *ins, *outs))
+
     def set_schedule(self, group_cells, streams):
         """Groups of about group_cells cells on `streams` internal streams
         (group_cells 0: every instance its own sequence of single-grid step

@@ -621,6 +621,11 @@ struct yh_batch {
   bool per_inst = false;
   std::vector<cudaGraphExec_t> igraphs;
   std::vector<int> iorder, istream;  // launch order and each one's stream
+  // yh_batch_run_host: per-instance host arrays copied in before the first
+  // segment's steps and out after the last one's (nullptr: none), on each
+  // instance's stream under the per-instance schedule
+  const float *const *hin[3] = {nullptr, nullptr, nullptr};
+  float *const *hout[3] = {nullptr, nullptr, nullptr};
   // the wavefront engine (0: off; else CTAs per instance) and its plan:
   // instances by cluster (d_wlist[d_wbeg[c] .. d_wbeg[c + 1]))
   int wave = 0;
@@ -1151,6 +1156,12 @@ int run_segment_inst(yh_batch *b, int len) {
     const BatchInst &I = b->inst[k];
     int lvl = b->cur, step = b->step;
     const int end = b->step + len;
+    const size_t bytes = b->cells[k] * sizeof(float);
+    for (int f = 0; f < 3 && e == cudaSuccess; ++f)
+      if (b->hin[f] && b->hin[f][k])
+        e = cudaMemcpyAsync(inst_level(b, k, lvl).f[f], b->hin[f][k], bytes,
+                            cudaMemcpyDefault, s);
+    if (e != cudaSuccess) return st(e);
     while (step < end) {
       int next = end;  // the first event step after `step`
       for (int v = 0; v < I.nev && e == cudaSuccess; ++v) {
@@ -1179,6 +1190,11 @@ int run_segment_inst(yh_batch *b, int len) {
       step += left;
       if (e != cudaSuccess) return st(e);
     }
+    for (int f = 0; f < 3 && e == cudaSuccess; ++f)
+      if (b->hout[f] && b->hout[f][k])
+        e = cudaMemcpyAsync(b->hout[f][k], inst_level(b, k, lvl).f[f], bytes,
+                            cudaMemcpyDefault, s);
+    if (e != cudaSuccess) return st(e);
   }
   for (int q = 0; q < b->nstreams && e == cudaSuccess; ++q) {
     e = cudaEventRecord(b->joins[q], b->streams[q]);
@@ -1440,8 +1456,52 @@ extern "C" int yh_batch_state_device(yh_batch *b, int k, yh_fields *cur) {
   return YH_OK;
 }
 
+namespace {
+// Copies every instance's host arrays h[f][k] into (in) or out of the
+// current level on the caller's stream.
+int copy_states(yh_batch *b, const float *const *const *hin,
+                float *const *const *hout) {
+  const Fld<float> f = level(b, b->cur);
+  for (int k = 0; k < b->count; ++k)
+    for (int q = 0; q < 3; ++q) {
+      const size_t n = b->cells[k] * sizeof(float);
+      cudaError_t e = cudaSuccess;
+      if (hin && hin[q] && hin[q][k])
+        e = cudaMemcpyAsync(f.f[q] + b->inst[k].off, hin[q][k], n,
+                            cudaMemcpyDefault, b->s);
+      if (e == cudaSuccess && hout && hout[q] && hout[q][k])
+        e = cudaMemcpyAsync(hout[q][k], f.f[q] + b->inst[k].off, n,
+                            cudaMemcpyDefault, b->s);
+      if (e != cudaSuccess) return st(e);
+    }
+  return YH_OK;
+}
+
+int batch_run(yh_batch *b, int nsteps, const yh_batch_stim *stims, int nstims,
+              const float *const *const *hin, float *const *const *hout);
+}  // namespace
+
 extern "C" int yh_batch_run(yh_batch *b, int nsteps, const yh_batch_stim *stims,
                             int nstims) {
+  return batch_run(b, nsteps, stims, nstims, nullptr, nullptr);
+}
+
+extern "C" int yh_batch_run_host(yh_batch *b, int nsteps,
+                                 const yh_batch_stim *stims, int nstims,
+                                 const float *const *u_in,
+                                 const float *const *v_in,
+                                 const float *const *w_in, float *const *u_out,
+                                 float *const *v_out, float *const *w_out) {
+  const float *const *hin[3] = {u_in, v_in, w_in};
+  float *const *hout[3] = {u_out, v_out, w_out};
+  int rc = batch_run(b, nsteps, stims, nstims, hin, hout);
+  if (rc == YH_OK) rc = st(cudaStreamSynchronize(b->s));
+  return rc;
+}
+
+namespace {
+int batch_run(yh_batch *b, int nsteps, const yh_batch_stim *stims, int nstims,
+              const float *const *const *hin, float *const *const *hout) {
   if (!b || nsteps < 0 || nstims < 0 || (nstims && !stims)) return YH_EINVAL;
   for (int k = 0; k < nstims; ++k)
     if (stims[k].instance < 0 || stims[k].instance >= b->count) return YH_EINVAL;
@@ -1489,11 +1549,37 @@ extern "C" int yh_batch_run(yh_batch *b, int nsteps, const yh_batch_stim *stims,
       had_events = k != next;
     }
     next = k;
+    // host arrays: copied by the instances' own streams under the
+    // per-instance schedule, else on the caller's stream around the run
+    const bool first = b->step == end - nsteps, last = seg_end == end;
+    const bool own = b->per_inst && !b->wave;
+    if (first && hin && !own) {
+      const int rc = copy_states(b, hin, nullptr);
+      if (rc) return rc;
+    }
+    for (int f = 0; f < 3; ++f) {
+      b->hin[f] = own && first && hin ? hin[f] : nullptr;
+      b->hout[f] = own && last && hout ? hout[f] : nullptr;
+    }
     const int rc = run_segment(b, seg_end - b->step);
+    for (int f = 0; f < 3; ++f) {
+      b->hin[f] = nullptr;
+      b->hout[f] = nullptr;
+    }
     if (rc) return rc;
+    if (last && hout && !own) {
+      const int rc2 = copy_states(b, nullptr, hout);
+      if (rc2) return rc2;
+    }
+  }
+  if (nsteps == 0 && (hin || hout)) {  // no segment: the copies alone
+    int rc = hin ? copy_states(b, hin, nullptr) : YH_OK;
+    if (!rc && hout) rc = copy_states(b, nullptr, hout);
+    return rc;
   }
   return YH_OK;
 }
+}  // namespace
 
 extern "C" int yh_batch_autotune(yh_batch *b, int probe_steps,
                                  long long *group_cells, int *streams,
