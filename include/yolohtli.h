@@ -531,12 +531,13 @@ int yh_space_apd(const yh_param_var *p, int count, const float *uold,
  * keeps its parameters in process-global __constant__ symbols
  * (main.cu:40-51), which rules out batching. Each instance of a batch has
  * its own grid size, parameters (D through rx/ry, the FK3V time constants),
- * hole mask and stimulus events. The instances are packed into groups small
- * enough to stay in the L2; a run advances each group by all its steps, one
- * kernel launch per step for the whole group (captured in CUDA graphs), the
- * groups spread over internal streams that fork from and join the caller's
- * stream. FK3V in FP32, the same cell update as the single-grid solver
- * (same bits); nx % 4 == 0. */
+ * hole mask and stimulus events. Three schedules advance them (the
+ * autotuner picks one): groups small enough to stay in the L2, each group
+ * by all the run's steps with one or two steps per launch; one launch
+ * sequence per instance (the single-grid kernels); or the wavefront engine,
+ * one persistent launch per run. Graphs and internal streams fork from and
+ * join the caller's stream. FK3V in FP32, the same cell update as the
+ * single-grid solver (same bits under every schedule); nx % 4 == 0. */
 typedef struct yh_batch yh_batch;
 
 /* A stimulus event of one instance of a batch. */

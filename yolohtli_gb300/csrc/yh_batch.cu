@@ -1,12 +1,12 @@
 // Batched solver (include/yolohtli.h, layer 3): many independent FK3V grids,
 // each with its own size, parameters, hole mask and stimulus events,
-// advanced together, one kernel launch per step for a whole group of them.
+// advanced together by one of three schedules (below).
 //
 // Layout: every instance's fields are a slice of three shared arrays
 // (u, v, w), each slice starting on a 256-byte boundary; the hole codes of
-// all instances are one byte array with the same offsets. A unit table
-// assigns each 256-thread block a tile of 8 float4 quads x 32 rows (32 x 32
-// cells) of one instance, so that the rows above and below a thread's quad
+// all instances are one byte array with the same offsets. In the grouped
+// kernels a unit table assigns each 256-thread block a tile of 8 float4
+// quads x 32 rows (32 x 32 cells) of one instance, so that the rows above and below a thread's quad
 // are mostly its tile's own (L1 reuse); the instance records (coefficients,
 // offsets, this run's events)
 // are copied into shared memory once per block. Stimulus events are applied
@@ -17,13 +17,21 @@
 // from a device word set before each graph replay plus the node's index.
 // The cell update is fk3v_cells4 of the single-grid kernels: same bits.
 //
-// Schedule: the instances are independent, so a run does not advance them
-// in lockstep. They are packed (largest first) into groups of about
-// `group_cells` cells, small enough that a group's two state levels stay in
-// the L2 for the whole run; each group runs all the run's steps as its own
-// sequence of launches (64-step graphs) on one of `streams` internal
-// streams, so several groups are in flight at once. The streams fork from
-// the caller's stream at the start of a run and join it at the end.
+// Schedules (the instances are independent, so a run does not advance them
+// in lockstep; every schedule gives the same bits):
+//   - grouped: the instances are packed (largest first) into groups of
+//     about `group_cells` cells, small enough that a group's two state
+//     levels stay in the L2 for the whole run; each group runs all the
+//     run's steps as its own sequence of launches (64-step graphs, one or
+//     two steps per launch) on one of `streams` internal streams;
+//   - per instance (group_cells 0): every instance runs the single-grid
+//     step or two-step kernel with its coefficients in the kernel
+//     parameters, 64-step graphs per instance, the instances spread over
+//     the streams so that large and small ones run together;
+//   - wavefront (yh_batch_set_wave): one persistent launch per run segment,
+//     an instance per cluster of CTAs, K steps per pass in shared memory.
+// The internal streams fork from the caller's stream at the start of a run
+// and join it at the end.
 #include <string.h>
 
 #include <algorithm>
