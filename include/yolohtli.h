@@ -462,6 +462,14 @@ int yh_sr_begin(yh_solver *h, int template_mode, const float *tu,
  * yh_get_sym's nsingular counts such solves since yh_sr_begin. Reads that
  * count back once per call (one stream synchronisation). */
 int yh_sr_step(yh_solver *h, int nsteps);
+/* yh_sr_step in two halves, for several handles driven from one thread (a
+ * sweep over parameters on several streams): yh_sr_enqueue enqueues the
+ * steps on the handle's stream and returns without waiting;
+ * yh_sr_status waits for the stream and returns YH_ESINGULAR when a
+ * solve since the last status read (by either call) found the system
+ * singular. */
+int yh_sr_enqueue(yh_solver *h, int nsteps);
+int yh_sr_status(yh_solver *h);
 int yh_get_sym(yh_solver *h, yh_sym_state *out);
 
 /* Steps taken so far, the clock that stimulus events are matched against.

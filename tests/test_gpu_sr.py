@@ -292,6 +292,37 @@ def sr_spiral_case(n=128, L=3.0, radius=30):
     return p, st
 
 
+def test_sr_enqueue_on_two_streams_equals_sr_step():
+    # two handles on their own streams, their steps enqueued one after the
+    # other without waiting (yh_sr_enqueue) and the status read at the end
+    # (yh_sr_status): each the same bits as a handle stepped by yh_sr_step
+    import torch
+    p, st = sr_spiral_case(n=96, L=2.25, radius=20)
+    ref = Monodomain(p, A.YH_MODEL_REF2V, None)
+    ref.set_state(*st)
+    ref.sr_begin()
+    for _ in range(3):
+        ref.sr_step(37)
+    want, wsym = ref.get_state(), ref.get_sym()
+    ref.close()
+    streams = [torch.cuda.Stream() for _ in range(2)]
+    hs = [Monodomain(p, A.YH_MODEL_REF2V, None, stream=s.cuda_stream) for s in streams]
+    for m in hs:
+        m.set_state(*st)
+        m.sr_begin()
+    for _ in range(3):
+        for m in hs:
+            m.sr_enqueue(37)
+    for m in hs:
+        m.sr_status()
+        got, gsym = m.get_state(), m.get_sym()
+        assert gsym.step == wsym.step == 111
+        assert list(gsym.c) == list(wsym.c) and list(gsym.phi) == list(wsym.phi)
+        for f in range(2):
+            assert np.array_equal(got[f], want[f]), f
+        m.close()
+
+
 def test_sr_frozen_template_trajectory_matches_oracle():
     """BASELINE-style symmetry reduction (template frozen at the start
     state) over 2,000 SR steps on 128^2: the FP32 product's c, phi and u

@@ -68,6 +68,8 @@ SIGNATURES = {
     "yh_get_tips": (_i, [_v, _P(A.Tip), _i, _P(_i)]),
     "yh_sr_begin": (_i, [_v, _i, _v, _v, _v]),
     "yh_sr_step": (_i, [_v, _i]),
+    "yh_sr_enqueue": (_i, [_v, _i]),
+    "yh_sr_status": (_i, [_v]),
     "yh_get_sym": (_i, [_v, _P(A.SymState)]),
     "yh_get_step": (_i, [_v, _P(_i)]),
     "yh_set_step": (_i, [_v, _i]),

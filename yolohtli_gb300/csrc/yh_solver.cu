@@ -726,9 +726,9 @@ static cudaError_t sr_body(yh_solver *h, int len) {
   return cudaSuccess;
 }
 
-extern "C" int yh_sr_step(yh_solver *h, int nsteps) {
-  if (!h || nsteps < 0) return YH_EINVAL;
-  if (!h->sr_ready) return YH_ENOTREADY;
+// The steps of yh_sr_step without the status read: enqueued on the
+// handle's stream, nothing waited for.
+static int sr_enqueue(yh_solver *h, int nsteps) {
   int left = nsteps;
   if (left > 0 && h->sr_step == 0) {
     cudaError_t e = enqueue_sr_step(h, true);
@@ -753,19 +753,39 @@ extern "C" int yh_sr_step(yh_solver *h, int nsteps) {
     h->sr_step += 1;
     h->step += 1;
   }
-  cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess && nsteps > 0) {
-    // the singular-solve count of the device state, read once per call
-    int ns = 0;
-    e = cudaMemcpyAsync(&ns, &h->sym->nsingular, sizeof(int),
-                        cudaMemcpyDeviceToHost, h->s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
-    if (e == cudaSuccess && ns != h->sr_nsingular) {
-      h->sr_nsingular = ns;
-      return YH_ESINGULAR;
-    }
+  return st(cudaGetLastError());
+}
+
+extern "C" int yh_sr_enqueue(yh_solver *h, int nsteps) {
+  if (!h || nsteps < 0) return YH_EINVAL;
+  if (!h->sr_ready) return YH_ENOTREADY;
+  return sr_enqueue(h, nsteps);
+}
+
+// Waits for the handle's stream and reads the singular-solve count of the
+// device state: YH_ESINGULAR when it grew since the last read.
+extern "C" int yh_sr_status(yh_solver *h) {
+  if (!h) return YH_EINVAL;
+  if (!h->sr_ready) return YH_ENOTREADY;
+  int ns = 0;
+  cudaError_t e = cudaMemcpyAsync(&ns, &h->sym->nsingular, sizeof(int),
+                                  cudaMemcpyDeviceToHost, h->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  if (e != cudaSuccess) return st(e);
+  if (ns != h->sr_nsingular) {
+    h->sr_nsingular = ns;
+    return YH_ESINGULAR;
   }
-  return st(e);
+  return YH_OK;
+}
+
+extern "C" int yh_sr_step(yh_solver *h, int nsteps) {
+  if (!h || nsteps < 0) return YH_EINVAL;
+  if (!h->sr_ready) return YH_ENOTREADY;
+  const int rc = sr_enqueue(h, nsteps);
+  if (rc || nsteps == 0) return rc;
+  // the singular-solve count of the device state, read once per call
+  return yh_sr_status(h);
 }
 
 extern "C" int yh_get_sym(yh_solver *h, yh_sym_state *out) {

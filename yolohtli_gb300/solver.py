@@ -204,6 +204,14 @@ class Monodomain:
     def sr_step(self, nsteps=1):
         check("yh_sr_step", self.lib.yh_sr_step(self.h, int(nsteps)))
 
+    def sr_enqueue(self, nsteps=1):
+        """sr_step without waiting: the steps are enqueued on the handle's
+        stream; sr_status() waits and reports a singular solve."""
+        check("yh_sr_enqueue", self.lib.yh_sr_enqueue(self.h, int(nsteps)))
+
+    def sr_status(self):
+        check("yh_sr_status", self.lib.yh_sr_status(self.h))
+
     def get_sym(self):
         s = A.SymState()
         check("yh_get_sym", self.lib.yh_get_sym(self.h, C.byref(s)))
