@@ -118,3 +118,41 @@ def test_invalid_arguments_are_rejected_without_a_gpu():
     q.solidSwitch = True  # holes requested without a mask
     assert lib.yh_create(C.byref(q), 0, None, None, None, C.byref(h)) == A.YH_EINVAL
     assert lib.yh_create(C.byref(p), 1, None, None, None, C.byref(h)) == A.YH_EINVAL
+
+
+C_PROGRAM = r"""
+#include <stdio.h>
+#include "yolohtli.h"
+int main(void) {
+  yh_param_var p;
+  int rc = yh_param_defaults(&p, 64, 48);
+  printf("%d %d %d %s\n", rc, p.nx, p.ny, yh_status_string(YH_EINVAL));
+  return rc;
+}
+"""
+
+
+def test_header_is_c_and_a_c_program_links_against_the_library(tmp_path):
+    # the C ABI as a C caller sees it: the header compiles as pedantic C99
+    # and as C++11, and a C program links against the library and calls its
+    # host-side functions (no GPU needed)
+    import shutil
+    import subprocess
+    import pytest
+    if shutil.which("gcc") is None or shutil.which("g++") is None:
+        pytest.skip("no C compiler")
+    inc = os.path.join(ROOT, "include")
+    src = tmp_path / "prog.c"
+    src.write_text(C_PROGRAM)
+    subprocess.check_call(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror",
+                           "-pedantic", "-fsyntax-only", "-I", inc, str(src)])
+    subprocess.check_call(["g++", "-std=c++11", "-Wall", "-Wextra", "-Werror",
+                           "-fsyntax-only", "-I", inc, "-x", "c++", str(src)])
+    libdir = os.path.dirname(load()._name)
+    exe = tmp_path / "prog"
+    subprocess.check_call(["gcc", "-std=c99", "-I", inc, str(src), "-o", str(exe),
+                           "-L", libdir, "-lyolohtli_gb300",
+                           "-Wl,-rpath," + libdir])
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True)
+    assert out.stdout.split()[:3] == ["0", "64", "48"]
+    assert "invalid" in out.stdout
